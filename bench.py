@@ -1,0 +1,344 @@
+#!/usr/bin/env python
+"""Benchmark of the MD hot path: velocity-Verlet steps of EAM Cu, fcc 63^3 =
+1,000,188 atoms (periodic, rc 5.0 A, skin 0.5 A, 300 K, dt 1 fs), in the
+mixed-precision form, on one GB300 per rank.
+
+One "step" = one MD step (drift + rebuild test, EAM density, EAM force, kick,
+and the neighbour-list rebuild whenever the half-skin test fires), the loop
+of the reference's drivers. Prints one JSON line (rank 0).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU oracle (the restated reference path) on this
+machine's host cores on the same workload. N>1 runs N independent replicas
+(one per GPU, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = ("EAM Cu fcc 63^3 = 1,000,188 atoms, periodic cube 22.77 nm, Finnis-Sinclair-type analytic tables "
+            "(5000-point splines), rc 5.0 A, skin 0.5 A, 1% jitter, 300 K, dt 1 fs")
+METRIC = "atom-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="mdg", choices=["mdg", "reference"])
+    ap.add_argument("--ncell", type=int, default=63)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--cpu-steps", type=int, default=6)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world, local):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as td
+            torch.cuda.set_device(local)
+            td.init_process_group("nccl")
+            self.td, self.torch = td, torch
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([x], device="cuda", dtype=self.torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([x], device="cuda", dtype=self.torch.float64)
+        self.td.all_reduce(t)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.device = device
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and "Active" in r[5 + k] and "Not" not in r[5 + k]:
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(ncell):
+    from mdcraft_gb300 import workloads as W
+    return W.eam_cu_fcc(ncell=ncell)
+
+
+def cpu_baseline(ncell, steps, threads=None):
+    """The CPU oracle (C restatement of the reference path, all host threads)
+    on the same workload: one list build, then `steps` timed driver steps."""
+    from oracle import mdref as R
+    atoms, box, _, p = make_workload(ncell)
+    threads = threads or R.hardware_threads()
+    ao = np.zeros(len(atoms), dtype=R.ATOM_DTYPE)
+    ao.view(np.uint8)[:] = atoms.view(np.uint8)
+    d = R.Domain(*box)
+    for k in range(3):
+        d.set_periodic(k, True)
+    t = p["tables"]
+    pot = R.EAM(t["rcut"], t["Femb"], t["Rho"], t["Vpar"], t["Nr1"], t["dr"], t["Nrh1"], t["drh"])
+    sol = R.Solver(pot, periodic=d, threads=threads)
+    nl = R.VerletList(ao, d, threads=threads)
+    nl.update(-1.0)
+    sol.prepare(ao)
+    sol.stages(ao, nl)
+    sol.run(ao, nl, d, p["dt"], 1)  # warm-up step
+    t0 = time.perf_counter()
+    rebuilds = sol.run(ao, nl, d, p["dt"], steps)
+    dt = time.perf_counter() - t0
+    return {"value": len(ao) * steps / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{len(ao)}-atom EAM Cu, {steps} timed Verlet steps after one list build "
+                      f"({rebuilds} rebuilds), {threads} threads", "seconds": dt}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import mdref as R
+    threads = R.hardware_threads()
+    # size the timed sample from one measured step: a few minutes at most
+    probe = cpu_baseline(args.ncell, 1, threads)
+    per_step = probe["seconds"]
+    steps = max(1, min(args.steps, int(90.0 / max(per_step, 1e-3))))
+    cb = cpu_baseline(args.ncell, steps, threads)
+    line = {"metric": METRIC, "value": cb["value"], "unit": METRIC, "n_gpus": args.gpus, "steps": steps,
+            "warmup": 2, "ms_per_step": 1e3 * cb["seconds"] / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "atoms": 4 * args.ncell ** 3, "threads": threads},
+            "impl": "reference",
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def run_mdg(args, rank, world, local):
+    import torch
+
+    import mdcraft_gb300 as mdg
+    from mdcraft_gb300 import build as B
+
+    B.build()
+    dist = Dist(world, local)
+    atoms, box, _, p = make_workload(args.ncell)
+    t = p["tables"]
+    n = len(atoms)
+    ctx = mdg.Context(local)
+    dom = mdg.Domain(*box)
+    for k in range(3):
+        dom.set_periodic(k, True)
+    sysg = mdg.System(ctx, dom, atoms)
+    nl = mdg.VerletList(sysg)
+    nl.update(-1.0)
+    pot = mdg.EAM(t["rcut"], t["Femb"], t["Rho"], t["Vpar"], t["Nr1"], t["dr"], t["Nrh1"], t["drh"])
+
+    # accuracy gate on the initial configuration: mixed vs FP64 forces
+    s64 = mdg.Single(pot, periodic=True, precision="fp64")
+    s64.prepare(sysg)
+    s64.stages(sysg)
+    f64 = sysg.forces()
+    smx = mdg.Single(pot, periodic=True, precision="mixed")
+    smx.prepare(sysg)
+    smx.stages(sysg)
+    fmx = sysg.forces()
+    dF = np.linalg.norm(fmx - f64, axis=1)
+    rms = np.sqrt(np.mean(np.sum(f64 ** 2, axis=1)))
+    err_l2 = float(np.linalg.norm(fmx - f64) / np.linalg.norm(f64))
+    err_max = float(dF.max() / rms)
+    off, _ = nl.csr()
+    L = float((off[-1] - n) / n)  # listed neighbours per atom, self excluded
+
+    # FP64 form throughput (same loop, FP64 stages)
+    st64 = mdg.Verlet(s64)
+    st64.run(sysg, p["dt"], 1)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    st64.run(sysg, p["dt"], args.fp64_steps)
+    ctx.synchronize()
+    fp64_rate = n * args.fp64_steps / (time.perf_counter() - t0)
+
+    # mixed form: warm-up, then K timed steps bracketed by events on the
+    # engine's stream
+    sysg.upload(atoms)
+    nl.update(-1.0)
+    smx.prepare(sysg)
+    smx.stages(sysg)
+    stepper = mdg.Verlet(smx)
+    stepper.run(sysg, p["dt"], args.warmup)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", local))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    ctx.synchronize()
+    ctx.set_timing(True)
+    rb0 = nl.rebuilds()
+    l0 = ctx.launches()
+    clocks = Clocks(local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0.record(stream)
+    stepper.run(sysg, p["dt"], args.steps)
+    e1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    dist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = ctx.launches() - l0
+    rebuilds = nl.rebuilds() - rb0
+    fms, fn = ctx.stage_time("forces")
+    dms, dn = ctx.stage_time("density")
+    drms, drn = ctx.stage_time("drift")
+    kms, kn = ctx.stage_time("kick")
+    rms_, rn = ctx.stage_time("rebuild")
+    ctx.set_timing(False)
+    ms_max = dist.max(ms)
+    total_atom_steps = dist.sum(float(n) * args.steps)
+    value = total_atom_steps / (ms_max / 1e3)
+
+    # end to end through the public API with pinned host buffers: each step
+    # uploads positions + velocities and downloads positions, velocities, forces
+    pos = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    vel = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    frc = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    pos[:] = sysg.positions()
+    vel[:] = sysg.velocities()
+    stepper.run_host(sysg, p["dt"], 1, pos, vel, frc)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        stepper.run_host(sysg, p["dt"], 1, pos, vel, frc)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = dist.sum(float(n) * args.e2e_steps) / e2e_s
+
+    # roofline of the dominant kernel (EAM force, mixed): compulsory bytes per
+    # atom = own offsets+F' (16) + list count (4) + list entries (4 L) + FP32 force (12)
+    bytes_atom = 32.0 + 4.0 * L
+    force_launch_ms = fms / max(fn, 1)
+    achieved = bytes_atom * n / (force_launch_ms / 1e3) / 1e9
+    pk = peaks()
+    peak = pk.get("hbm_gbs", 6800.0)
+    roof = {"bound": "hbm", "kernel": "k_eam_mixed (EAM force, mixed)", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
+            "bytes_per_atom": bytes_atom, "launch_ms": force_launch_ms}
+
+    if rank == 0:
+        cb = None
+        if not args.no_cpu and world == 1:
+            cb = cpu_baseline(args.ncell, args.cpu_steps)
+            cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "mixed: f32 pair math, f64 state",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "atoms": n, "precision": "mixed",
+                       "l2": f"inputs larger than L2 (~{n * 500 / 1e6:.0f} MB resident per replica)",
+                       "parallelism": f"replicas x{world}", "neighbours_per_atom": L},
+            "fp64_form": {"value": fp64_rate, "unit": METRIC, "mixed_speedup": value / world / fp64_rate},
+            "force_error": {"l2_rel": err_l2, "max_over_rms": err_max, "bar": 1e-5},
+            "rebuilds": rebuilds,
+            "stage_ms_per_launch": {"drift": drms / max(drn, 1), "density": dms / max(dn, 1),
+                                    "forces": force_launch_ms, "kick": kms / max(kn, 1),
+                                    "rebuild": rms_ / max(rn, 1)},
+            "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": n * 48, "d2h_bytes_per_step": n * 72},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "cpu_baseline": cb,
+            "clocks": ck,
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_mdg(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,218 @@
+/*
+ * mdg.h — C-ABI of the GB300-native MD step engine (libmdg.so).
+ *
+ * Drop-in boundary for MDcraft's per-step hot path on one periodic or open
+ * domain: linked-cell binning + Verlet list (mdcraft/neibs), LJsCut and
+ * two-pass EAM forces through the Single / Multi solvers with the Periodic
+ * boundary (mdcraft/solver), and velocity-Verlet (mdcraft/solver/stepper).
+ * Each entry point names the reference interface it replaces.
+ *
+ * Conventions
+ *  - Every function returns an int status: MDG_OK (0) or a negative MDG_ERR_*.
+ *    mdg_last_error() returns a message for the calling thread's last error.
+ *  - Units are MDcraft's: nm, ps, g/mol, kJ/mol.
+ *  - Atoms cross the boundary in MDcraft's 208-byte Atom layout
+ *    (mdcraft/data/atom.h:21-40) or as plain SoA double arrays, always in
+ *    the caller's atom order. Internally atoms are kept cell-sorted on the
+ *    device; indices returned by the API are caller indices.
+ *  - Calls on one system are stream-ordered on that system's context
+ *    stream; a handle may be used by one host thread at a time.
+ *  - There is no CPU fallback: creating a context without a usable CUDA
+ *    device fails with MDG_ERR_NODEV.
+ */
+#ifndef MDG_H
+#define MDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MDG_OK 0
+#define MDG_ERR_INVALID (-1)  /* bad argument or call order */
+#define MDG_ERR_NOMEM (-2)    /* device or host allocation failed */
+#define MDG_ERR_OVERFLOW (-3) /* neighbour capacity exceeded (internal retry failed) */
+#define MDG_ERR_RANGE (-4)    /* atom outside the grid, or table range (results flagged) */
+#define MDG_ERR_TIMEOUT (-5)  /* bounded device wait expired */
+#define MDG_ERR_CUDA (-6)     /* CUDA runtime error */
+#define MDG_ERR_STATE (-7)    /* object not ready (e.g. forces before a list) */
+#define MDG_ERR_NODEV (-8)    /* no CUDA device */
+#define MDG_ERR_IO (-9)       /* potential file could not be read */
+
+/* Arithmetic of the force stages. */
+#define MDG_PREC_FP64 0  /* reference arithmetic in FP64 (parity form) */
+#define MDG_PREC_MIXED 1 /* FP32 pair math, compensated FP32 sums, FP64 state */
+
+typedef struct mdg_ctx mdg_ctx;
+typedef struct mdg_system mdg_system;
+typedef struct mdg_potential mdg_potential;
+typedef struct mdg_solver mdg_solver;
+
+/* mdcraft::data::Atom, 208 bytes, V column-major (Eigen 3x3). */
+typedef struct mdg_atom {
+    double r[3];
+    double v[3];
+    double f[3];
+    double V[9];
+    double m, rcut, rns, Ep, Em, nc;
+    uint16_t bc, kind;
+    uint32_t uid;
+    uint16_t tag;
+    uint16_t _pad[3];
+} mdg_atom;
+
+/* mdcraft::lattice::Domain (mdcraft/lattice/domain.h:84-108):
+ * box [bmin, bmax] and per-axis periodic flags. */
+typedef struct mdg_domain {
+    double bmin[3];
+    double bmax[3];
+    int32_t periodic[3];
+} mdg_domain;
+
+/* Totals of the reference's measure_state (test/cxx/support/md_test_utils.h:214-239). */
+typedef struct mdg_state {
+    double Ep, Em, KE, Etot, virial;
+    double vcom[3];
+} mdg_state;
+
+const char* mdg_last_error(void);
+const char* mdg_version(void);
+
+/* ---- context ---------------------------------------------------------- */
+/* One CUDA device and one stream. No reference counterpart (the reference
+ * runs on host threads, mdcraft/tools/threads.h:28-221). */
+int mdg_ctx_create(int device, mdg_ctx** out);
+int mdg_ctx_destroy(mdg_ctx* ctx);
+int mdg_ctx_synchronize(mdg_ctx* ctx);
+/* The context's cudaStream_t (as void*), for callers that order their own
+ * work or timing events after the engine's. */
+int mdg_ctx_stream(mdg_ctx* ctx, void** stream);
+/* Kernels this context has launched since creation (bench bookkeeping). */
+int mdg_ctx_launch_count(mdg_ctx* ctx, uint64_t* out);
+/* Per-stage device timing with CUDA events on the context stream (no
+ * reference counterpart). While on, the step loop brackets each stage's
+ * kernel with events; mdg_ctx_stage_time sums their elapsed times.
+ * which: 0 drift, 1 density (EAM charge), 2 forces, 3 kick, 4 list rebuild. */
+#define MDG_TIME_DRIFT 0
+#define MDG_TIME_DENSITY 1
+#define MDG_TIME_FORCES 2
+#define MDG_TIME_KICK 3
+#define MDG_TIME_REBUILD 4
+int mdg_ctx_set_timing(mdg_ctx* ctx, int on);
+int mdg_ctx_stage_time(mdg_ctx* ctx, int which, double* total_ms, uint64_t* launches);
+
+/* ---- systems: device-resident atoms ------------------------------------ */
+/* Replaces the caller-owned `Atoms` vector + `Domain` pair that every
+ * reference class binds (mdcraft/data/atom.h:40, mdcraft/lattice/domain.h:84). */
+int mdg_system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n,
+                      mdg_system** out);
+int mdg_system_destroy(mdg_system* sys);
+int mdg_system_size(mdg_system* sys, size_t* n);
+/* Upload/download all fields in the 208-byte Atom layout, caller order. */
+int mdg_system_upload_atoms(mdg_system* sys, const mdg_atom* atoms, size_t n);
+int mdg_system_download_atoms(mdg_system* sys, mdg_atom* atoms, size_t n);
+/* SoA fast paths: xyz arrays are n*3 doubles, caller order. */
+int mdg_system_set_positions(mdg_system* sys, const double* xyz);
+int mdg_system_get_positions(mdg_system* sys, double* xyz);
+int mdg_system_set_velocities(mdg_system* sys, const double* xyz);
+int mdg_system_get_velocities(mdg_system* sys, double* xyz);
+int mdg_system_get_forces(mdg_system* sys, double* xyz);
+
+/* ---- Verlet list -------------------------------------------------------- */
+/* VerletList::update(kbuf) (mdcraft/neibs/verlet-list.cxx:41-55): wraps
+ * positions into the periodic box, rebuilds the linked-cell grid
+ * (grid.cxx:43-95) and the full (half=0) or half list, snapshots positions.
+ * kbuf > 0 first resets rns = kbuf * max(rcut_i + rcut_j) over the current
+ * list (verlet-list.cxx:72-92). Half lists are only exported, never used
+ * by the force stages (the reference rejects them with threads,
+ * verlet-list.cxx:27-32). Returns MDG_ERR_RANGE when an atom lies outside
+ * the grid (the reference indexes out of bounds there); the atom is clamped
+ * into the nearest cell. */
+int mdg_nlist_update(mdg_system* sys, double kbuf, int half);
+/* VerletList::decide (verlet-list.cxx:110-158): *need = 1 when a rebuild is
+ * due (size/uid/rcut/rns changed, or a half-skin displacement). */
+int mdg_nlist_decide(mdg_system* sys, int* need);
+/* Number of entries of the whole list, self entries included
+ * (verlet-list.cxx:345-348 lists each atom as its own neighbour). */
+int mdg_nlist_total(mdg_system* sys, size_t* total);
+/* VerletList::get() as CSR in caller order: offsets[n+1], idx[total]. Each
+ * atom's entries are sorted ascending (the set equals the reference's). */
+int mdg_nlist_export(mdg_system* sys, uint64_t* offsets, uint64_t* idx,
+                     size_t cap);
+/* VerletList::list_for(x) (verlet-list.cxx:251-276). */
+int mdg_nlist_list_for(mdg_system* sys, const double x[3], uint64_t* out,
+                       size_t cap, size_t* count);
+/* Grid geometry of the last rebuild (Grid members, grid.h:154-180):
+ * ints = {domain_num_cells[3], grid_offset[3], num_cells[3]},
+ * dbls = {cell_sizes[3]}. */
+int mdg_nlist_grid(mdg_system* sys, int32_t ints[9], double dbls[3]);
+/* Rebuilds performed by mdg_run / mdg_nlist_update since creation. */
+int mdg_nlist_rebuilds(mdg_system* sys, uint64_t* count);
+
+/* ---- potentials ----------------------------------------------------------- */
+/* LJsCut(a, s, rcut) (mdcraft/solver/potential/LJs-cut.h:15-19). */
+int mdg_pot_ljcut_create(double a, double s, double rcut, mdg_potential** out);
+/* EAM(rcut, Femb, Rho, Vpar, Nr1, dr, Nrh1, drh) (EAM.h:13-21): tables of
+ * F(rho), rho(r) and r*phi(r); knot slopes are built with the reference's
+ * tridiagonal sweep (EAM.cxx:603-686). */
+int mdg_pot_eam_create(double rcut, const double* Femb, const double* Rho,
+                       const double* Vpar, int Nr1, double dr, int Nrh1,
+                       double drh, mdg_potential** out);
+/* EAM(std::string filename) (EAM.cxx:55-87): single-element setfl file;
+ * unlike the reference, a missing or short file fails with MDG_ERR_IO. */
+int mdg_pot_eam_create_from_file(const char* path, mdg_potential** out);
+int mdg_pot_destroy(mdg_potential* pot);
+/* Base::rcut() (mdcraft/solver/potential/base.h:37). */
+int mdg_pot_rcut(mdg_potential* pot, double* rcut);
+
+/* ---- solvers ------------------------------------------------------------------- */
+/* Single(pot, boundary) (mdcraft/solver/single.h:37-42). periodic != 0
+ * selects boundary::Periodic(domain) (boundary/periodic.h:29), else the
+ * no-op boundary. */
+int mdg_solver_single(mdg_potential* pot, int periodic, mdg_solver** out);
+/* Multi(boundary, thermostat, nkinds) (mdcraft/solver/multi.h:42-47). */
+int mdg_solver_multi(int nkinds, int periodic, mdg_solver** out);
+/* Multi::add_potential(i, j, pot) (multi.cxx:28-49). */
+int mdg_solver_add_potential(mdg_solver* s, int i, int j, mdg_potential* pot);
+int mdg_solver_destroy(mdg_solver* s);
+/* stages.size() (mdcraft/solver/isolver.h:31): 1 for pair, 2 for EAM. */
+int mdg_solver_num_stages(mdg_solver* s, int* n);
+int mdg_solver_set_precision(mdg_solver* s, int precision);
+/* Pair::prepare / charge / forces / virials (mdcraft/solver/pair.cxx:16-114)
+ * on a system whose list is built. */
+int mdg_solver_prepare(mdg_solver* s, mdg_system* sys);
+int mdg_solver_charge(mdg_solver* s, mdg_system* sys);
+int mdg_solver_forces(mdg_solver* s, mdg_system* sys);
+int mdg_solver_virials(mdg_solver* s, mdg_system* sys);
+/* All of solver.stages in order (single.cxx:23-35). */
+int mdg_solver_stages(mdg_solver* s, mdg_system* sys);
+
+/* ---- stepper ----------------------------------------------------------------------- */
+/* stepper::Verlet::make_step(atoms, nlist, dt) (verlet.cxx:36-48). */
+int mdg_verlet_make_step(mdg_solver* s, mdg_system* sys, double dt);
+/* Driver loop, fused on the device: `steps` x { make_step(dt); if decide():
+ * update(-1) }, the loop of the reference's drivers
+ * (test/python/solver/test-EAM.py:158-200). The rebuild test is read back
+ * while the force kernels of the same step run. */
+int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps);
+/* Same loop, end to end from host buffers: uploads positions and velocities
+ * (n*3 doubles each, caller order), runs `steps`, and downloads positions,
+ * velocities and forces. */
+int mdg_run_host(mdg_solver* s, mdg_system* sys, double dt, long steps,
+                 double* pos, double* vel, double* force);
+
+/* ---- measurement ---------------------------------------------------------------- */
+/* FP64 device reduction of measure_state (md_test_utils.h:214-239). Uses
+ * the per-atom Ep, Em, V of the last mdg_solver_virials call. */
+int mdg_system_measure(mdg_system* sys, mdg_state* out);
+/* Error/diagnostic flags accumulated on the device since the last call
+ * (bit 0 atom out of grid, bit 1 neighbour overflow, bit 2 EAM table range,
+ * bit 3 non-finite force); clears them. */
+int mdg_system_flags(mdg_system* sys, uint32_t* flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,429 @@
+"""mdcraft_gb300 — GB300-native MD step engine (Python host over libmdg).
+
+Python mirror of MDcraft's neighbour / potential / solver / stepper API
+(python/mdcraft/{neibs,solver,solver/potential,solver/stepper} bindings of the
+reference) on top of the C-ABI in include/mdg.h. Atoms live on the device in
+cell-sorted order; every index crossing this API is a caller index, and atom
+records use MDcraft's 208-byte Atom layout (mdcraft/data/atom.h:21-40).
+
+There is no CPU fallback: importing works without a GPU, but creating a
+Context raises when libmdg.so is missing or no CUDA device is present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = [
+    "ATOM_DTYPE", "Context", "Domain", "System", "VerletList", "LJsCut", "EAM", "Single", "Multi", "Verlet",
+    "MDGError", "new_atoms", "lib", "lib_path", "PREC_FP64", "PREC_MIXED",
+]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_build", "libmdg.so")
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+ATOM_DTYPE = np.dtype(
+    [("r", "<f8", (3,)), ("v", "<f8", (3,)), ("f", "<f8", (3,)), ("V", "<f8", (9,)), ("m", "<f8"),
+     ("rcut", "<f8"), ("rns", "<f8"), ("Ep", "<f8"), ("Em", "<f8"), ("nc", "<f8"), ("bc", "<u2"),
+     ("kind", "<u2"), ("uid", "<u4"), ("tag", "<u2"), ("_pad", "<u2", (3,))]
+)
+assert ATOM_DTYPE.itemsize == 208
+
+_ERRORS = {
+    -1: "invalid argument", -2: "out of memory", -3: "neighbour overflow", -4: "out of range",
+    -5: "timeout", -6: "CUDA error", -7: "bad state", -8: "no CUDA device", -9: "I/O error",
+}
+
+
+class MDGError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"mdg error {code} ({_ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _LIB
+
+
+def lib():
+    """Loads libmdg.so (built by mdcraft_gb300.build). Raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB):
+        raise RuntimeError(f"libmdg.so not built ({_LIB}); run `python -m mdcraft_gb300.build`")
+    L = C.CDLL(_LIB)
+    vp, sz, dp, ip, u64p = C.c_void_p, C.c_size_t, C.c_double, C.c_int, C.POINTER(C.c_uint64)
+    pp = C.POINTER(C.c_void_p)
+    sig = {
+        "mdg_last_error": ([], C.c_char_p), "mdg_version": ([], C.c_char_p),
+        "mdg_ctx_create": ([ip, pp], ip), "mdg_ctx_destroy": ([vp], ip), "mdg_ctx_synchronize": ([vp], ip),
+        "mdg_ctx_launch_count": ([vp, u64p], ip), "mdg_ctx_set_timing": ([vp, ip], ip),
+        "mdg_ctx_stream": ([vp, pp], ip),
+        "mdg_ctx_stage_time": ([vp, ip, C.POINTER(C.c_double), u64p], ip),
+        "mdg_system_create": ([vp, vp, sz, pp], ip), "mdg_system_destroy": ([vp], ip),
+        "mdg_system_size": ([vp, C.POINTER(C.c_size_t)], ip),
+        "mdg_system_upload_atoms": ([vp, vp, sz], ip), "mdg_system_download_atoms": ([vp, vp, sz], ip),
+        "mdg_system_set_positions": ([vp, vp], ip), "mdg_system_get_positions": ([vp, vp], ip),
+        "mdg_system_set_velocities": ([vp, vp], ip), "mdg_system_get_velocities": ([vp, vp], ip),
+        "mdg_system_get_forces": ([vp, vp], ip),
+        "mdg_nlist_update": ([vp, dp, ip], ip), "mdg_nlist_decide": ([vp, C.POINTER(C.c_int)], ip),
+        "mdg_nlist_total": ([vp, C.POINTER(C.c_size_t)], ip), "mdg_nlist_export": ([vp, vp, vp, sz], ip),
+        "mdg_nlist_list_for": ([vp, vp, vp, sz, C.POINTER(C.c_size_t)], ip),
+        "mdg_nlist_grid": ([vp, vp, vp], ip), "mdg_nlist_rebuilds": ([vp, u64p], ip),
+        "mdg_pot_ljcut_create": ([dp, dp, dp, pp], ip),
+        "mdg_pot_eam_create": ([dp, vp, vp, vp, ip, dp, ip, dp, pp], ip),
+        "mdg_pot_eam_create_from_file": ([C.c_char_p, pp], ip), "mdg_pot_destroy": ([vp], ip),
+        "mdg_pot_rcut": ([vp, C.POINTER(C.c_double)], ip),
+        "mdg_solver_single": ([vp, ip, pp], ip), "mdg_solver_multi": ([ip, ip, pp], ip),
+        "mdg_solver_add_potential": ([vp, ip, ip, vp], ip), "mdg_solver_destroy": ([vp], ip),
+        "mdg_solver_num_stages": ([vp, C.POINTER(C.c_int)], ip), "mdg_solver_set_precision": ([vp, ip], ip),
+        "mdg_solver_prepare": ([vp, vp], ip), "mdg_solver_charge": ([vp, vp], ip),
+        "mdg_solver_forces": ([vp, vp], ip), "mdg_solver_virials": ([vp, vp], ip),
+        "mdg_solver_stages": ([vp, vp], ip), "mdg_verlet_make_step": ([vp, vp, dp], ip),
+        "mdg_run": ([vp, vp, dp, C.c_long], ip), "mdg_run_host": ([vp, vp, dp, C.c_long, vp, vp, vp], ip),
+        "mdg_system_measure": ([vp, vp], ip), "mdg_system_flags": ([vp, C.POINTER(C.c_uint32)], ip),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc: int, allow=()) -> int:
+    if rc != 0 and rc not in allow:
+        raise MDGError(rc, lib().mdg_last_error().decode(errors="replace"))
+    return rc
+
+
+def _ptr(a: np.ndarray) -> int:
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data
+
+
+def new_atoms(n: int) -> np.ndarray:
+    """Zeroed atoms with the reference's default tag (uint16 max)."""
+    a = np.zeros(n, dtype=ATOM_DTYPE)
+    a["tag"] = 0xFFFF
+    return a
+
+
+class Context:
+    """One CUDA device and one stream."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        _check(lib().mdg_ctx_create(device, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def synchronize(self):
+        _check(lib().mdg_ctx_synchronize(self.h))
+
+    def launches(self) -> int:
+        v = C.c_uint64()
+        _check(lib().mdg_ctx_launch_count(self.h, C.byref(v)))
+        return v.value
+
+    def stream_handle(self) -> int:
+        """The engine's cudaStream_t as an integer handle."""
+        p = C.c_void_p()
+        _check(lib().mdg_ctx_stream(self.h, C.byref(p)))
+        return p.value or 0
+
+    STAGES = {"drift": 0, "density": 1, "forces": 2, "kick": 3, "rebuild": 4}
+
+    def set_timing(self, on: bool = True):
+        """Brackets each stage launch of the step loop with CUDA events."""
+        _check(lib().mdg_ctx_set_timing(self.h, int(on)))
+
+    def stage_time(self, which: str):
+        """(total ms, launches) of one stage since set_timing(True)."""
+        ms = C.c_double()
+        n = C.c_uint64()
+        _check(lib().mdg_ctx_stage_time(self.h, self.STAGES[which], C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mdg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Domain:
+    """mdcraft::lattice::Domain (mdcraft/lattice/domain.h:84-108)."""
+
+    class _C(C.Structure):
+        _fields_ = [("bmin", C.c_double * 3), ("bmax", C.c_double * 3), ("periodic", C.c_int32 * 3)]
+
+    def __init__(self, xmin, xmax, ymin, ymax, zmin, zmax):
+        self.c = Domain._C()
+        self.c.bmin[:] = [xmin, ymin, zmin]
+        self.c.bmax[:] = [xmax, ymax, zmax]
+
+    def set_periodic(self, axis: int, val: bool = True):
+        self.c.periodic[axis] = 1 if val else 0
+
+    @property
+    def size(self):
+        return np.array([self.c.bmax[k] - self.c.bmin[k] for k in range(3)])
+
+
+class System:
+    """Device-resident atoms + domain (the Atoms vector every reference class binds)."""
+
+    def __init__(self, ctx: Context, domain: Domain, atoms: np.ndarray | int):
+        n = atoms if isinstance(atoms, int) else len(atoms)
+        h = C.c_void_p()
+        _check(lib().mdg_system_create(ctx.h, C.byref(domain.c), n, C.byref(h)))
+        self.h, self.ctx, self.domain, self.n = h, ctx, domain, n
+        if not isinstance(atoms, int):
+            self.upload(atoms)
+
+    def upload(self, atoms: np.ndarray):
+        a = np.ascontiguousarray(atoms, dtype=ATOM_DTYPE)
+        _check(lib().mdg_system_upload_atoms(self.h, _ptr(a), len(a)))
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.zeros(self.n, dtype=ATOM_DTYPE) if out is None else out
+        _check(lib().mdg_system_download_atoms(self.h, _ptr(out), self.n))
+        return out
+
+    def _vec(self, fn, arr=None):
+        out = np.zeros((self.n, 3)) if arr is None else np.ascontiguousarray(arr, dtype=np.float64)
+        _check(fn(self.h, _ptr(out)))
+        return out
+
+    def positions(self):
+        return self._vec(lib().mdg_system_get_positions)
+
+    def velocities(self):
+        return self._vec(lib().mdg_system_get_velocities)
+
+    def forces(self):
+        return self._vec(lib().mdg_system_get_forces)
+
+    def set_positions(self, xyz):
+        self._vec(lib().mdg_system_set_positions, xyz)
+
+    def set_velocities(self, xyz):
+        self._vec(lib().mdg_system_set_velocities, xyz)
+
+    def measure(self) -> dict:
+        """FP64 totals of measure_state (test/cxx/support/md_test_utils.h:214-239)."""
+        buf = (C.c_double * 8)()
+        _check(lib().mdg_system_measure(self.h, buf))
+        v = list(buf)
+        return {"Ep": v[0], "Em": v[1], "KE": v[2], "Etot": v[3], "virial": v[4], "vcom": np.array(v[5:8])}
+
+    def flags(self) -> int:
+        f = C.c_uint32()
+        _check(lib().mdg_system_flags(self.h, C.byref(f)))
+        return f.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mdg_system_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class VerletList:
+    """mdcraft::neibs::VerletList (mdcraft/neibs/verlet-list.h:158-245) on a System."""
+
+    def __init__(self, system: System, half: bool = False):
+        self.sys = system
+        self.half = bool(half)
+        self.last_status = 0
+
+    def update(self, kbuf: float = -1.0) -> int:
+        self.last_status = _check(lib().mdg_nlist_update(self.sys.h, kbuf, int(self.half)), allow=(-4,))
+        return self.last_status
+
+    def decide(self) -> bool:
+        v = C.c_int()
+        _check(lib().mdg_nlist_decide(self.sys.h, C.byref(v)))
+        return bool(v.value)
+
+    def csr(self):
+        tot = C.c_size_t()
+        _check(lib().mdg_nlist_total(self.sys.h, C.byref(tot)))
+        off = np.zeros(self.sys.n + 1, dtype=np.uint64)
+        idx = np.zeros(max(tot.value, 1), dtype=np.uint64)
+        _check(lib().mdg_nlist_export(self.sys.h, _ptr(off), _ptr(idx), tot.value))
+        return off, idx[: tot.value]
+
+    def lists(self):
+        off, idx = self.csr()
+        return [idx[off[i]: off[i + 1]] for i in range(self.sys.n)]
+
+    def list_for(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(65536, dtype=np.uint64)
+        cnt = C.c_size_t()
+        _check(lib().mdg_nlist_list_for(self.sys.h, _ptr(x), _ptr(out), len(out), C.byref(cnt)))
+        return out[: min(cnt.value, len(out))]
+
+    def grid(self) -> dict:
+        ints = np.zeros(9, dtype=np.int32)
+        dbl = np.zeros(3)
+        _check(lib().mdg_nlist_grid(self.sys.h, _ptr(ints), _ptr(dbl)))
+        return {"domain_num_cells": ints[0:3], "grid_offset": ints[3:6], "num_cells": ints[6:9],
+                "cell_sizes": dbl}
+
+    def rebuilds(self) -> int:
+        v = C.c_uint64()
+        _check(lib().mdg_nlist_rebuilds(self.sys.h, C.byref(v)))
+        return v.value
+
+
+class _Pot:
+    def rcut(self) -> float:
+        v = C.c_double()
+        _check(lib().mdg_pot_rcut(self.h, C.byref(v)))
+        return v.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().mdg_pot_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+class LJsCut(_Pot):
+    """LJsCut(a, s, rcut) (mdcraft/solver/potential/LJs-cut.h:15-19)."""
+
+    def __init__(self, a: float, s: float, rcut: float):
+        h = C.c_void_p()
+        _check(lib().mdg_pot_ljcut_create(a, s, rcut, C.byref(h)))
+        self.h = h
+
+
+class EAM(_Pot):
+    """EAM(rcut, Femb, Rho, Vpar, Nr1, dr, Nrh1, drh) (EAM.h:13-21)."""
+
+    def __init__(self, rcut, Femb, Rho, Vpar, Nr1, dr, Nrh1, drh):
+        F = np.ascontiguousarray(Femb, dtype=np.float64)
+        R = np.ascontiguousarray(Rho, dtype=np.float64)
+        V = np.ascontiguousarray(Vpar, dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib().mdg_pot_eam_create(rcut, _ptr(F), _ptr(R), _ptr(V), int(Nr1), dr, int(Nrh1), drh,
+                                        C.byref(h)))
+        self.h = h
+
+    @classmethod
+    def from_file(cls, path: str) -> "EAM":
+        """EAM(std::string filename) (EAM.cxx:55-87)."""
+        obj = cls.__new__(cls)
+        h = C.c_void_p()
+        _check(lib().mdg_pot_eam_create_from_file(path.encode(), C.byref(h)))
+        obj.h = h
+        return obj
+
+
+class _Solver:
+    def __init__(self):
+        self._pots = []
+
+    def num_stages(self) -> int:
+        v = C.c_int()
+        _check(lib().mdg_solver_num_stages(self.h, C.byref(v)))
+        return v.value
+
+    def set_precision(self, precision):
+        p = {"fp64": PREC_FP64, "mixed": PREC_MIXED}.get(precision, precision)
+        _check(lib().mdg_solver_set_precision(self.h, int(p)))
+        return self
+
+    def prepare(self, sys: System):
+        _check(lib().mdg_solver_prepare(self.h, sys.h))
+
+    def charge(self, sys: System):
+        _check(lib().mdg_solver_charge(self.h, sys.h))
+
+    def forces(self, sys: System):
+        _check(lib().mdg_solver_forces(self.h, sys.h))
+
+    def virials(self, sys: System):
+        _check(lib().mdg_solver_virials(self.h, sys.h))
+
+    def stages(self, sys: System):
+        _check(lib().mdg_solver_stages(self.h, sys.h))
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().mdg_solver_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+class Single(_Solver):
+    """Single(pot, boundary) (mdcraft/solver/single.h:37-42); periodic=True
+    selects boundary::Periodic(domain)."""
+
+    def __init__(self, pot: _Pot, periodic: bool = False, precision="fp64"):
+        super().__init__()
+        h = C.c_void_p()
+        _check(lib().mdg_solver_single(pot.h, int(periodic), C.byref(h)))
+        self.h = h
+        self._pots.append(pot)
+        self.set_precision(precision)
+
+
+class Multi(_Solver):
+    """Multi(boundary, thermostat, nkinds) (mdcraft/solver/multi.h:42-47)."""
+
+    def __init__(self, nkinds: int, periodic: bool = False, precision="fp64"):
+        super().__init__()
+        h = C.c_void_p()
+        _check(lib().mdg_solver_multi(nkinds, int(periodic), C.byref(h)))
+        self.h = h
+        self.set_precision(precision)
+
+    def add_potential(self, i: int, j: int, pot: _Pot):
+        self._pots.append(pot)
+        _check(lib().mdg_solver_add_potential(self.h, i, j, pot.h))
+
+
+class Verlet:
+    """stepper::Verlet (mdcraft/solver/stepper/verlet.h:34-64)."""
+
+    def __init__(self, solver: _Solver):
+        self.solver = solver
+
+    def make_step(self, sys: System, dt: float):
+        _check(lib().mdg_verlet_make_step(self.solver.h, sys.h, dt))
+
+    def run(self, sys: System, dt: float, steps: int):
+        """steps x {make_step; if decide(): update(-1)} fused on the device."""
+        _check(lib().mdg_run(self.solver.h, sys.h, dt, int(steps)), allow=(-4,))
+
+    def run_host(self, sys: System, dt: float, steps: int, pos, vel, force=None):
+        fp = _ptr(force) if force is not None else None
+        _check(lib().mdg_run_host(self.solver.h, sys.h, dt, int(steps), _ptr(pos), _ptr(vel), fp), allow=(-4,))

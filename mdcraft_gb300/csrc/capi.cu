@@ -1,0 +1,1315 @@
+// capi.cu — the extern "C" entry points of include/mdg.h.
+//
+// Host orchestration only: object lifetimes, host<->device transfers in the
+// caller's atom order, spline set-up of EAM tables, the stage sequence of
+// Single / Multi (mdcraft/solver/{single,multi}.cxx) and the Verlet step
+// loop (mdcraft/solver/stepper/verlet.cxx:36-48). All arithmetic on atoms
+// happens in the kernels of nlist.cu, forces.cu and integrate.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "mdg_host.h"
+
+namespace mdg {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+int cuda_status(cudaError_t e, const char* what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return MDG_ERR_NOMEM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return MDG_ERR_NODEV;
+    return MDG_ERR_CUDA;
+}
+
+int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int precision, int stage);
+int launch_virials(mdg_system* sys, const PotSet* dps, const PotSet& ps);
+int launch_drift(mdg_system* sys, double dt, int precision, double pot_rcut, int periodic_boundary, int drift,
+                 int check);
+int launch_kick(mdg_system* sys, double dt, int precision);
+int launch_decide(mdg_system* sys);
+int launch_trig(mdg_system* sys);
+int launch_offsets(mdg_system* sys);
+int launch_force_copy(mdg_system* sys, int to64);
+int launch_zero(mdg_system* sys, int eam);
+int launch_measure(mdg_system* sys, double out[11]);
+
+// ---------------------------------------------------------------------------
+// transfers between the caller's order and the device slot order
+// ---------------------------------------------------------------------------
+static inline int nblk(size_t n, int b = kBlock) { return (int)((n + b - 1) / b); }
+
+struct XferArgs {
+    int n;
+    const uint32_t* slot_of;
+    double* f64[NF64];
+    float* f32[3];
+    uint32_t* u32[NU32];
+    uint16_t* u16[NU16];
+};
+
+static XferArgs xfer_args(mdg_system* sys) {
+    XferArgs X;
+    memset(&X, 0, sizeof(X));
+    int c = sys->cur;
+    X.n = (int)sys->n;
+    X.slot_of = sys->slot_of;
+    for (int f = 0; f < NF64; ++f) X.f64[f] = sys->f64[f][c];
+    for (int f = 0; f < 3; ++f) X.f32[f] = sys->f32[f][c];
+    for (int f = 0; f < NU32; ++f) X.u32[f] = sys->u32[f][c];
+    for (int f = 0; f < NU16; ++f) X.u16[f] = sys->u16[f][c];
+    return X;
+}
+
+// 208-byte Atom records (caller order) -> SoA slots.
+__global__ void k_atoms_in(XferArgs X, const mdg_atom* __restrict__ in) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= X.n) return;
+    const mdg_atom& a = in[k];
+    uint32_t s = X.slot_of[k];
+    for (int c = 0; c < 3; ++c) {
+        X.f64[RX + c][s] = a.r[c];
+        X.f64[VX + c][s] = a.v[c];
+        X.f64[FX + c][s] = a.f[c];
+        X.f32[c][s] = (float)a.f[c];
+    }
+    X.f64[MASS][s] = a.m;
+    X.f64[RCUT][s] = a.rcut;
+    X.f64[RNS][s] = a.rns;
+    X.f64[EP][s] = a.Ep;
+    X.f64[EM][s] = a.Em;
+    X.f64[NC][s] = a.nc;
+    for (int q = 0; q < 9; ++q) X.f64[V0 + q][s] = a.V[q];
+    X.u32[UID][s] = a.uid;
+    X.u16[KIND][s] = a.kind;
+    X.u16[TAG][s] = a.tag;
+}
+
+__global__ void k_atoms_out(XferArgs X, const uint8_t* __restrict__ bc, mdg_atom* __restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= X.n) return;
+    mdg_atom& a = out[k];
+    uint32_t s = X.slot_of[k];
+    for (int c = 0; c < 3; ++c) {
+        a.r[c] = X.f64[RX + c][s];
+        a.v[c] = X.f64[VX + c][s];
+        a.f[c] = X.f64[FX + c][s];
+    }
+    a.m = X.f64[MASS][s];
+    a.rcut = X.f64[RCUT][s];
+    a.rns = X.f64[RNS][s];
+    a.Ep = X.f64[EP][s];
+    a.Em = X.f64[EM][s];
+    a.nc = X.f64[NC][s];
+    for (int q = 0; q < 9; ++q) a.V[q] = X.f64[V0 + q][s];
+    a.uid = X.u32[UID][s];
+    a.kind = X.u16[KIND][s];
+    a.tag = X.u16[TAG][s];
+    a.bc = bc[s];
+    a._pad[0] = a._pad[1] = a._pad[2] = 0;
+}
+
+// xyz triples (caller order) <-> three SoA fields.
+__global__ void k_vec_in(int n, const uint32_t* __restrict__ slot_of, const double* __restrict__ in, double* x,
+                         double* y, double* z) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t s = slot_of[k];
+    x[s] = in[3 * k];
+    y[s] = in[3 * k + 1];
+    z[s] = in[3 * k + 2];
+}
+
+__global__ void k_vec_out(int n, const uint32_t* __restrict__ slot_of, const double* x, const double* y,
+                          const double* z, double* __restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t s = slot_of[k];
+    out[3 * k] = x[s];
+    out[3 * k + 1] = y[s];
+    out[3 * k + 2] = z[s];
+}
+
+__global__ void k_iota(int n, uint32_t* a, uint32_t* b) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) {
+        a[k] = (uint32_t)k;
+        b[k] = (uint32_t)k;
+    }
+}
+
+cudaEvent_t timer_begin(mdg_ctx* ctx) {
+    if (!ctx->timing) return nullptr;
+    cudaEvent_t e = nullptr;
+    if (!ctx->ev_pool.empty()) {
+        e = ctx->ev_pool.back();
+        ctx->ev_pool.pop_back();
+    } else if (cudaEventCreate(&e) != cudaSuccess) {
+        return nullptr;
+    }
+    cudaEventRecord(e, ctx->stream);
+    return e;
+}
+
+void timer_end(mdg_ctx* ctx, int which, cudaEvent_t start) {
+    if (!start) return;
+    cudaEvent_t e = nullptr;
+    if (!ctx->ev_pool.empty()) {
+        e = ctx->ev_pool.back();
+        ctx->ev_pool.pop_back();
+    } else if (cudaEventCreate(&e) != cudaSuccess) {
+        return;
+    }
+    cudaEventRecord(e, ctx->stream);
+    ctx->ev_pending[which].push_back({start, e});
+}
+
+int ensure_pinned(mdg_system* sys, size_t bytes) {
+    if (bytes <= sys->pin_bytes) return MDG_OK;
+    if (sys->pin) cudaFreeHost(sys->pin);
+    sys->pin = nullptr;
+    MDG_CUDA(cudaMallocHost(&sys->pin, bytes));
+    sys->pin_bytes = bytes;
+    return MDG_OK;
+}
+
+// device scratch for host transfers (one per host thread and device)
+static int xfer_buffer(mdg_system* sys, size_t bytes, void** out) {
+    static thread_local void* buf = nullptr;
+    static thread_local size_t cap = 0;
+    static thread_local int dev = -1;
+    if (dev != sys->ctx->device || bytes > cap) {
+        if (buf) cudaFree(buf);
+        buf = nullptr;
+        cap = 0;
+        MDG_CUDA(cudaMalloc(&buf, bytes));
+        cap = bytes;
+        dev = sys->ctx->device;
+    }
+    *out = buf;
+    return MDG_OK;
+}
+
+template <typename T>
+static int dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    MDG_CUDA(cudaMalloc((void**)p, count * sizeof(T)));
+    return MDG_OK;
+}
+
+int system_alloc(mdg_system* sys) {
+    size_t np = std::max<size_t>(sys->np, 32);
+    int rc;
+#define TRY(x) \
+    if ((rc = (x)) != MDG_OK) return rc
+    for (int f = 0; f < NF64; ++f)
+        for (int b = 0; b < 2; ++b) TRY(dalloc(&sys->f64[f][b], np));
+    for (int f = 0; f < 3; ++f)
+        for (int b = 0; b < 2; ++b) TRY(dalloc(&sys->f32[f][b], np));
+    for (int f = 0; f < NU32; ++f)
+        for (int b = 0; b < 2; ++b) TRY(dalloc(&sys->u32[f][b], np));
+    for (int f = 0; f < NU16; ++f)
+        for (int b = 0; b < 2; ++b) TRY(dalloc(&sys->u16[f][b], np));
+    for (int a = 0; a < 3; ++a) {
+        TRY(dalloc(&sys->Rc[a], np));
+        TRY(dalloc(&sys->r0[a], np));
+    }
+    TRY(dalloc(&sys->cellp, np));
+    TRY(dalloc(&sys->pos32, 2 * np));
+    TRY(dalloc(&sys->o0, np));
+    TRY(dalloc(&sys->saved_rcut, np));
+    TRY(dalloc(&sys->saved_rns, np));
+    TRY(dalloc(&sys->saved_uid, np));
+    TRY(dalloc(&sys->slot_of, np));
+    TRY(dalloc(&sys->bc, np));
+    TRY(dalloc(&sys->Fp64, (size_t)kMaxKinds * np));
+    TRY(dalloc(&sys->Fp32, (size_t)kMaxKinds * np));
+    TRY(dalloc(&sys->trig32, np));
+    TRY(dalloc(&sys->key, np));
+    TRY(dalloc(&sys->rank, np));
+    TRY(dalloc(&sys->src, np));
+    TRY(dalloc(&sys->ncnt, np));
+    TRY(dalloc(&sys->dstat, 1));
+    TRY(dalloc(&sys->dgrid, 1));
+    TRY(dalloc(&sys->red, 16));
+#undef TRY
+    MDG_CUDA(cudaMallocHost((void**)&sys->hgrid, sizeof(GridParams)));
+    MDG_CUDA(cudaMallocHost((void**)&sys->hstat, sizeof(DevStatus)));
+    MDG_CUDA(cudaMallocHost((void**)&sys->hred, 16 * sizeof(double)));
+    cudaStream_t st = sys->ctx->stream;
+    MDG_CUDA(cudaMemsetAsync(sys->dstat, 0, sizeof(DevStatus), st));
+    MDG_CUDA(cudaMemsetAsync(sys->ncnt, 0, np * sizeof(uint32_t), st));
+    MDG_CUDA(cudaMemsetAsync(sys->bc, 0, np, st));
+    MDG_CUDA(cudaMemsetAsync(sys->Fp64, 0, (size_t)kMaxKinds * np * sizeof(double), st));
+    MDG_CUDA(cudaMemsetAsync(sys->trig32, 0, np * sizeof(float), st));
+    for (int a = 0; a < 3; ++a) MDG_CUDA(cudaMemsetAsync(sys->Rc[a], 0, np * sizeof(double), st));
+    if (sys->n) {
+        k_iota<<<nblk(sys->n), kBlock, 0, st>>>((int)sys->n, sys->u32[ORIG][0], sys->slot_of);
+        MDG_LAUNCHED(sys->ctx);
+    }
+    MDG_CUDA(cudaStreamSynchronize(st));
+    return MDG_OK;
+}
+
+void system_free(mdg_system* sys) {
+    for (int f = 0; f < NF64; ++f)
+        for (int b = 0; b < 2; ++b) cudaFree(sys->f64[f][b]);
+    for (int f = 0; f < 3; ++f)
+        for (int b = 0; b < 2; ++b) cudaFree(sys->f32[f][b]);
+    for (int f = 0; f < NU32; ++f)
+        for (int b = 0; b < 2; ++b) cudaFree(sys->u32[f][b]);
+    for (int f = 0; f < NU16; ++f)
+        for (int b = 0; b < 2; ++b) cudaFree(sys->u16[f][b]);
+    for (int a = 0; a < 3; ++a) {
+        cudaFree(sys->Rc[a]);
+        cudaFree(sys->r0[a]);
+    }
+    void* ps[] = {sys->cellp, sys->pos32, sys->o0, sys->saved_rcut, sys->saved_rns, sys->saved_uid,
+                  sys->slot_of, sys->bc, sys->Fp64, sys->Fp32, sys->trig32, sys->key, sys->rank, sys->src,
+                  sys->bin_count, sys->bin_start, sys->scan_tmp, sys->part, sys->nbr, sys->ncnt, sys->dstat,
+                  sys->dgrid, sys->red};
+    for (void* p : ps) cudaFree(p);
+    cudaFreeHost(sys->hgrid);
+    cudaFreeHost(sys->hstat);
+    cudaFreeHost(sys->hred);
+    if (sys->pin) cudaFreeHost(sys->pin);
+}
+
+// ---------------------------------------------------------------------------
+// potentials: tables, spline slopes (EAM::init_spline, EAM.cxx:603-686)
+// ---------------------------------------------------------------------------
+static void init_spline(const double* y, double* z, double H1, size_t N, int ib) {
+    std::vector<double> a(N, 2.0), b(N, 0.0), c(N, 0.0), d(N, 0.0);
+    std::vector<double> s(N + 1, 0.0), t(N + 1, 0.0), u(N + 1, 0.0), v(N + 1, 0.0), w(N + 1, 0.0);
+    b[0] = 1.0;
+    c[0] = 0.0;
+    d[0] = 3.0 * H1 * (y[1] - y[0]);
+    b[N - 1] = 0.0;
+    if (ib == 1) {
+        c[N - 1] = 0.0;
+        d[N - 1] = 0.0;
+    } else if (ib == 2) {
+        c[N - 1] = 1.0;
+        d[N - 1] = 3.0 * H1 * (y[N - 1] - y[N - 2]);
+    }
+    for (size_t i = 1; i < N - 1; i++) {
+        c[i] = 0.5;
+        b[i] = 0.5;
+        d[i] = 1.5 * H1 * (y[i + 1] - y[i - 1]);
+    }
+    u[0] = 0.0;
+    v[0] = 0.0;
+    w[0] = 1.0;
+    for (size_t i = 0; i < N; i++) {
+        double rp = -1.0 / (a[i] + c[i] * v[i]);
+        v[i + 1] = rp * b[i];
+        u[i + 1] = rp * (c[i] * u[i] - d[i]);
+        w[i + 1] = rp * c[i] * w[i];
+    }
+    s[N - 1] = 1.0;
+    t[N - 1] = 0.0;
+    for (long i = (long)N - 2; i >= 0; i--) {
+        s[i] = v[i + 1] * s[i + 1] + w[i + 1];
+        t[i] = v[i + 1] * t[i + 1] + u[i + 1];
+    }
+    for (size_t i = 0; i < N; ++i) z[i] = 0.0;
+    z[N - 1] = (d[N - 1] - b[N - 1] * t[0] - c[N - 1] * t[N - 2]) /
+               (a[N - 1] + b[N - 1] * s[0] + c[N - 1] * s[N - 2]);
+    // The reference reads z[i] (zero on entry) in this update.
+    for (size_t i = 0; i < N - 1; i++) z[i] = s[i] * z[i] + t[i];
+}
+
+// Cubic coefficients of the Hermite piece on [x_n, x_n + h] in u = (x - x_n)/h:
+// value = y_n + u*(h z_n) + u^2*(-h b) + u^3*(h a) with the reference's a, b.
+static void cubic_coeffs(const std::vector<double>& y, const std::vector<double>& z, double h, int N,
+                         std::vector<float4>& out) {
+    out.resize(N);
+    double h1 = 1.0 / h;
+    for (int n = 0; n < N; ++n) {
+        double m = (y[n + 1] - y[n]) * h1;
+        double aa = (z[n + 1] - m) - (m - z[n]);
+        double bb = aa - (m - z[n]);
+        out[n] = make_float4((float)y[n], (float)(h * z[n]), (float)(-h * bb), (float)(h * aa));
+    }
+}
+
+int pot_upload(mdg_potential* p, int device) {
+    if (p->type != 2 || p->device == device) return MDG_OK;
+    if (p->d_tab64) cudaFree(p->d_tab64);
+    if (p->d_tab32) cudaFree(p->d_tab32);
+    p->d_tab64 = nullptr;
+    p->d_tab32 = nullptr;
+    size_t nr = (size_t)p->Nr1 + 1, nh = (size_t)p->Nrh1 + 1;
+    std::vector<double> h64;
+    h64.reserve(4 * nr + 2 * nh);
+    for (auto* v : {&p->Rho, &p->dRho, &p->Vpar, &p->dVpar}) h64.insert(h64.end(), v->begin(), v->end());
+    for (auto* v : {&p->Femb, &p->dFemb}) h64.insert(h64.end(), v->begin(), v->end());
+    std::vector<float4> rc, vc, fc, h32;
+    cubic_coeffs(p->Rho, p->dRho, p->dr, p->Nr1, rc);
+    cubic_coeffs(p->Vpar, p->dVpar, p->dr, p->Nr1, vc);
+    cubic_coeffs(p->Femb, p->dFemb, p->drh, p->Nrh1, fc);
+    h32.insert(h32.end(), rc.begin(), rc.end());
+    h32.insert(h32.end(), vc.begin(), vc.end());
+    h32.insert(h32.end(), fc.begin(), fc.end());
+    MDG_CUDA(cudaSetDevice(device));
+    MDG_CUDA(cudaMalloc(&p->d_tab64, h64.size() * sizeof(double)));
+    MDG_CUDA(cudaMalloc(&p->d_tab32, h32.size() * sizeof(float4)));
+    MDG_CUDA(cudaMemcpy(p->d_tab64, h64.data(), h64.size() * sizeof(double), cudaMemcpyHostToDevice));
+    MDG_CUDA(cudaMemcpy(p->d_tab32, h32.data(), h32.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    p->device = device;
+    return MDG_OK;
+}
+
+static void fill_params(const mdg_potential* p, PotParams& P) {
+    memset(&P, 0, sizeof(P));
+    P.type = p->type;
+    P.R2cut = p->rcut * p->rcut;
+    P.r2cut_f = (float)P.R2cut;
+    if (p->type == 1) {
+        P.a = p->a;
+        P.s6 = p->s6;
+        P.lj1 = p->lj1;
+        P.lj2 = p->lj2;
+        P.factor = p->factor;
+        P.lj1_f = (float)p->lj1;
+        P.lj2_f = (float)p->lj2;
+        P.mhf_f = (float)(-0.5 * p->factor);
+    } else if (p->type == 2) {
+        size_t nr = (size_t)p->Nr1 + 1, nh = (size_t)p->Nrh1 + 1;
+        P.Nr1 = p->Nr1;
+        P.Nrh1 = p->Nrh1;
+        P.dr = p->dr;
+        P.drh = p->drh;
+        P.dr1 = p->dr1;
+        P.drh1 = p->drh1;
+        P.Rho = p->d_tab64;
+        P.dRho = p->d_tab64 + nr;
+        P.Vpar = p->d_tab64 + 2 * nr;
+        P.dVpar = p->d_tab64 + 3 * nr;
+        P.Femb = p->d_tab64 + 4 * nr;
+        P.dFemb = p->d_tab64 + 4 * nr + nh;
+        P.rho_c = p->d_tab32;
+        P.v_c = p->d_tab32 + p->Nr1;
+        P.f_c = p->d_tab32 + 2 * p->Nr1;
+        P.inv_dr_f = (float)(1.0 / p->dr);
+        P.inv_drh_f = (float)(1.0 / p->drh);
+        P.dr1_f = (float)p->dr1;
+        P.drh_f = (float)p->drh;
+    }
+}
+
+}  // namespace mdg
+
+using namespace mdg;
+
+// solver + system binding: the PotSet lives in device memory, one per
+// (solver, device); rebuilt when potentials change.
+struct SolverDev {
+    PotSet host;
+    PotSet* dev = nullptr;
+    int device = -1;
+    int version = -1;
+};
+
+struct mdg_solver_ext {
+    mdg_solver s;
+    SolverDev d;
+    int version = 0;
+};
+
+static mdg_solver_ext* ext(mdg_solver* s) { return reinterpret_cast<mdg_solver_ext*>(s); }
+
+namespace mdg {
+int potset_build(mdg_solver* s, mdg_system* sys, PotSet* out) {
+    mdg_solver_ext* e = ext(s);
+    int dev = sys->ctx->device;
+    if (e->d.device == dev && e->d.version == e->version && e->d.dev) {
+        e->d.host.periodic = s->periodic;
+        if (out) *out = e->d.host;
+        return MDG_OK;
+    }
+    PotSet ps;
+    memset(&ps, 0, sizeof(ps));
+    ps.nkinds = s->multi ? s->nkinds : 1;
+    ps.multi = s->multi;
+    ps.periodic = s->periodic;
+    for (int i = 0; i < ps.nkinds; ++i)
+        for (int j = 0; j < ps.nkinds; ++j) {
+            mdg_potential* p = s->pot[i][j];
+            if (!p) continue;
+            int rc = pot_upload(p, dev);
+            if (rc) return rc;
+            fill_params(p, ps.p[i][j]);
+            if (p->type == 2) ps.any_eam = 1;
+        }
+    if (!e->d.dev || e->d.device != dev) {
+        if (e->d.dev) cudaFree(e->d.dev);
+        e->d.dev = nullptr;
+        MDG_CUDA(cudaMalloc(&e->d.dev, sizeof(PotSet)));
+    }
+    MDG_CUDA(cudaMemcpy(e->d.dev, &ps, sizeof(PotSet), cudaMemcpyHostToDevice));
+    e->d.host = ps;
+    e->d.device = dev;
+    e->d.version = e->version;
+    if (out) *out = ps;
+    return MDG_OK;
+}
+}  // namespace mdg
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+const char* mdg_last_error(void) { return g_err.c_str(); }
+const char* mdg_version(void) { return "mdg 0.1 (sm_103a)"; }
+
+int mdg_ctx_create(int device, mdg_ctx** out) {
+    if (!out) return MDG_ERR_INVALID;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        set_error("no CUDA device available (libmdg has no CPU fallback)");
+        return MDG_ERR_NODEV;
+    }
+    if (device < 0 || device >= count) {
+        set_error("device index out of range");
+        return MDG_ERR_INVALID;
+    }
+    MDG_CUDA(cudaSetDevice(device));
+    mdg_ctx* c = new mdg_ctx();
+    c->device = device;
+    cudaError_t e2 = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e2 != cudaSuccess) {
+        delete c;
+        return cuda_status(e2, "cudaStreamCreate");
+    }
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    *out = c;
+    return MDG_OK;
+}
+
+int mdg_ctx_destroy(mdg_ctx* ctx) {
+    if (!ctx) return MDG_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return MDG_OK;
+}
+
+int mdg_ctx_synchronize(mdg_ctx* ctx) {
+    if (!ctx) return MDG_ERR_INVALID;
+    MDG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return MDG_OK;
+}
+
+int mdg_ctx_stream(mdg_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return MDG_ERR_INVALID;
+    *stream = (void*)ctx->stream;
+    return MDG_OK;
+}
+
+int mdg_ctx_launch_count(mdg_ctx* ctx, uint64_t* out) {
+    if (!ctx || !out) return MDG_ERR_INVALID;
+    *out = ctx->launches;
+    return MDG_OK;
+}
+
+int mdg_ctx_set_timing(mdg_ctx* ctx, int on) {
+    if (!ctx) return MDG_ERR_INVALID;
+    MDG_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->timing = on ? 1 : 0;
+    for (int w = 0; w < 5; ++w) {
+        for (auto& pr : ctx->ev_pending[w]) {
+            ctx->ev_pool.push_back(pr.first);
+            ctx->ev_pool.push_back(pr.second);
+        }
+        ctx->ev_pending[w].clear();
+        ctx->stage_ms[w] = 0.0;
+        ctx->stage_n[w] = 0;
+    }
+    return MDG_OK;
+}
+
+int mdg_ctx_stage_time(mdg_ctx* ctx, int which, double* total_ms, uint64_t* launches) {
+    if (!ctx || which < 0 || which > 4 || !total_ms) return MDG_ERR_INVALID;
+    MDG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int w = 0; w < 5; ++w) {
+        for (auto& pr : ctx->ev_pending[w]) {
+            float ms = 0.f;
+            MDG_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+            ctx->stage_ms[w] += ms;
+            ctx->stage_n[w]++;
+            ctx->ev_pool.push_back(pr.first);
+            ctx->ev_pool.push_back(pr.second);
+        }
+        ctx->ev_pending[w].clear();
+    }
+    *total_ms = ctx->stage_ms[which];
+    if (launches) *launches = ctx->stage_n[which];
+    return MDG_OK;
+}
+
+int mdg_system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n, mdg_system** out) {
+    if (!ctx || !domain || !out) return MDG_ERR_INVALID;
+    *out = nullptr;
+    if (n >= kMaxAtoms) {
+        set_error("system too large: at most 2^25 - 1 atoms per system");
+        return MDG_ERR_INVALID;
+    }
+    MDG_CUDA(cudaSetDevice(ctx->device));
+    mdg_system* s = new mdg_system();
+    s->ctx = ctx;
+    s->dom = *domain;
+    double zs = domain->bmax[2] - domain->bmin[2], ys = domain->bmax[1] - domain->bmin[1];
+    s->dim = std::fabs(-zs) > 1e-15 ? 3 : std::fabs(-ys) > 1e-15 ? 2 : 1;
+    s->n = n;
+    s->np = (n + 31) & ~size_t(31);
+    int rc = system_alloc(s);
+    if (rc) {
+        system_free(s);
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return MDG_OK;
+}
+
+int mdg_system_destroy(mdg_system* sys) {
+    if (!sys) return MDG_ERR_INVALID;
+    cudaSetDevice(sys->ctx->device);
+    cudaStreamSynchronize(sys->ctx->stream);
+    system_free(sys);
+    delete sys;
+    return MDG_OK;
+}
+
+int mdg_system_size(mdg_system* sys, size_t* n) {
+    if (!sys || !n) return MDG_ERR_INVALID;
+    *n = sys->n;
+    return MDG_OK;
+}
+
+int mdg_system_upload_atoms(mdg_system* sys, const mdg_atom* atoms, size_t n) {
+    if (!sys || (!atoms && n) || n != sys->n) {
+        set_error("atom count differs from the system size");
+        return MDG_ERR_INVALID;
+    }
+    if (n == 0) return MDG_OK;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    cudaStream_t st = sys->ctx->stream;
+    size_t bytes = n * sizeof(mdg_atom);
+    void* dbuf;
+    int rc = ensure_pinned(sys, bytes);
+    if (rc) return rc;
+    rc = xfer_buffer(sys, bytes, &dbuf);
+    if (rc) return rc;
+    memcpy(sys->pin, atoms, bytes);
+    MDG_CUDA(cudaMemcpyAsync(dbuf, sys->pin, bytes, cudaMemcpyHostToDevice, st));
+    k_atoms_in<<<nblk(n), kBlock, 0, st>>>(xfer_args(sys), (const mdg_atom*)dbuf);
+    MDG_LAUNCHED(sys->ctx);
+    sys->force_prec = MDG_PREC_FP64;
+    if (sys->have_list) {
+        rc = launch_offsets(sys);
+        if (rc) return rc;
+    }
+    MDG_CUDA(cudaStreamSynchronize(st));
+    return MDG_OK;
+}
+
+static int sync_forces64(mdg_system* sys) {
+    if (sys->force_prec == MDG_PREC_MIXED) {
+        int rc = launch_force_copy(sys, 1);
+        if (rc) return rc;
+        sys->force_prec = MDG_PREC_FP64;
+    }
+    return MDG_OK;
+}
+
+int mdg_system_download_atoms(mdg_system* sys, mdg_atom* atoms, size_t n) {
+    if (!sys || (!atoms && n) || n != sys->n) return MDG_ERR_INVALID;
+    if (n == 0) return MDG_OK;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    cudaStream_t st = sys->ctx->stream;
+    size_t bytes = n * sizeof(mdg_atom);
+    void* dbuf;
+    int rc = ensure_pinned(sys, bytes);
+    if (rc) return rc;
+    rc = xfer_buffer(sys, bytes, &dbuf);
+    if (rc) return rc;
+    rc = sync_forces64(sys);
+    if (rc) return rc;
+    k_atoms_out<<<nblk(n), kBlock, 0, st>>>(xfer_args(sys), sys->bc, (mdg_atom*)dbuf);
+    MDG_LAUNCHED(sys->ctx);
+    MDG_CUDA(cudaMemcpyAsync(sys->pin, dbuf, bytes, cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    memcpy(atoms, sys->pin, bytes);
+    return MDG_OK;
+}
+
+static int vec_io(mdg_system* sys, double* host, int field, int in) {
+    if (!sys || !host) return MDG_ERR_INVALID;
+    size_t n = sys->n;
+    if (n == 0) return MDG_OK;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    cudaStream_t st = sys->ctx->stream;
+    size_t bytes = n * 3 * sizeof(double);
+    void* dbuf;
+    int rc = xfer_buffer(sys, bytes, &dbuf);
+    if (rc) return rc;
+    int c = sys->cur;
+    if (in) {
+        MDG_CUDA(cudaMemcpyAsync(dbuf, host, bytes, cudaMemcpyHostToDevice, st));
+        k_vec_in<<<nblk(n), kBlock, 0, st>>>((int)n, sys->slot_of, (const double*)dbuf, sys->f64[field][c],
+                                             sys->f64[field + 1][c], sys->f64[field + 2][c]);
+        MDG_LAUNCHED(sys->ctx);
+        if (field == RX && sys->have_list) {
+            rc = launch_offsets(sys);
+            if (rc) return rc;
+        }
+        MDG_CUDA(cudaStreamSynchronize(st));
+    } else {
+        if (field == FX) {
+            rc = sync_forces64(sys);
+            if (rc) return rc;
+        }
+        k_vec_out<<<nblk(n), kBlock, 0, st>>>((int)n, sys->slot_of, sys->f64[field][c], sys->f64[field + 1][c],
+                                              sys->f64[field + 2][c], (double*)dbuf);
+        MDG_LAUNCHED(sys->ctx);
+        MDG_CUDA(cudaMemcpyAsync(host, dbuf, bytes, cudaMemcpyDeviceToHost, st));
+        MDG_CUDA(cudaStreamSynchronize(st));
+    }
+    return MDG_OK;
+}
+
+int mdg_system_set_positions(mdg_system* sys, const double* xyz) { return vec_io(sys, (double*)xyz, RX, 1); }
+int mdg_system_get_positions(mdg_system* sys, double* xyz) { return vec_io(sys, xyz, RX, 0); }
+int mdg_system_set_velocities(mdg_system* sys, const double* xyz) { return vec_io(sys, (double*)xyz, VX, 1); }
+int mdg_system_get_velocities(mdg_system* sys, double* xyz) { return vec_io(sys, xyz, VX, 0); }
+int mdg_system_get_forces(mdg_system* sys, double* xyz) { return vec_io(sys, xyz, FX, 0); }
+
+// ---- Verlet list -----------------------------------------------------------
+int mdg_nlist_update(mdg_system* sys, double kbuf, int half) {
+    if (!sys) return MDG_ERR_INVALID;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    int rc = nlist_build(sys, kbuf, half ? 1 : 0);
+    if (rc && rc != MDG_ERR_RANGE) return rc;
+    int rc2 = launch_trig(sys);
+    if (rc2) return rc2;
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    return rc;
+}
+
+int mdg_nlist_decide(mdg_system* sys, int* need) {
+    if (!sys || !need) return MDG_ERR_INVALID;
+    if (!sys->have_list) {
+        *need = 1;
+        return MDG_OK;
+    }
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    cudaStream_t st = sys->ctx->stream;
+    MDG_CUDA(cudaMemsetAsync(&sys->dstat->need_rebuild, 0, sizeof(uint32_t), st));
+    int rc = launch_decide(sys);
+    if (rc) return rc;
+    MDG_CUDA(cudaMemcpyAsync(sys->hstat, sys->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    *need = sys->hstat->need_rebuild ? 1 : 0;
+    return MDG_OK;
+}
+
+// host copies of the list in caller order
+static int host_lists(mdg_system* sys, std::vector<uint64_t>& off, std::vector<uint64_t>& idx) {
+    size_t n = sys->n, np = sys->np;
+    cudaStream_t st = sys->ctx->stream;
+    std::vector<uint32_t> cnt(n), orig(n), slot(n), nbr((size_t)sys->K * np);
+    if (n) {
+        MDG_CUDA(cudaMemcpyAsync(cnt.data(), sys->ncnt, n * 4, cudaMemcpyDeviceToHost, st));
+        MDG_CUDA(cudaMemcpyAsync(orig.data(), sys->u32[ORIG][sys->cur], n * 4, cudaMemcpyDeviceToHost, st));
+        MDG_CUDA(cudaMemcpyAsync(slot.data(), sys->slot_of, n * 4, cudaMemcpyDeviceToHost, st));
+        if (sys->K) MDG_CUDA(cudaMemcpyAsync(nbr.data(), sys->nbr, nbr.size() * 4, cudaMemcpyDeviceToHost, st));
+        MDG_CUDA(cudaStreamSynchronize(st));
+    }
+    off.assign(n + 1, 0);
+    for (size_t c = 0; c < n; ++c) off[c + 1] = off[c] + cnt[slot[c]] + 1;
+    idx.assign(off[n], 0);
+    for (size_t c = 0; c < n; ++c) {
+        uint32_t s = slot[c];
+        uint64_t* o = idx.data() + off[c];
+        o[0] = c;
+        for (uint32_t k = 0; k < cnt[s]; ++k) o[k + 1] = orig[nbr[(size_t)k * np + s] & kJMask];
+        std::sort(o, o + cnt[s] + 1);
+    }
+    return MDG_OK;
+}
+
+int mdg_nlist_total(mdg_system* sys, size_t* total) {
+    if (!sys || !total) return MDG_ERR_INVALID;
+    if (!sys->have_list) return MDG_ERR_STATE;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    std::vector<uint32_t> cnt(sys->n);
+    if (sys->n) {
+        MDG_CUDA(cudaMemcpyAsync(cnt.data(), sys->ncnt, sys->n * 4, cudaMemcpyDeviceToHost, sys->ctx->stream));
+        MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    }
+    size_t t = 0;
+    for (uint32_t c : cnt) t += c + 1;
+    *total = t;
+    return MDG_OK;
+}
+
+int mdg_nlist_export(mdg_system* sys, uint64_t* offsets, uint64_t* idx, size_t cap) {
+    if (!sys || !offsets) return MDG_ERR_INVALID;
+    if (!sys->have_list) return MDG_ERR_STATE;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    std::vector<uint64_t> off, ix;
+    int rc = host_lists(sys, off, ix);
+    if (rc) return rc;
+    if (ix.size() > cap || (!idx && !ix.empty())) {
+        set_error("export capacity too small");
+        return MDG_ERR_INVALID;
+    }
+    memcpy(offsets, off.data(), off.size() * sizeof(uint64_t));
+    if (!ix.empty()) memcpy(idx, ix.data(), ix.size() * sizeof(uint64_t));
+    return MDG_OK;
+}
+
+int mdg_nlist_grid(mdg_system* sys, int32_t ints[9], double dbls[3]) {
+    if (!sys || !ints || !dbls) return MDG_ERR_INVALID;
+    if (!sys->have_list) return MDG_ERR_STATE;
+    for (int a = 0; a < 3; ++a) {
+        ints[a] = sys->grid.dom_n[a];
+        ints[3 + a] = sys->grid.offset[a];
+        ints[6 + a] = sys->grid.num[a];
+        dbls[a] = sys->grid.cs[a];
+    }
+    return MDG_OK;
+}
+
+int mdg_nlist_rebuilds(mdg_system* sys, uint64_t* count) {
+    if (!sys || !count) return MDG_ERR_INVALID;
+    *count = sys->rebuilds;
+    return MDG_OK;
+}
+
+// VerletList::list_for (verlet-list.cxx:251-276), evaluated on the host from
+// the device's last grid and positions; radius = Grid::cell_size().
+int mdg_nlist_list_for(mdg_system* sys, const double x[3], uint64_t* out, size_t cap, size_t* count) {
+    if (!sys || !x || !count) return MDG_ERR_INVALID;
+    if (!sys->have_list) return MDG_ERR_STATE;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    cudaStream_t st = sys->ctx->stream;
+    const GridParams& g = sys->grid;
+    size_t n = sys->n;
+    std::vector<double> rx(n), ry(n), rz(n), rns(n);
+    std::vector<uint32_t> orig(n), start((size_t)g.nbins + 1);
+    int c = sys->cur;
+    MDG_CUDA(cudaMemcpyAsync(rx.data(), sys->f64[RX][c], n * 8, cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaMemcpyAsync(ry.data(), sys->f64[RY][c], n * 8, cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaMemcpyAsync(rz.data(), sys->f64[RZ][c], n * 8, cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaMemcpyAsync(rns.data(), sys->f64[RNS][c], n * 8, cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaMemcpyAsync(orig.data(), sys->u32[ORIG][c], n * 4, cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaMemcpyAsync(start.data(), sys->bin_start, start.size() * 4, cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    int cell[3] = {0, 0, 0};
+    for (int a = 0; a < g.dim; ++a) cell[a] = (int)std::floor((x[a] - g.bmin[a]) / g.cs[a]);
+    bool edge[3] = {false, false, false};
+    for (int a = 0; a < g.dim; ++a) edge[a] = cell[a] == 0 || cell[a] == g.num[a] - 1;
+    double rad = std::max(g.cs[0], std::max(g.cs[1], g.cs[2]));
+    std::vector<uint64_t> found;
+    for (int dx = -1; dx <= 1; ++dx) {
+        if (g.periodic[0] && ((g.dom_n[0] == 1 && dx != 0) || (g.dom_n[0] == 2 && dx == 1))) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            if (g.periodic[1] && ((g.dom_n[1] == 1 && dy != 0) || (g.dom_n[1] == 2 && dy == 1))) continue;
+            for (int dz = -1; dz <= 1; ++dz) {
+                if (g.periodic[2] && ((g.dom_n[2] == 1 && dz != 0) || (g.dom_n[2] == 2 && dz == 1))) continue;
+                int nb[3] = {cell[0] + dx, cell[1] + dy, cell[2] + dz};
+                for (int a = 0; a < 3; ++a)
+                    if (g.periodic[a]) nb[a] = (nb[a] + g.dom_n[a]) % g.dom_n[a];
+                int lc[3] = {nb[0] - g.offset[0], nb[1] - g.offset[1], nb[2] - g.offset[2]};
+                bool in = true;
+                for (int a = 0; a < 3; ++a) in = in && lc[a] >= 0 && lc[a] < g.num[a];
+                if (!in) continue;
+                int b = bin_key(g, lc[0], lc[1], lc[2]);
+                for (uint32_t j = start[b]; j < start[b + 1]; ++j) {
+                    double dd = rad < rns[j] ? rns[j] : rad;
+                    double d2 = dd * dd;
+                    double d[3] = {x[0] - rx[j], x[1] - ry[j], x[2] - rz[j]};
+                    for (int a = 0; a < 3; ++a) {
+                        double L = g.size[a];
+                        if (edge[a] && g.periodic[a] && (2 * d[a] < -L)) d[a] += L;
+                        if (edge[a] && g.periodic[a] && (2 * d[a] > L)) d[a] -= L;
+                    }
+                    volatile double s0 = d[0] * d[0];
+                    volatile double s1 = d[1] * d[1];
+                    volatile double s2 = d[2] * d[2];
+                    volatile double s01 = s0 + s1;
+                    if (s01 + s2 <= d2) found.push_back(orig[j]);
+                }
+            }
+        }
+    }
+    std::sort(found.begin(), found.end());
+    *count = found.size();
+    for (size_t k = 0; k < found.size() && k < cap; ++k) out[k] = found[k];
+    return MDG_OK;
+}
+
+// ---- potentials ----------------------------------------------------------
+int mdg_pot_ljcut_create(double a, double s, double rcut, mdg_potential** out) {
+    if (!out || !(rcut > 0.0)) return MDG_ERR_INVALID;
+    mdg_potential* p = new mdg_potential();
+    p->type = 1;
+    p->rcut = rcut;
+    p->a = a;
+    p->s = s;
+    p->s6 = std::pow(s, 6);
+    p->lj1 = 2 * p->s6;
+    p->lj2 = 1.;
+    p->factor = 48. * p->a * p->s6;
+    *out = p;
+    return MDG_OK;
+}
+
+int mdg_pot_eam_create(double rcut, const double* Femb, const double* Rho, const double* Vpar, int Nr1, double dr,
+                       int Nrh1, double drh, mdg_potential** out) {
+    if (!out || !Femb || !Rho || !Vpar || Nr1 < 3 || Nrh1 < 3 || !(dr > 0) || !(drh > 0)) {
+        set_error("invalid EAM tables");
+        return MDG_ERR_INVALID;
+    }
+    mdg_potential* p = new mdg_potential();
+    p->type = 2;
+    p->rcut = rcut;
+    p->Nr1 = Nr1;
+    p->Nrh1 = Nrh1;
+    p->dr = dr;
+    p->drh = drh;
+    p->dr1 = 1.0 / dr;
+    p->drh1 = 1.0 / drh;
+    p->Rho.assign(Rho, Rho + Nr1);
+    p->Vpar.assign(Vpar, Vpar + Nr1);
+    p->Femb.assign(Femb, Femb + Nrh1);
+    p->dRho.assign(Nr1 + 1, 0.0);
+    p->dVpar.assign(Nr1 + 1, 0.0);
+    p->dFemb.assign(Nrh1 + 1, 0.0);
+    init_spline(p->Vpar.data(), p->dVpar.data(), p->dr1, Nr1, 1);
+    init_spline(p->Rho.data(), p->dRho.data(), p->dr1, Nr1, 1);
+    init_spline(p->Femb.data(), p->dFemb.data(), p->drh1, Nrh1, 2);
+    // one padding element: the reference reads index N at the table edge
+    p->Rho.push_back(p->Rho.back());
+    p->Vpar.push_back(p->Vpar.back());
+    p->Femb.push_back(p->Femb.back());
+    p->dRho[Nr1] = p->dRho[Nr1 - 1];
+    p->dVpar[Nr1] = p->dVpar[Nr1 - 1];
+    p->dFemb[Nrh1] = p->dFemb[Nrh1 - 1];
+    *out = p;
+    return MDG_OK;
+}
+
+int mdg_pot_eam_create_from_file(const char* path, mdg_potential** out) {
+    // EAM::EAM(std::string) (EAM.cxx:55-87)
+    if (!path || !out) return MDG_ERR_INVALID;
+    std::ifstream file(path);
+    if (!file.is_open()) {
+        set_error(std::string("cannot open EAM file: ") + path);
+        return MDG_ERR_IO;
+    }
+    const double N_a = 6.02214076e+23, Qelectron = 1.602176634e-19;
+    const double UnMass = 1e-3 / N_a, UnLeng = 1e-9, UnTime = 1e-12;
+    const double UnEnrg = UnMass * (UnLeng / UnTime) * (UnLeng / UnTime);
+    std::string line;
+    for (int k = 0; k < 4; ++k) std::getline(file, line);
+    int Nrh1 = 0, Nr1 = 0, Z = 0;
+    double drh = 0, dr = 0, rcut = 0, M = 0, Ecoh = 0;
+    std::string lattice;
+    file >> Nrh1 >> drh >> Nr1 >> dr >> rcut;
+    file >> Z >> M >> Ecoh >> lattice;
+    if (!file || Nrh1 < 3 || Nr1 < 3) {
+        set_error("malformed EAM setfl header");
+        return MDG_ERR_IO;
+    }
+    dr /= 10;
+    rcut /= 10;
+    std::vector<double> F(Nrh1), R(Nr1), V(Nr1);
+    for (int i = 0; i < Nrh1; ++i) {
+        file >> F[i];
+        F[i] *= Qelectron / UnEnrg;
+    }
+    for (int i = 0; i < Nr1; ++i) file >> R[i];
+    for (int i = 0; i < Nr1; ++i) {
+        file >> V[i];
+        V[i] *= Qelectron / (10 * UnEnrg);
+    }
+    if (!file) {
+        set_error("EAM file ended before all tables were read");
+        return MDG_ERR_IO;
+    }
+    return mdg_pot_eam_create(rcut, F.data(), R.data(), V.data(), Nr1, dr, Nrh1, drh, out);
+}
+
+int mdg_pot_destroy(mdg_potential* p) {
+    if (!p) return MDG_ERR_INVALID;
+    if (p->d_tab64) cudaFree(p->d_tab64);
+    if (p->d_tab32) cudaFree(p->d_tab32);
+    delete p;
+    return MDG_OK;
+}
+
+int mdg_pot_rcut(mdg_potential* p, double* rcut) {
+    if (!p || !rcut) return MDG_ERR_INVALID;
+    *rcut = p->rcut;
+    return MDG_OK;
+}
+
+// ---- solvers ----------------------------------------------------------------
+static void set_stages(mdg_solver* s, int type, bool first) {
+    if (first) {
+        if (type == 1) {
+            s->nstages = 1;
+            s->stages[0] = 1;
+        } else if (type == 2) {
+            s->nstages = 2;
+            s->stages[0] = 0;
+            s->stages[1] = 1;
+        }
+    } else if (type == 2 && s->nstages == 1) {
+        s->nstages = 2;
+        s->stages[0] = 0;
+        s->stages[1] = 1;
+    }
+}
+
+int mdg_solver_single(mdg_potential* pot, int periodic, mdg_solver** out) {
+    if (!pot || !out) return MDG_ERR_INVALID;
+    mdg_solver_ext* e = new mdg_solver_ext();
+    e->s.multi = 0;
+    e->s.nkinds = 1;
+    e->s.periodic = periodic ? 1 : 0;
+    e->s.pot[0][0] = pot;
+    set_stages(&e->s, pot->type, true);
+    *out = &e->s;
+    return MDG_OK;
+}
+
+int mdg_solver_multi(int nkinds, int periodic, mdg_solver** out) {
+    if (!out || nkinds < 1 || nkinds > kMaxKinds) {
+        set_error("nkinds must be in [1, 4]");
+        return MDG_ERR_INVALID;
+    }
+    mdg_solver_ext* e = new mdg_solver_ext();
+    e->s.multi = 1;
+    e->s.nkinds = nkinds;
+    e->s.periodic = periodic ? 1 : 0;
+    *out = &e->s;
+    return MDG_OK;
+}
+
+int mdg_solver_add_potential(mdg_solver* s, int i, int j, mdg_potential* pot) {
+    if (!s || !pot || !s->multi || i < 0 || j < 0 || i >= s->nkinds || j >= s->nkinds) return MDG_ERR_INVALID;
+    bool first = s->nstages == 0;
+    s->pot[i][j] = pot;
+    s->pot[j][i] = pot;
+    set_stages(s, pot->type, first);
+    ext(s)->version++;
+    return MDG_OK;
+}
+
+int mdg_solver_destroy(mdg_solver* s) {
+    if (!s) return MDG_ERR_INVALID;
+    mdg_solver_ext* e = ext(s);
+    if (e->d.dev) cudaFree(e->d.dev);
+    delete e;
+    return MDG_OK;
+}
+
+int mdg_solver_num_stages(mdg_solver* s, int* n) {
+    if (!s || !n) return MDG_ERR_INVALID;
+    *n = s->nstages;
+    return MDG_OK;
+}
+
+int mdg_solver_set_precision(mdg_solver* s, int precision) {
+    if (!s || (precision != MDG_PREC_FP64 && precision != MDG_PREC_MIXED)) return MDG_ERR_INVALID;
+    s->precision = precision;
+    return MDG_OK;
+}
+
+static int check_ready(mdg_solver* s, mdg_system* sys, PotSet* ps) {
+    if (!s || !sys) return MDG_ERR_INVALID;
+    if (s->nstages == 0) {
+        set_error("solver has no potential");
+        return MDG_ERR_STATE;
+    }
+    if (!sys->have_list && sys->n) {
+        set_error("no Verlet list: call mdg_nlist_update first");
+        return MDG_ERR_STATE;
+    }
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    if (s->multi) {
+        for (int i = 0; i < s->nkinds; ++i)
+            for (int j = 0; j < s->nkinds; ++j)
+                if (!s->pot[i][j]) {
+                    set_error("Multi solver: a kind pair has no potential");
+                    return MDG_ERR_STATE;
+                }
+    }
+    return potset_build(s, sys, ps);
+}
+
+static double pot_rcut_of(mdg_solver* s) { return s->multi ? -1.0 : s->pot[0][0]->rcut; }
+
+int mdg_solver_prepare(mdg_solver* s, mdg_system* sys) {
+    PotSet ps;
+    int rc = check_ready(s, sys, &ps);
+    if (rc) return rc;
+    rc = launch_zero(sys, ps.any_eam);
+    if (rc) return rc;
+    rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
+    if (rc) return rc;
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    return MDG_OK;
+}
+
+static int stage_impl(mdg_solver* s, mdg_system* sys, const PotSet& ps, int stage, int prec) {
+    mdg_solver_ext* e = ext(s);
+    int rc = launch_stage(sys, e->d.dev, ps, prec, stage);
+    if (rc) return rc;
+    if (stage == 1) sys->force_prec = prec;
+    return MDG_OK;
+}
+
+int mdg_solver_charge(mdg_solver* s, mdg_system* sys) {
+    PotSet ps;
+    int rc = check_ready(s, sys, &ps);
+    if (rc) return rc;
+    rc = stage_impl(s, sys, ps, 0, s->precision);
+    if (rc) return rc;
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    return MDG_OK;
+}
+
+int mdg_solver_forces(mdg_solver* s, mdg_system* sys) {
+    PotSet ps;
+    int rc = check_ready(s, sys, &ps);
+    if (rc) return rc;
+    rc = stage_impl(s, sys, ps, 1, s->precision);
+    if (rc) return rc;
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    return MDG_OK;
+}
+
+int mdg_solver_stages(mdg_solver* s, mdg_system* sys) {
+    PotSet ps;
+    int rc = check_ready(s, sys, &ps);
+    if (rc) return rc;
+    for (int k = 0; k < s->nstages; ++k) {
+        rc = stage_impl(s, sys, ps, s->stages[k], s->precision);
+        if (rc) return rc;
+    }
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    return MDG_OK;
+}
+
+int mdg_solver_virials(mdg_solver* s, mdg_system* sys) {
+    // energies/virials are always evaluated in FP64 (measurement); for the
+    // mixed form the FP64 densities are computed first
+    PotSet ps;
+    int rc = check_ready(s, sys, &ps);
+    if (rc) return rc;
+    mdg_solver_ext* e = ext(s);
+    if (ps.any_eam && s->precision == MDG_PREC_MIXED) {
+        rc = launch_stage(sys, e->d.dev, ps, MDG_PREC_FP64, 0);
+        if (rc) return rc;
+    } else if (ps.any_eam) {
+        // F'(nc) of the current densities (the reference recomputes them)
+        rc = launch_stage(sys, e->d.dev, ps, MDG_PREC_FP64, 0);
+        if (rc) return rc;
+    }
+    rc = launch_virials(sys, e->d.dev, ps);
+    if (rc) return rc;
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    return MDG_OK;
+}
+
+// One Verlet step: drift (+ prepare + rebuild test), stages, kick.
+static int step_impl(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt) {
+    mdg_solver_ext* e = ext(s);
+    int prec = s->precision;
+    int rc;
+    if (sys->force_prec != prec) {
+        rc = launch_force_copy(sys, prec == MDG_PREC_FP64);
+        if (rc) return rc;
+        sys->force_prec = prec;
+    }
+    rc = launch_drift(sys, dt, prec, pot_rcut_of(s), s->periodic, 1, 1);
+    if (rc) return rc;
+    for (int k = 0; k < s->nstages; ++k) {
+        rc = launch_stage(sys, e->d.dev, ps, prec, s->stages[k]);
+        if (rc) return rc;
+    }
+    sys->force_prec = prec;
+    return launch_kick(sys, dt, prec);
+}
+
+int mdg_verlet_make_step(mdg_solver* s, mdg_system* sys, double dt) {
+    PotSet ps;
+    int rc = check_ready(s, sys, &ps);
+    if (rc) return rc;
+    if (s->precision == MDG_PREC_MIXED) {
+        // Pair::prepare's rcut assignment and boundary flags, then the
+        // offsets the mixed kernels read
+        rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
+        if (rc) return rc;
+    }
+    rc = step_impl(s, sys, ps, dt);
+    if (rc) return rc;
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    return MDG_OK;
+}
+
+int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
+    PotSet ps;
+    int rc = check_ready(s, sys, &ps);
+    if (rc) return rc;
+    cudaStream_t st = sys->ctx->stream;
+    cudaEvent_t ev;
+    MDG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    int prec = s->precision;
+    if (prec == MDG_PREC_MIXED) {
+        // prepare once (rcut, boundary flags); rebuild first if that or an
+        // upload changed what the list was built from
+        rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
+        if (rc) goto done;
+        int need = 0;
+        rc = mdg_nlist_decide(sys, &need);
+        if (rc) goto done;
+        if (need) {
+            rc = mdg_nlist_update(sys, -1.0, 0);
+            if (rc && rc != MDG_ERR_RANGE) goto done;
+        }
+        rc = launch_offsets(sys);
+        if (rc) goto done;
+    }
+    for (long k = 0; k < steps; ++k) {
+        cudaError_t ce = cudaMemsetAsync(&sys->dstat->need_rebuild, 0, sizeof(uint32_t), st);
+        if (ce != cudaSuccess) {
+            rc = cuda_status(ce, "memset");
+            goto done;
+        }
+        if (sys->force_prec != prec) {
+            rc = launch_force_copy(sys, prec == MDG_PREC_FP64);
+            if (rc) goto done;
+            sys->force_prec = prec;
+        }
+        {
+            cudaEvent_t t0 = timer_begin(sys->ctx);
+            rc = launch_drift(sys, dt, prec, pot_rcut_of(s), s->periodic, 1, 1);
+            timer_end(sys->ctx, MDG_TIME_DRIFT, t0);
+        }
+        if (rc) goto done;
+        // the rebuild flag is final once the drift pass is done
+        ce = cudaMemcpyAsync(&sys->hstat->need_rebuild, &sys->dstat->need_rebuild, sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, st);
+        if (ce == cudaSuccess) ce = cudaEventRecord(ev, st);
+        if (ce != cudaSuccess) {
+            rc = cuda_status(ce, "flag copy");
+            goto done;
+        }
+        for (int q = 0; q < s->nstages; ++q) {
+            cudaEvent_t t0 = timer_begin(sys->ctx);
+            rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q]);
+            timer_end(sys->ctx, s->stages[q] == 0 ? MDG_TIME_DENSITY : MDG_TIME_FORCES, t0);
+            if (rc) goto done;
+        }
+        sys->force_prec = prec;
+        {
+            cudaEvent_t t0 = timer_begin(sys->ctx);
+            rc = launch_kick(sys, dt, prec);
+            timer_end(sys->ctx, MDG_TIME_KICK, t0);
+        }
+        if (rc) goto done;
+        // overlap: wait for the flag while the force kernels run
+        ce = cudaEventSynchronize(ev);
+        if (ce != cudaSuccess) {
+            rc = cuda_status(ce, "event");
+            goto done;
+        }
+        if (sys->hstat->need_rebuild) {
+            cudaEvent_t t0 = timer_begin(sys->ctx);
+            rc = nlist_build(sys, -1.0, 0);
+            timer_end(sys->ctx, MDG_TIME_REBUILD, t0);
+            if (rc && rc != MDG_ERR_RANGE) goto done;
+            rc = launch_trig(sys);
+            if (rc) goto done;
+            if (prec == MDG_PREC_MIXED) {
+                rc = launch_offsets(sys);
+                if (rc) goto done;
+            }
+        }
+    }
+    {
+        cudaError_t ce = cudaStreamSynchronize(st);
+        if (ce != cudaSuccess) rc = cuda_status(ce, "run");
+    }
+done:
+    cudaEventDestroy(ev);
+    return rc;
+}
+
+int mdg_run_host(mdg_solver* s, mdg_system* sys, double dt, long steps, double* pos, double* vel, double* force) {
+    if (!s || !sys || !pos || !vel) return MDG_ERR_INVALID;
+    int rc = mdg_system_set_positions(sys, pos);
+    if (rc) return rc;
+    rc = mdg_system_set_velocities(sys, vel);
+    if (rc) return rc;
+    rc = mdg_run(s, sys, dt, steps);
+    if (rc && rc != MDG_ERR_RANGE) return rc;
+    rc = mdg_system_get_positions(sys, pos);
+    if (rc) return rc;
+    rc = mdg_system_get_velocities(sys, vel);
+    if (rc) return rc;
+    if (force) rc = mdg_system_get_forces(sys, force);
+    return rc;
+}
+
+int mdg_system_measure(mdg_system* sys, mdg_state* out) {
+    if (!sys || !out) return MDG_ERR_INVALID;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    double r[11];
+    int rc = launch_measure(sys, r);
+    if (rc) return rc;
+    out->Ep = r[0];
+    out->Em = r[1];
+    out->virial = r[2];
+    out->KE = r[7];
+    out->Etot = r[0] + r[1] + r[7];
+    out->vcom[0] = r[8];
+    out->vcom[1] = r[9];
+    out->vcom[2] = r[10];
+    return MDG_OK;
+}
+
+int mdg_system_flags(mdg_system* sys, uint32_t* flags) {
+    if (!sys || !flags) return MDG_ERR_INVALID;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    cudaStream_t st = sys->ctx->stream;
+    MDG_CUDA(cudaMemcpyAsync(sys->hstat, sys->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    *flags = sys->hstat->flags;
+    MDG_CUDA(cudaMemsetAsync(&sys->dstat->flags, 0, sizeof(uint32_t), st));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    return MDG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,170 @@
+// mdg_host.h — host-side objects behind the opaque C-ABI handles.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "mdg_internal.cuh"
+
+namespace mdg {
+
+void set_error(const std::string& msg);
+int cuda_status(cudaError_t e, const char* what);
+
+#define MDG_CUDA(call)                                            \
+    do {                                                          \
+        cudaError_t e__ = (call);                                 \
+        if (e__ != cudaSuccess) return ::mdg::cuda_status(e__, #call); \
+    } while (0)
+
+#define MDG_LAUNCHED(ctx)                                            \
+    do {                                                             \
+        (ctx)->launches++;                                           \
+        cudaError_t e__ = cudaGetLastError();                        \
+        if (e__ != cudaSuccess) return ::mdg::cuda_status(e__, "kernel launch"); \
+    } while (0)
+
+// Fields permuted together at every rebuild.
+enum F64Field {
+    RX, RY, RZ, VX, VY, VZ, FX, FY, FZ, MASS, RCUT, RNS, EP, EM, NC,
+    V0, V1, V2, V3, V4, V5, V6, V7, V8, NF64
+};
+enum U32Field { ORIG, UID, NU32 };
+enum U16Field { KIND, TAG, NU16 };
+
+struct DevArray {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace mdg
+
+struct mdg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t launches = 0;
+    int num_sms = 0;
+    // per-stage event timing (mdg_ctx_set_timing)
+    int timing = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending[5];
+    double stage_ms[5] = {0, 0, 0, 0, 0};
+    uint64_t stage_n[5] = {0, 0, 0, 0, 0};
+};
+
+namespace mdg {
+// Records a start event for `which` when timing is on (else returns null).
+cudaEvent_t timer_begin(mdg_ctx* ctx);
+void timer_end(mdg_ctx* ctx, int which, cudaEvent_t start);
+}  // namespace mdg
+
+struct mdg_potential {
+    int type = 0;  // 1 pair (LJsCut), 2 EAM
+    double rcut = 0.0;
+    // LJsCut
+    double a = 0, s = 0, s6 = 0, lj1 = 0, lj2 = 0, factor = 0;
+    // EAM host tables (padded by one element) and device copies
+    int Nr1 = 0, Nrh1 = 0;
+    double dr = 0, drh = 0, dr1 = 0, drh1 = 0;
+    std::vector<double> Rho, dRho, Vpar, dVpar, Femb, dFemb;
+    int device = -1;
+    double* d_tab64 = nullptr;   // Rho,dRho,Vpar,dVpar (Nr1+1 each), Femb,dFemb (Nrh1+1 each)
+    float4* d_tab32 = nullptr;   // rho_c, v_c (Nr1 each), f_c (Nrh1)
+};
+
+struct mdg_solver {
+    int multi = 0;
+    int nkinds = 1;
+    int periodic = 0;
+    int precision = MDG_PREC_FP64;
+    int nstages = 0;
+    int stages[2] = {0, 0};  // 0 charge, 1 forces
+    mdg_potential* pot[mdg::kMaxKinds][mdg::kMaxKinds] = {};
+};
+
+struct mdg_system {
+    mdg_ctx* ctx = nullptr;
+    mdg_domain dom{};
+    int dim = 3;
+    size_t n = 0;
+    size_t np = 0;  // n rounded up to 32
+
+    // permuted fields, double-buffered (cur = index of the live buffer)
+    int cur = 0;
+    double* f64[mdg::NF64][2] = {};
+    float* f32[3][2] = {};
+    uint32_t* u32[mdg::NU32][2] = {};
+    uint16_t* u16[mdg::NU16][2] = {};
+
+    // rebuilt per list build (slot order)
+    double* Rc[3] = {};        // cell centres
+    uint32_t* cellp = nullptr; // packed local cell coordinates
+    float4* pos32 = nullptr;   // offsets from the cell centre + w (EAM F')
+    float4* o0 = nullptr;      // offsets at the rebuild (skin test, mixed form)
+    double* r0[3] = {};        // positions at the rebuild (skin test, FP64 form)
+    double* saved_rcut = nullptr;
+    double* saved_rns = nullptr;
+    uint32_t* saved_uid = nullptr;
+    uint32_t* slot_of = nullptr;  // caller index -> slot
+    uint8_t* bc = nullptr;        // Periodic boundary flag
+    double* Fp64 = nullptr;       // F'(nc) per kind column [nk][np] (FP64 form)
+    float* Fp32 = nullptr;        // F'(rho) per kind column [nk][np] (mixed Multi)
+    float* trig32 = nullptr;      // (skin/2)^2 per atom for the mixed half-skin test
+    int force_prec = MDG_PREC_FP64;  // arithmetic of the forces last computed
+
+    // rebuild scratch
+    uint32_t* key = nullptr;
+    uint32_t* rank = nullptr;
+    uint32_t* src = nullptr;
+    uint32_t* bin_count = nullptr;
+    uint32_t* bin_start = nullptr;  // nbins + 1
+    uint32_t* scan_tmp = nullptr;
+    size_t bin_cap = 0;
+    double* part = nullptr;  // per-block bounds partials
+    size_t part_cap = 0;
+
+    // neighbour list (ELL)
+    uint32_t* nbr = nullptr;
+    uint32_t* ncnt = nullptr;
+    int K = 0;        // capacity per atom (self excluded)
+    int half = 0;
+    int have_list = 0;
+    uint64_t rebuilds = 0;
+
+    // device status + grid
+    mdg::DevStatus* dstat = nullptr;
+    mdg::GridParams* dgrid = nullptr;
+    mdg::GridParams grid{};        // host copy of the last rebuild
+    mdg::GridParams* hgrid = nullptr;  // pinned
+    mdg::DevStatus* hstat = nullptr;   // pinned
+    double* red = nullptr;             // reduction scratch (device)
+    double* hred = nullptr;            // pinned
+    int dirty = 1;                     // host-side changes since the last list
+
+    // pinned staging for host transfers
+    void* pin = nullptr;
+    size_t pin_bytes = 0;
+
+    double* cur64(int f) { return f64[f][cur]; }
+    float* cur32(int c) { return f32[c][cur]; }
+    uint32_t* curu32(int f) { return u32[f][cur]; }
+    uint16_t* curu16(int f) { return u16[f][cur]; }
+};
+
+namespace mdg {
+int system_alloc(mdg_system* sys);
+void system_free(mdg_system* sys);
+int nlist_build(mdg_system* sys, double kbuf, int half);
+int potset_build(mdg_solver* s, mdg_system* sys, PotSet* out);
+int pot_upload(mdg_potential* p, int device);
+int run_prepare(mdg_solver* s, mdg_system* sys, const PotSet& ps, int check_rcut);
+int run_stage(mdg_solver* s, mdg_system* sys, const PotSet& ps, int stage);
+int run_virials(mdg_solver* s, mdg_system* sys, const PotSet& ps);
+int run_drift(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt);
+int run_kick(mdg_solver* s, mdg_system* sys, double dt);
+int run_decide(mdg_system* sys);
+int ensure_pinned(mdg_system* sys, size_t bytes);
+}  // namespace mdg
