@@ -500,12 +500,24 @@ int mdg_ctx_create(int device, mdg_ctx** out) {
     return MDG_OK;
 }
 
-int mdg_ctx_destroy(mdg_ctx* ctx) {
-    if (!ctx) return MDG_ERR_INVALID;
+static void ctx_release(mdg_ctx* ctx) {
+    if (--ctx->refs > 0) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    for (int w = 0; w < 5; ++w)
+        for (auto& pr : ctx->ev_pending[w]) {
+            cudaEventDestroy(pr.first);
+            cudaEventDestroy(pr.second);
+        }
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
+}
+
+int mdg_ctx_destroy(mdg_ctx* ctx) {
+    if (!ctx || ctx->closed) return MDG_ERR_INVALID;
+    ctx->closed = 1;
+    ctx_release(ctx);
     return MDG_OK;
 }
 
@@ -583,16 +595,19 @@ int mdg_system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n, mdg_syst
         delete s;
         return rc;
     }
+    ctx->refs++;
     *out = s;
     return MDG_OK;
 }
 
 int mdg_system_destroy(mdg_system* sys) {
     if (!sys) return MDG_ERR_INVALID;
-    cudaSetDevice(sys->ctx->device);
-    cudaStreamSynchronize(sys->ctx->stream);
+    mdg_ctx* ctx = sys->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
     system_free(sys);
     delete sys;
+    ctx_release(ctx);
     return MDG_OK;
 }
 

@@ -47,6 +47,10 @@ struct mdg_ctx {
     cudaStream_t stream = nullptr;
     uint64_t launches = 0;
     int num_sms = 0;
+    // lifetime: the caller's handle plus one per live system; the context
+    // is freed when both the handle is destroyed and no system remains
+    int refs = 1;
+    int closed = 0;
     // per-stage event timing (mdg_ctx_set_timing)
     int timing = 0;
     std::vector<cudaEvent_t> ev_pool;

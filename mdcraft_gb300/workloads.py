@@ -75,14 +75,18 @@ def _wrap_inside(r, lo, L):
     return r
 
 
-def lj_argon_fcc(ncell=10, seed=1, T=100.0):
-    """Config 1 (LJ argon fcc 10^3 = 4000 atoms)."""
+def lj_argon_fcc(ncell=10, seed=1, T=100.0, jitter=0.0):
+    """Config 1 (LJ argon fcc 10^3 = 4000 atoms; perfect lattice unless a
+    Gaussian jitter, as a fraction of a, is asked for)."""
     a = 0.526
     sigma, eps = 0.3405, 0.0104 * EV
     rc = 2.5 * sigma
     skin = 0.03
     L = ncell * a
+    rng = np.random.default_rng(seed)
     r = fcc_positions(ncell, ncell, ncell, a) + 0.25 * a
+    if jitter:
+        r = r + rng.standard_normal(r.shape) * (jitter * a)
     atoms = new_atoms(len(r))
     atoms["r"] = _wrap_inside(r, 0.0, L)
     atoms["m"] = AR_MASS
@@ -90,7 +94,6 @@ def lj_argon_fcc(ncell=10, seed=1, T=100.0):
     atoms["rns"] = rc + skin
     atoms["uid"] = np.arange(1, len(r) + 1)
     atoms["kind"] = 0
-    rng = np.random.default_rng(seed)
     atoms["v"] = maxwell_boltzmann(rng, atoms["m"].copy(), T)
     params = dict(kind="lj", a=eps, s=sigma, rcut=rc, skin=skin, dt=0.002, steps=1000)
     return (*_finish(atoms, (0, 0, 0), (L, L, L)), params)

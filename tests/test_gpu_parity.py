@@ -268,7 +268,7 @@ def test_half_list_matches_oracle():
 
 # ---- forces / energies ------------------------------------------------------
 FORCE_CASES = [
-    ("lj_argon", lambda: W.lj_argon_fcc()),
+    ("lj_argon", lambda: W.lj_argon_fcc(jitter=0.01)),
     ("eam_cu", lambda: W.eam_cu_fcc(ncell=10)),
     ("nial_multi", lambda: W.eam_nial_b2(ncell=8)),
 ]
@@ -290,7 +290,8 @@ def test_fp64_forces_energies_match_oracle(case):
     a = g["sys"].download()
     fo = o["atoms"]["f"]
     scale = np.sqrt(np.mean(np.sum(fo ** 2, axis=1)))
-    assert np.max(np.abs(a["f"] - fo)) <= FP64_REL * scale * 10
+    # per-atom sums of ~50-80 pair terms in another order: relative to the RMS force
+    assert np.max(np.abs(a["f"] - fo)) <= FP64_REL * scale
     for key in ("Ep", "Em", "nc"):
         ref = o["atoms"][key]
         assert np.max(np.abs(a[key] - ref)) <= FP64_REL * max(np.max(np.abs(ref)), 1e-300)
