@@ -316,6 +316,22 @@ __device__ __forceinline__ float dcubic(const float4 c, float u) {
 // the cutoff); bit 31 marks them.
 constexpr uint32_t kWrapBit = 1u << 31;
 
+// Cutoff membership of a pair. The FP32 r^2 decides unless it lies within
+// 1e-5 (relative) of rc^2; those rare pairs are decided on the FP64
+// positions, so the mixed form cuts exactly the pairs the FP64 form cuts
+// (the potentials are discontinuous at rc, so a flipped pair would change
+// forces by a whole pair term).
+__device__ __forceinline__ bool cut_in(const FArgs& A, int i, uint32_t j, float r2, float r2c, double R2cut) {
+    if (r2 < 1e-15f) return false;
+    float band = 1e-5f * r2c;
+    if (r2 < r2c - band) return true;
+    if (r2 > r2c + band) return false;
+    double dx = shortest1(A.rx[j] - A.rx[i], A.L[0], A.periodic[0]);
+    double dy = shortest1(A.ry[j] - A.ry[i], A.L[1], A.periodic[1]);
+    double dz = shortest1(A.rz[j] - A.rz[i], A.L[2], A.periodic[2]);
+    return dx * dx + dy * dy + dz * dz <= R2cut;
+}
+
 template <bool MULTI>
 __global__ void __launch_bounds__(kBlock) k_lj_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -326,6 +342,7 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(FArgs A, const PotSet* __re
     const bool per = ps->periodic;
     const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
     float r2c = ps->p[0][0].r2cut_f, l1 = ps->p[0][0].lj1_f, l2 = ps->p[0][0].lj2_f, mh = ps->p[0][0].mhf_f;
+    double R2c = ps->p[0][0].R2cut;
     Kahan3 acc;
     const uint32_t* row = A.nbr + i;
     for (int k = 0; k < cnt; ++k) {
@@ -335,12 +352,12 @@ __global__ void __launch_bounds__(kBlock) k_lj_mixed(FArgs A, const PotSet* __re
         float4 pj = __ldg(A.pos32 + j);
         if (MULTI) {
             const PotParams& P = ps->p[ki][(A.kind[j] & 3)];
-            r2c = P.r2cut_f; l1 = P.lj1_f; l2 = P.lj2_f; mh = P.mhf_f;
+            r2c = P.r2cut_f; l1 = P.lj1_f; l2 = P.lj2_f; mh = P.mhf_f; R2c = P.R2cut;
         }
         float dx, dy, dz;
         pair_vec32(e, pi, pj, csf, dx, dy, dz);
         float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (r2 > r2c || r2 < 1e-15f) continue;
+        if (!cut_in(A, i, j, r2, r2c, R2c)) continue;
         float r2inv = __frcp_rn(r2);
         float r6inv = r2inv * r2inv * r2inv;
         float pref = mh * fmaf(l1, r6inv, -l2) * r6inv * r2inv;
@@ -380,6 +397,7 @@ __global__ void __launch_bounds__(kBlock) k_density_mixed(FArgs A, const PotSet*
         int cnt = A.ncnt[i];
         const PotParams* P = &ps->p[ki][0];
         float r2c = P->r2cut_f, idr = P->inv_dr_f;
+        double R2c = P->R2cut;
         int Nr1 = P->Nr1;
         const float4* tab = P->rho_c;
         const uint32_t* row = A.nbr + i;
@@ -390,13 +408,13 @@ __global__ void __launch_bounds__(kBlock) k_density_mixed(FArgs A, const PotSet*
             float4 pj = __ldg(A.pos32 + j);
             if (MULTI) {
                 P = &ps->p[ki][(A.kind[j] & 3)];
-                r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; tab = P->rho_c;
+                r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; tab = P->rho_c; R2c = P->R2cut;
                 if (P->type != 2) continue;
             }
             float dx, dy, dz;
             pair_vec32(e, pi, pj, csf, dx, dy, dz);
             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (r2 > r2c || r2 < 1e-15f) continue;
+            if (!cut_in(A, i, j, r2, r2c, R2c)) continue;
             float t = sqrtf(r2) * idr;
             int nn = (int)t;
             if (nn >= Nr1) continue;
@@ -427,6 +445,7 @@ __global__ void __launch_bounds__(kBlock) k_eam_mixed(FArgs A, const PotSet* __r
     const bool per = ps->periodic;
     const PotParams* P = &ps->p[ki][0];
     float r2c = P->r2cut_f, idr = P->inv_dr_f;
+    double R2c = P->R2cut;
     int Nr1 = P->Nr1;
     const float4* rt = P->rho_c;
     const float4* vt = P->v_c;
@@ -443,14 +462,14 @@ __global__ void __launch_bounds__(kBlock) k_eam_mixed(FArgs A, const PotSet* __r
             int kj = (A.kind[j] & 3);
             P = &ps->p[ki][kj];
             if (P->type != 2) continue;
-            r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; rt = P->rho_c; vt = P->v_c;
+            r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; rt = P->rho_c; vt = P->v_c; R2c = P->R2cut;
             Fpj = A.Fp32[(size_t)ki * A.np + j];
             Fpi = A.Fp32[(size_t)kj * A.np + i];
         }
         float dx, dy, dz;
         pair_vec32(e, pi, pj, csf, dx, dy, dz);
         float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (r2 > r2c || r2 < 1e-15f) continue;
+        if (!cut_in(A, i, j, r2, r2c, R2c)) continue;
         float r = sqrtf(r2);
         float t = r * idr;
         int nn = (int)t;
