@@ -756,15 +756,21 @@ static int host_lists(mdg_system* sys, std::vector<uint64_t>& off, std::vector<u
         if (sys->K) MDG_CUDA(cudaMemcpyAsync(nbr.data(), sys->nbr, nbr.size() * 4, cudaMemcpyDeviceToHost, st));
         MDG_CUDA(cudaStreamSynchronize(st));
     }
+    // self entry first (the reference lists each atom as its own neighbour),
+    // then the stored entries without the self padding
     off.assign(n + 1, 0);
-    for (size_t c = 0; c < n; ++c) off[c + 1] = off[c] + cnt[slot[c]] + 1;
-    idx.assign(off[n], 0);
+    idx.clear();
+    idx.reserve(n * 64);
     for (size_t c = 0; c < n; ++c) {
         uint32_t s = slot[c];
-        uint64_t* o = idx.data() + off[c];
-        o[0] = c;
-        for (uint32_t k = 0; k < cnt[s]; ++k) o[k + 1] = orig[nbr[(size_t)k * np + s] & kJMask];
-        std::sort(o, o + cnt[s] + 1);
+        size_t b = idx.size();
+        idx.push_back(c);
+        for (uint32_t k = 0; k < cnt[s]; ++k) {
+            uint32_t j = nbr[nidx((int)k, s, np)] & kJMask;
+            if (j != s) idx.push_back(orig[j]);
+        }
+        std::sort(idx.begin() + b, idx.end());
+        off[c + 1] = idx.size();
     }
     return MDG_OK;
 }
@@ -773,14 +779,10 @@ int mdg_nlist_total(mdg_system* sys, size_t* total) {
     if (!sys || !total) return MDG_ERR_INVALID;
     if (!sys->have_list) return MDG_ERR_STATE;
     MDG_CUDA(cudaSetDevice(sys->ctx->device));
-    std::vector<uint32_t> cnt(sys->n);
-    if (sys->n) {
-        MDG_CUDA(cudaMemcpyAsync(cnt.data(), sys->ncnt, sys->n * 4, cudaMemcpyDeviceToHost, sys->ctx->stream));
-        MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
-    }
-    size_t t = 0;
-    for (uint32_t c : cnt) t += c + 1;
-    *total = t;
+    std::vector<uint64_t> off, ix;
+    int rc = host_lists(sys, off, ix);
+    if (rc) return rc;
+    *total = ix.size();
     return MDG_OK;
 }
 

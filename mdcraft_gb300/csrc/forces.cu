@@ -133,7 +133,7 @@ __device__ __forceinline__ void visit64(const FArgs& A, int i, Fn&& fn) {
     int cnt = A.ncnt[i];
     // main pass (the self entry contributes nothing: r2 < 1e-15)
     for (int k = 0; k < cnt; ++k) {
-        uint32_t j = A.nbr[(size_t)k * A.np + i] & kJMask;
+        uint32_t j = A.nbr[nidx(k, i, A.np)] & kJMask;
         int kj = MULTI ? (A.kind[j] & 3) : 0;
         double dx = A.rx[j] - xi, dy = A.ry[j] - yi, dz = A.rz[j] - zi;
         double r2 = dx * dx + dy * dy + dz * dz;
@@ -142,7 +142,7 @@ __device__ __forceinline__ void visit64(const FArgs& A, int i, Fn&& fn) {
     if (!A.bc[i]) return;
     double rni = A.rns[i];
     for (int k = 0; k < cnt; ++k) {
-        uint32_t j = A.nbr[(size_t)k * A.np + i] & kJMask;
+        uint32_t j = A.nbr[nidx(k, i, A.np)] & kJMask;
         int kj = MULTI ? (A.kind[j] & 3) : 0;
         double dx = A.rx[j] - xi, dy = A.ry[j] - yi, dz = A.rz[j] - zi;
         double rnj = A.rns[j];
@@ -332,38 +332,61 @@ __device__ __forceinline__ bool cut_in(const FArgs& A, int i, uint32_t j, float 
     return dx * dx + dy * dy + dz * dz <= R2cut;
 }
 
+// Cutoff membership from the FP32 r^2, with the rare pairs inside the
+// 1e-5 band around rc^2 (and entries that crossed a periodic face when the
+// solver has no Periodic boundary) settled exactly.
+__device__ __forceinline__ bool pair_in(const FArgs& A, int i, uint32_t e, float r2, float r2c, double R2c,
+                                        bool per) {
+    bool in = r2 >= 1e-15f && r2 <= r2c;
+    if (fabsf(r2 - r2c) <= 1e-5f * r2c) in = cut_in(A, i, e & kJMask, r2, r2c, R2c);
+    return in && (per || !(e & kWrapBit));
+}
+
+// The pair loops below read four list entries with one 16-byte load, then
+// the four neighbour records, so the loads of a group overlap; the four
+// contributions are summed in FP32 and the group sum enters a Kahan sum.
+
 template <bool MULTI>
 __global__ void __launch_bounds__(kBlock) k_lj_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.n || A.tag[i] == 0) return;
     const float4 pi = A.pos32[i];
-    int cnt = A.ncnt[i];
-    int ki = MULTI ? (A.kind[i] & 3) : 0;
+    const int ng = A.ncnt[i] >> 2;
+    const int ki = MULTI ? (A.kind[i] & 3) : 0;
     const bool per = ps->periodic;
     const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
-    float r2c = ps->p[0][0].r2cut_f, l1 = ps->p[0][0].lj1_f, l2 = ps->p[0][0].lj2_f, mh = ps->p[0][0].mhf_f;
-    double R2c = ps->p[0][0].R2cut;
+    const PotParams& P0 = ps->p[ki][0];
+    float r2c = P0.r2cut_f, l1 = P0.lj1_f, l2 = P0.lj2_f, mh = P0.mhf_f;
+    double R2c = P0.R2cut;
     Kahan3 acc;
-    const uint32_t* row = A.nbr + i;
-    for (int k = 0; k < cnt; ++k) {
-        uint32_t e = __ldg(row + (size_t)k * A.np);
-        if (!per && (e & kWrapBit)) continue;
-        uint32_t j = e & kJMask;
-        float4 pj = __ldg(A.pos32 + j);
-        if (MULTI) {
-            const PotParams& P = ps->p[ki][(A.kind[j] & 3)];
-            r2c = P.r2cut_f; l1 = P.lj1_f; l2 = P.lj2_f; mh = P.mhf_f; R2c = P.R2cut;
+    const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
+    for (int g = 0; g < ng; ++g) {
+        const uint4 e4 = __ldg(row + (size_t)g * A.np);
+        const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+        float4 pj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32 + (e[q] & kJMask));
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (MULTI) {
+                const PotParams& P = ps->p[ki][A.kind[e[q] & kJMask] & 3];
+                r2c = P.r2cut_f; l1 = P.lj1_f; l2 = P.lj2_f; mh = P.mhf_f; R2c = P.R2cut;
+            }
+            float dx, dy, dz;
+            pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            bool in = pair_in(A, i, e[q], r2, r2c, R2c, per);
+            float r2inv = __frcp_rn(fmaxf(r2, 1e-12f));
+            float r6inv = r2inv * r2inv * r2inv;
+            float pref = in ? mh * fmaf(l1, r6inv, -l2) * r6inv * r2inv : 0.f;
+            fx = fmaf(dx, pref, fx);
+            fy = fmaf(dy, pref, fy);
+            fz = fmaf(dz, pref, fz);
         }
-        float dx, dy, dz;
-        pair_vec32(e, pi, pj, csf, dx, dy, dz);
-        float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (!cut_in(A, i, j, r2, r2c, R2c)) continue;
-        float r2inv = __frcp_rn(r2);
-        float r6inv = r2inv * r2inv * r2inv;
-        float pref = mh * fmaf(l1, r6inv, -l2) * r6inv * r2inv;
-        acc.add(0, dx * pref);
-        acc.add(1, dy * pref);
-        acc.add(2, dz * pref);
+        acc.add(0, fx);
+        acc.add(1, fy);
+        acc.add(2, fz);
     }
     A.gx[i] = acc.s[0];
     A.gy[i] = acc.s[1];
@@ -389,37 +412,46 @@ __global__ void __launch_bounds__(kBlock) k_density_mixed(FArgs A, const PotSet*
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.n) return;
     const float4 pi = A.pos32[i];
-    int ki = MULTI ? (A.kind[i] & 3) : 0;
+    const int ki = MULTI ? (A.kind[i] & 3) : 0;
     const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
     const bool per = ps->periodic;
     float s = 0.f, c = 0.f;
     if (A.tag[i] != 0) {
-        int cnt = A.ncnt[i];
+        const int ng = A.ncnt[i] >> 2;
         const PotParams* P = &ps->p[ki][0];
         float r2c = P->r2cut_f, idr = P->inv_dr_f;
         double R2c = P->R2cut;
         int Nr1 = P->Nr1;
         const float4* tab = P->rho_c;
-        const uint32_t* row = A.nbr + i;
-        for (int k = 0; k < cnt; ++k) {
-            uint32_t e = __ldg(row + (size_t)k * A.np);
-            if (!per && (e & kWrapBit)) continue;
-            uint32_t j = e & kJMask;
-            float4 pj = __ldg(A.pos32 + j);
-            if (MULTI) {
-                P = &ps->p[ki][(A.kind[j] & 3)];
-                r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; tab = P->rho_c; R2c = P->R2cut;
-                if (P->type != 2) continue;
+        const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
+        for (int g = 0; g < ng; ++g) {
+            const uint4 e4 = __ldg(row + (size_t)g * A.np);
+            const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+            float4 pj[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32 + (e[q] & kJMask));
+            float part = 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                bool eam = true;
+                if (MULTI) {
+                    P = &ps->p[ki][A.kind[e[q] & kJMask] & 3];
+                    r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; tab = P->rho_c; R2c = P->R2cut;
+                    eam = P->type == 2;
+                }
+                float dx, dy, dz;
+                pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                bool in = eam && pair_in(A, i, e[q], r2, r2c, R2c, per);
+                float t = sqrtf(r2) * idr;
+                int nn = (int)t;
+                in = in && nn < Nr1;
+                nn = in ? nn : 0;
+                float u = t - (float)nn;
+                float v = in ? cubic(__ldg(tab + nn), u) : 0.f;
+                part += v;
             }
-            float dx, dy, dz;
-            pair_vec32(e, pi, pj, csf, dx, dy, dz);
-            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (!cut_in(A, i, j, r2, r2c, R2c)) continue;
-            float t = sqrtf(r2) * idr;
-            int nn = (int)t;
-            if (nn >= Nr1) continue;
-            float u = t - (float)nn;
-            ksum_add(s, c, cubic(__ldg(tab + nn), u));
+            ksum_add(s, c, part);
         }
     }
     float rho = s;
@@ -439,8 +471,8 @@ __global__ void __launch_bounds__(kBlock) k_eam_mixed(FArgs A, const PotSet* __r
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.n || A.tag[i] == 0) return;
     const float4 pi = A.pos32b[i];
-    int cnt = A.ncnt[i];
-    int ki = MULTI ? (A.kind[i] & 3) : 0;
+    const int ng = A.ncnt[i] >> 2;
+    const int ki = MULTI ? (A.kind[i] & 3) : 0;
     const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
     const bool per = ps->periodic;
     const PotParams* P = &ps->p[ki][0];
@@ -449,47 +481,59 @@ __global__ void __launch_bounds__(kBlock) k_eam_mixed(FArgs A, const PotSet* __r
     int Nr1 = P->Nr1;
     const float4* rt = P->rho_c;
     const float4* vt = P->v_c;
-    float Fpi = pi.w;
     Kahan3 acc;
-    const uint32_t* row = A.nbr + i;
-    for (int k = 0; k < cnt; ++k) {
-        uint32_t e = __ldg(row + (size_t)k * A.np);
-        if (!per && (e & kWrapBit)) continue;
-        uint32_t j = e & kJMask;
-        float4 pj = __ldg(A.pos32b + j);
-        float Fpj = pj.w;
-        if (MULTI) {
-            int kj = (A.kind[j] & 3);
-            P = &ps->p[ki][kj];
-            if (P->type != 2) continue;
-            r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; rt = P->rho_c; vt = P->v_c; R2c = P->R2cut;
-            Fpj = A.Fp32[(size_t)ki * A.np + j];
-            Fpi = A.Fp32[(size_t)kj * A.np + i];
+    const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
+    for (int g = 0; g < ng; ++g) {
+        const uint4 e4 = __ldg(row + (size_t)g * A.np);
+        const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+        float4 pj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32b + (e[q] & kJMask));
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float Fpi = pi.w, Fpj = pj[q].w;
+            bool eam = true;
+            if (MULTI) {
+                uint32_t j = e[q] & kJMask;
+                int kj = A.kind[j] & 3;
+                P = &ps->p[ki][kj];
+                eam = P->type == 2;
+                r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; rt = P->rho_c; vt = P->v_c; R2c = P->R2cut;
+                Fpj = A.Fp32[(size_t)ki * A.np + j];
+                Fpi = A.Fp32[(size_t)kj * A.np + i];
+            }
+            float dx, dy, dz;
+            pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            bool in = eam && pair_in(A, i, e[q], r2, r2c, R2c, per);
+            float r = sqrtf(r2);
+            float t = r * idr;
+            int nn = (int)t;
+            in = in && nn < Nr1;
+            nn = in ? nn : 0;
+            float u = t - (float)nn;
+            float4 cr = __ldg(rt + nn);
+            float4 cv = __ldg(vt + nn);
+            float drho = dcubic(cr, u) * idr;
+            float V = cubic(cv, u);
+            float dV = dcubic(cv, u) * idr;
+            float rinv = __frcp_rn(fmaxf(r, 1e-6f));
+            float FF = fmaf(Fpi + Fpj, drho, (dV * r - V) * (rinv * rinv)) * rinv;
+            FF = in ? FF : 0.f;
+            fx = fmaf(FF, dx, fx);
+            fy = fmaf(FF, dy, fy);
+            fz = fmaf(FF, dz, fz);
         }
-        float dx, dy, dz;
-        pair_vec32(e, pi, pj, csf, dx, dy, dz);
-        float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (!cut_in(A, i, j, r2, r2c, R2c)) continue;
-        float r = sqrtf(r2);
-        float t = r * idr;
-        int nn = (int)t;
-        if (nn >= Nr1) continue;
-        float u = t - (float)nn;
-        float4 cr = __ldg(rt + nn);
-        float4 cv = __ldg(vt + nn);
-        float drho = dcubic(cr, u) * idr;
-        float V = cubic(cv, u);
-        float dV = dcubic(cv, u) * idr;
-        float rinv = __frcp_rn(r);
-        float FF = fmaf(Fpi + Fpj, drho, (dV * r - V) * (rinv * rinv)) * rinv;
-        acc.add(0, FF * dx);
-        acc.add(1, FF * dy);
-        acc.add(2, FF * dz);
+        acc.add(0, fx);
+        acc.add(1, fy);
+        acc.add(2, fz);
     }
     A.gx[i] = acc.s[0];
     A.gy[i] = acc.s[1];
     A.gz[i] = acc.s[2];
 }
+
 
 // ---------------------------------------------------------------------------
 // host side

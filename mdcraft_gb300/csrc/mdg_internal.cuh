@@ -76,6 +76,16 @@ __host__ __device__ inline void unpack_cell(uint32_t p, int& cx, int& cy, int& c
     cz = (int)((p >> 20) & 1023u);
 }
 
+// Position of list entry k of atom (slot) i: entries are stored in groups of
+// four per atom ("ELL4"), so a thread reads four neighbours with one 16-byte
+// load and a warp reads 512 contiguous bytes per group. Lists are padded to
+// a multiple of four with self entries (r = 0, excluded by every force
+// kernel's r^2 >= 1e-15 test).
+__host__ __device__ inline size_t nidx(int k, size_t i, size_t np) {
+    return (((size_t)(k >> 2) * np + i) << 2) + (size_t)(k & 3);
+}
+constexpr uint32_t kSelfCode = 0x15u << kJBits;  // image (0,0,0)
+
 // Image offset encoded in a list entry (2 bits per axis, value+1).
 __device__ inline float image_shift(uint32_t e, int axis, float cs) {
     uint32_t b = (e >> (kJBits + 2 * axis)) & 3u;

@@ -455,14 +455,17 @@ __global__ void __launch_bounds__(kBlock) k_nbuild(NbArgs A, const GridParams* _
                             int own[3] = {cx, cy, cz};
                             if (dlt != lc[a] - own[a]) code |= 1u << 6;
                         }
-                        if (cnt < A.K) A.nbr[(size_t)cnt * A.np + i] = j | (code << kJBits);
+                        if (cnt < A.K) A.nbr[nidx(cnt, i, A.np)] = j | (code << kJBits);
                         ++cnt;
                     }
                 }
             }
         }
         if (active) {
-            A.ncnt[i] = cnt < A.K ? cnt : A.K;
+            // pad to a multiple of four with self entries
+            int padded = (cnt + 3) & ~3;
+            for (int k = cnt; k < padded && k < A.K; ++k) A.nbr[nidx(k, i, A.np)] = i | kSelfCode;
+            A.ncnt[i] = padded < A.K ? padded : A.K;
             if (cnt > A.K) atomicOr(&A.st->flags, FLAG_OVERFLOW);
             atomicMax(&A.st->max_count, (uint32_t)cnt);
             A.r0x[i] = xi;
@@ -489,7 +492,7 @@ __global__ void k_optimize_rns(int n, int np, double kbuf, int have_list, const 
         hmax = ri + ri;
         int c = ncnt[i];
         for (int k = 0; k < c; ++k) {
-            uint32_t j = nbr[(size_t)k * np + i] & kJMask;
+            uint32_t j = nbr[nidx(k, i, np)] & kJMask;
             double h = ri + rcut[j];
             hmax = h > hmax ? h : hmax;
         }
