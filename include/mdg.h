@@ -207,6 +207,22 @@ int mdg_run_host(mdg_solver* s, mdg_system* sys, double dt, long steps,
 /* FP64 device reduction of measure_state (md_test_utils.h:214-239). Uses
  * the per-atom Ep, Em, V of the last mdg_solver_virials call. */
 int mdg_system_measure(mdg_system* sys, mdg_state* out);
+/* The reduction of mdg_system_measure on device arrays the caller owns,
+ * allocating nothing: for callers that cannot call cudaMalloc (code running
+ * under another component's device-memory pool, latency-critical loops that
+ * cannot afford an allocation's synchronisation, plug-in hosts that only
+ * hand out pre-registered buffers). No counterpart in the reference.
+ * Inputs (device, FP64, n atoms): d_m[n]; d_v[3n] = vx|vy|vz; d_Ep[n];
+ * d_Em[n]; d_V[9n] = the nine virial components, component-major. Output:
+ * d_out[8] (device) = {Ep, Em, KE, Etot, virial trace, vcom x, y, z}.
+ * Launches on `stream` (a cudaStream_t; NULL = default stream) and does not
+ * synchronise. Scratch is a static device array of 256 KB held by every GPU
+ * that loads the library: at most 8,388,608 atoms per call (larger n fails
+ * with MDG_ERR_INVALID); calls whose kernels overlap on the GPU race on it.
+ * The first call on a device looks the array up (cudaGetSymbolAddress); make
+ * it before any stream capture. */
+int mdg_measure_static(const double* d_m, const double* d_v, const double* d_Ep, const double* d_Em,
+                       const double* d_V, size_t n, double* d_out, void* stream);
 /* Error/diagnostic flags accumulated on the device since the last call
  * (bit 0 atom out of grid, bit 1 neighbour overflow, bit 2 EAM table range,
  * bit 3 non-finite force); clears them. */
