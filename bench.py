@@ -248,7 +248,6 @@ def run_mdg(args, rank, world, local):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     ctx.synchronize()
-    ctx.set_timing(True)
     rb0 = nl.rebuilds()
     l0 = ctx.launches()
     clocks = Clocks(local)
@@ -256,7 +255,7 @@ def run_mdg(args, rank, world, local):
     torch.cuda.synchronize()
     clocks.start()
     e0.record(stream)
-    stepper.run(sysg, p["dt"], args.steps)
+    stepper.run(sysg, p["dt"], args.steps)  # one captured graph: steps + device-side rebuilds
     e1.record(stream)
     ctx.synchronize()
     torch.cuda.synchronize()
@@ -265,6 +264,11 @@ def run_mdg(args, rank, world, local):
     ms = e0.elapsed_time(e1)
     launches = ctx.launches() - l0
     rebuilds = nl.rebuilds() - rb0
+
+    # per-kernel durations: the same loop step by step with CUDA events around
+    # each stage on the engine's stream (events cannot sit inside the graph)
+    ctx.set_timing(True)
+    stepper.run(sysg, p["dt"], min(args.steps, 40))
     fms, fn = ctx.stage_time("forces")
     dms, dn = ctx.stage_time("density")
     drms, drn = ctx.stage_time("drift")

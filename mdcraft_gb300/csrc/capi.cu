@@ -262,6 +262,9 @@ int system_alloc(mdg_system* sys) {
 }
 
 void system_free(mdg_system* sys) {
+    if (sys->run_exec) cudaGraphExecDestroy(sys->run_exec);
+    if (sys->run_graph) cudaGraphDestroy(sys->run_graph);
+    cudaFree(sys->dcounter);
     for (int f = 0; f < NF64; ++f)
         for (int b = 0; b < 2; ++b) cudaFree(sys->f64[f][b]);
     for (int f = 0; f < 3; ++f)
@@ -1068,6 +1071,10 @@ static int check_ready(mdg_solver* s, mdg_system* sys, PotSet* ps) {
         set_error("solver has no potential");
         return MDG_ERR_STATE;
     }
+    if (sys->have_list && sys->half && sys->n) {
+        set_error("the force stages need a full Verlet list (half lists are export-only)");
+        return MDG_ERR_STATE;
+    }
     if (!sys->have_list && sys->n) {
         set_error("no Verlet list: call mdg_nlist_update first");
         return MDG_ERR_STATE;
@@ -1195,10 +1202,200 @@ int mdg_verlet_make_step(mdg_solver* s, mdg_system* sys, double dt) {
     return MDG_OK;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// The driver loop as one CUDA graph: a WHILE node whose body is one Verlet
+// step, the rebuild test and an IF node holding the whole list rebuild. The
+// conditions are set on the device, so a run of any length is one graph
+// launch with no host round trip per step.
+// ---------------------------------------------------------------------------
+namespace mdg {
+
+__global__ void k_rebuild_cond(cudaGraphConditionalHandle h, DevStatus* st) {
+    if (threadIdx.x != 0) return;
+    unsigned need = st->need_rebuild;
+    st->need_rebuild = 0;
+    if (need) st->pad[0] += 1;  // rebuilds done inside graphs
+    cudaGraphSetConditional(h, need ? 1u : 0u);
+}
+
+// One step done; continue while steps remain and no rebuild overflowed its
+// capacities (the host then grows them and resumes).
+__global__ void k_loop_ctrl(cudaGraphConditionalHandle h, unsigned long long* counter, DevStatus* st) {
+    if (threadIdx.x != 0) return;
+    unsigned long long c = *counter;
+    c = c > 0 ? c - 1 : 0;
+    *counter = c;
+    bool go = c > 0 && !(st->build_flags & FLAG_OVERFLOW);
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+__global__ void k_set_counter(unsigned long long* counter, unsigned long long v, DevStatus* st) {
+    if (threadIdx.x == 0) {
+        *counter = v;
+        st->need_rebuild = 0;
+        st->build_flags = 0;
+        st->pad[0] = 0;
+    }
+}
+
+static void graph_free(mdg_system* sys) {
+    if (sys->run_exec) cudaGraphExecDestroy(sys->run_exec);
+    if (sys->run_graph) cudaGraphDestroy(sys->run_graph);
+    sys->run_exec = nullptr;
+    sys->run_graph = nullptr;
+}
+
+// kernels launched by one step / one rebuild (launch accounting)
+static int g_step_kernels = 0, g_rebuild_kernels = 0;
+
+static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt) {
+    graph_free(sys);
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    int prec = s->precision;
+    if (!sys->dcounter) MDG_CUDA(cudaMalloc(&sys->dcounter, sizeof(unsigned long long)));
+    cudaGraph_t g = nullptr;
+    MDG_CUDA(cudaGraphCreate(&g, 0));
+    sys->run_graph = g;
+    cudaGraphConditionalHandle hloop, hrb;
+    MDG_CUDA(cudaGraphConditionalHandleCreate(&hloop, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = hloop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    MDG_CUDA(cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp));
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    MDG_CUDA(cudaGraphConditionalHandleCreate(&hrb, body, 0, cudaGraphCondAssignDefault));
+
+    uint64_t l0 = ctx->launches;
+    MDG_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int rc = launch_drift(sys, dt, prec, s->multi ? -1.0 : s->pot[0][0]->rcut, s->periodic, 1, 1);
+    for (int q = 0; rc == 0 && q < s->nstages; ++q) rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q]);
+    if (rc == 0) rc = launch_kick(sys, dt, prec);
+    if (rc == 0) {
+        k_rebuild_cond<<<1, 32, 0, st>>>(hrb, sys->dstat);
+        ctx->launches++;
+    }
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* ed = nullptr;
+    size_t nd = 0;
+    cudaGraphNodeParams ip = {};
+    cudaGraphNode_t inode = nullptr;
+    if (rc == 0) {
+        cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, &ed, &nd);
+        if (e == cudaSuccess) {
+            ip.type = cudaGraphNodeTypeConditional;
+            ip.conditional.handle = hrb;
+            ip.conditional.type = cudaGraphCondTypeIf;
+            ip.conditional.size = 1;
+            e = cudaGraphAddNode(&inode, cg, deps, ed, nd, &ip);
+        }
+        if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(st, &inode, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (e != cudaSuccess) rc = cuda_status(e, "graph IF node");
+    }
+    if (rc == 0) {
+        k_loop_ctrl<<<1, 32, 0, st>>>(hloop, sys->dcounter, sys->dstat);
+        ctx->launches++;
+    }
+    cudaGraph_t out = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(st, &out);
+    if (rc) return rc;
+    if (e2 != cudaSuccess) return cuda_status(e2, "step capture");
+    g_step_kernels = (int)(ctx->launches - l0);
+
+    l0 = ctx->launches;
+    MDG_CUDA(cudaStreamBeginCaptureToGraph(st, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal));
+    rc = nlist_enqueue(sys);
+    if (rc == 0) rc = launch_trig(sys);
+    e2 = cudaStreamEndCapture(st, &out);
+    if (rc) return rc;
+    if (e2 != cudaSuccess) return cuda_status(e2, "rebuild capture");
+    g_rebuild_kernels = (int)(ctx->launches - l0);
+    ctx->launches -= (uint64_t)g_step_kernels + (uint64_t)g_rebuild_kernels;  // counted when run
+    MDG_CUDA(cudaGraphInstantiate(&sys->run_exec, g, 0));
+    return MDG_OK;
+}
+
+static int run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt, long steps) {
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    long left = steps;
+    for (int round = 0; left > 0 && round < 64; ++round) {
+        uint64_t dtbits;
+        memcpy(&dtbits, &dt, sizeof(dtbits));
+        uint64_t key[4] = {(uint64_t)(uintptr_t)s, dtbits, (uint64_t)s->precision + 2 * (uint64_t)ext(s)->version,
+                           sys->cap_version};
+        if (!sys->run_exec || memcmp(key, sys->run_key, sizeof(key)) != 0) {
+            int rc = build_run_graph(s, sys, ps, dt);
+            if (rc) {
+                graph_free(sys);
+                return rc;
+            }
+            memcpy(sys->run_key, key, sizeof(key));
+        }
+        k_set_counter<<<1, 32, 0, st>>>(sys->dcounter, (unsigned long long)left, sys->dstat);
+        MDG_LAUNCHED(ctx);
+        MDG_CUDA(cudaGraphLaunch(sys->run_exec, st));
+        unsigned long long rem = 0;
+        MDG_CUDA(cudaMemcpyAsync(&rem, sys->dcounter, sizeof(rem), cudaMemcpyDeviceToHost, st));
+        MDG_CUDA(cudaMemcpyAsync(sys->hstat, sys->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+        MDG_CUDA(cudaStreamSynchronize(st));
+        long done = left - (long)rem;
+        uint32_t nreb = sys->hstat->pad[0];
+        sys->rebuilds += nreb;
+        ctx->launches += (uint64_t)done * g_step_kernels + (uint64_t)nreb * g_rebuild_kernels;
+        sys->force_prec = s->precision;
+        left = (long)rem;
+        if (sys->hstat->build_flags & FLAG_OVERFLOW) {
+            // the last step's rebuild outgrew a capacity: rebuild on the host
+            // path, which grows it, then resume
+            sys->rebuilds--;
+            int rc = nlist_build(sys, -1.0, sys->half);
+            if (rc && rc != MDG_ERR_RANGE) return rc;
+            rc = launch_trig(sys);
+            if (rc) return rc;
+        }
+    }
+    return left > 0 ? MDG_ERR_OVERFLOW : MDG_OK;
+}
+
+}  // namespace mdg
+
+extern "C" {
+
 int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
     PotSet ps;
     int rc = check_ready(s, sys, &ps);
     if (rc) return rc;
+    if (steps <= 0) return MDG_OK;
+    if (!sys->ctx->timing && sys->n > 0 && !sys->half) {
+        if (s->precision == MDG_PREC_MIXED) {
+            rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
+            if (rc) return rc;
+            int need = 0;
+            rc = mdg_nlist_decide(sys, &need);
+            if (rc) return rc;
+            if (need) {
+                rc = mdg_nlist_update(sys, -1.0, 0);
+                if (rc && rc != MDG_ERR_RANGE) return rc;
+            }
+            rc = launch_offsets(sys);
+            if (rc) return rc;
+        }
+        if (sys->force_prec != s->precision) {
+            rc = launch_force_copy(sys, s->precision == MDG_PREC_FP64);
+            if (rc) return rc;
+            sys->force_prec = s->precision;
+        }
+        return run_graph(s, sys, ps, dt, steps);
+    }
     cudaStream_t st = sys->ctx->stream;
     cudaEvent_t ev;
     MDG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));

@@ -137,6 +137,15 @@ struct mdg_system {
     int half = 0;
     int have_list = 0;
     uint64_t rebuilds = 0;
+    int cap_ready = 0;        // bin and list capacities sized
+    uint64_t cap_version = 0; // bumped when a capacity buffer is reallocated
+
+    // captured step loop (mdg_run): graph of the driver loop, rebuilt when
+    // capacities, the solver, dt or the precision change
+    cudaGraphExec_t run_exec = nullptr;
+    cudaGraph_t run_graph = nullptr;
+    uint64_t run_key[4] = {0, 0, 0, 0};
+    unsigned long long* dcounter = nullptr;  // steps left (device)
 
     // device status + grid
     mdg::DevStatus* dstat = nullptr;
@@ -162,6 +171,8 @@ namespace mdg {
 int system_alloc(mdg_system* sys);
 void system_free(mdg_system* sys);
 int nlist_build(mdg_system* sys, double kbuf, int half);
+int nlist_capacity(mdg_system* sys, int half);
+int nlist_enqueue(mdg_system* sys);
 int potset_build(mdg_solver* s, mdg_system* sys, PotSet* out);
 int pot_upload(mdg_potential* p, int device);
 int run_prepare(mdg_solver* s, mdg_system* sys, const PotSet& ps, int check_rcut);

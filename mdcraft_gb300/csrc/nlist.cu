@@ -69,7 +69,7 @@ __global__ void k_wrap_bounds(int n, double* __restrict__ rx, double* __restrict
 }
 
 __global__ void k_grid_finalize(const double* __restrict__ part, int nparts, DomainDev d,
-                                GridParams* __restrict__ out) {
+                                GridParams* __restrict__ out, long long bin_cap, DevStatus* st) {
     __shared__ double sh[7][kBlock];
     int t = threadIdx.x;
     double v[7] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308,
@@ -144,6 +144,13 @@ __global__ void k_grid_finalize(const double* __restrict__ part, int nparts, Dom
     if (nb > (1LL << 30)) g.empty = -2;
     g.ncells = (int)nc;
     g.nbins = (int)nb;
+    // the bin arrays were sized on the host; a grid that outgrew them
+    // invalidates this rebuild (every later kernel of it returns early)
+    if (g.empty == 0 && nb + 1 > bin_cap) {
+        g.empty = -3;
+        atomicOr(&st->flags, FLAG_OVERFLOW);
+        atomicOr(&st->build_flags, FLAG_OVERFLOW);
+    }
     *out = g;
 }
 
@@ -169,7 +176,7 @@ __global__ void k_bin_count(int n, const double* __restrict__ rx, const double* 
                             uint32_t* __restrict__ bin_count, DevStatus* st) {
     const GridParams g = *gp;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || g.empty) return;
     int c[3];
     bool cl;
     local_cell(g, rx[i], ry[i], rz[i], c, cl);
@@ -212,8 +219,13 @@ __device__ uint32_t block_excl_scan(uint32_t v, uint32_t* sh, uint32_t* total) {
     return base + x - v;
 }
 
-__global__ void k_scan_partial(const uint32_t* __restrict__ in, int nb, uint32_t* __restrict__ bsum) {
+// Number of bins of the current rebuild (0 when the grid is invalid).
+__device__ __forceinline__ int live_bins(const GridParams* gp) { return gp->empty ? 0 : gp->nbins; }
+
+__global__ void k_scan_partial(const uint32_t* __restrict__ in, const GridParams* __restrict__ gp,
+                               uint32_t* __restrict__ bsum) {
     __shared__ uint32_t sh[32];
+    const int nb = live_bins(gp);
     int base = blockIdx.x * kScanT * kScanItems + threadIdx.x * kScanItems;
     uint32_t s = 0;
     for (int k = 0; k < kScanItems; ++k) s += (base + k < nb) ? in[base + k] : 0u;
@@ -222,8 +234,11 @@ __global__ void k_scan_partial(const uint32_t* __restrict__ in, int nb, uint32_t
     if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
 }
 
-__global__ void k_scan_top(uint32_t* __restrict__ bsum, int nblk) {
+__global__ void k_scan_top(uint32_t* __restrict__ bsum, const GridParams* __restrict__ gp) {
     __shared__ uint32_t sh[32];
+    // block totals up to and including the block that holds index nb, whose
+    // exclusive prefix is the grand total written to start[nb]
+    const int nblk = live_bins(gp) / (kScanT * kScanItems) + 1;
     int base = threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
     uint32_t s = 0;
@@ -238,9 +253,13 @@ __global__ void k_scan_top(uint32_t* __restrict__ bsum, int nblk) {
     }
 }
 
-__global__ void k_scan_final(const uint32_t* __restrict__ in, int nb, const uint32_t* __restrict__ bsum,
-                             uint32_t* __restrict__ out) {
+__global__ void k_scan_final(const uint32_t* __restrict__ in, const GridParams* __restrict__ gp,
+                             const uint32_t* __restrict__ bsum, uint32_t* __restrict__ out) {
     __shared__ uint32_t sh[32];
+    const int nb = live_bins(gp);
+    // blocks beyond the live bins (the grid is sized for the capacity) idle
+    if (blockIdx.x * kScanT * kScanItems > nb) return;
+    const int last = nb / (kScanT * kScanItems);
     int base = blockIdx.x * kScanT * kScanItems + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
     uint32_t s = 0;
@@ -254,20 +273,21 @@ __global__ void k_scan_final(const uint32_t* __restrict__ in, int nb, const uint
         if (base + k < nb) out[base + k] = off;
         off += v[k];
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[nb] = off;
+    if ((int)blockIdx.x == last && threadIdx.x == blockDim.x - 1) out[nb] = off;
 }
 
 __global__ void k_scatter(int n, const uint32_t* __restrict__ key, const uint32_t* __restrict__ rank,
-                          const uint32_t* __restrict__ start, uint32_t* __restrict__ src) {
+                          const uint32_t* __restrict__ start, uint32_t* __restrict__ src,
+                          const GridParams* __restrict__ gp) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) src[start[key[i]] + rank[i]] = (uint32_t)i;
+    if (i < n && !gp->empty) src[start[key[i]] + rank[i]] = (uint32_t)i;
 }
 
 // Deterministic order inside a bin: ascending caller index.
-__global__ void k_bin_sort(int nb, const uint32_t* __restrict__ start, uint32_t* __restrict__ src,
-                           const uint32_t* __restrict__ orig) {
+__global__ void k_bin_sort(const GridParams* __restrict__ gp, const uint32_t* __restrict__ start,
+                           uint32_t* __restrict__ src, const uint32_t* __restrict__ orig) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nb) return;
+    if (b >= live_bins(gp)) return;
     uint32_t s = start[b], e = start[b + 1];
     for (uint32_t k = s + 1; k < e; ++k) {
         uint32_t v = src[k];
@@ -289,12 +309,23 @@ struct GatherSet {
 };
 
 template <int NF, typename T>
-__global__ void k_gather(int n, const uint32_t* __restrict__ src, GatherSet<NF, T> gs) {
+__global__ void k_gather(int n, const uint32_t* __restrict__ src, GatherSet<NF, T> gs,
+                         const GridParams* __restrict__ gp) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    if (k >= n || gp->empty) return;
     uint32_t s = src[k];
 #pragma unroll
     for (int f = 0; f < NF; ++f) gs.out[f][k] = gs.in[f][s];
+}
+
+// The permuted fields back into the live buffers (so device pointers stay
+// fixed across rebuilds, as a captured graph needs).
+template <int NF, typename T>
+__global__ void k_copy(int n, GatherSet<NF, T> gs, const GridParams* __restrict__ gp) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || gp->empty) return;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) gs.out[f][k] = gs.in[f][k];
 }
 
 // Cell centre, cell-relative FP32 offsets and packed cell of every atom.
@@ -305,7 +336,7 @@ __global__ void k_cells(int n, const double* __restrict__ rx, const double* __re
                         const uint32_t* __restrict__ orig, uint32_t* __restrict__ slot_of) {
     const GridParams g = *gp;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || g.empty) return;
     double r[3] = {rx[i], ry[i], rz[i]};
     int c[3];
     bool cl;
@@ -333,8 +364,7 @@ __global__ void k_cells(int n, const double* __restrict__ rx, const double* __re
 // Verlet list: one warp per cell, lanes over the cell's atoms
 // ---------------------------------------------------------------------------
 struct NbArgs {
-    int n, np, K, half, uniform_rns;
-    float lo2, hi2;  // rns^2 (1 -/+ 1e-5) when uniform
+    int n, np, K, half;
     const double *rx, *ry, *rz, *rns, *rcut;
     const uint32_t *orig, *uid, *cellp, *bin_start;
     const float4* o0;
@@ -367,7 +397,11 @@ __global__ void __launch_bounds__(kBlock) k_nbuild(NbArgs A, const GridParams* _
     __syncthreads();
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
-    if (warp >= g.nbins) return;
+    if (g.empty || warp >= g.nbins) return;
+    // prefilter band: rns^2 (1 -/+ 1e-5), valid when every atom has the same rns
+    const float lo2 = (float)(g.max_rns * g.max_rns * (1.0 - 1e-5));
+    const float hi2 = (float)(g.max_rns * g.max_rns * (1.0 + 1e-5));
+    const bool uniform_rns = A.st->nonuniform == 0;
     uint32_t s0 = A.bin_start[warp], s1 = A.bin_start[warp + 1];
     if (s0 == s1) return;
     int cx, cy, cz;
@@ -377,7 +411,7 @@ __global__ void __launch_bounds__(kBlock) k_nbuild(NbArgs A, const GridParams* _
     if (g.dim < 2) gc[1] = 0;
     bool edge[3] = {false, false, false};
     for (int a = 0; a < g.dim; ++a) edge[a] = gc[a] == 0 || gc[a] == g.num[a] - 1;
-    const bool prefilter = A.uniform_rns && !g.small_box;
+    const bool prefilter = uniform_rns && !g.small_box;
 
     for (uint32_t base = s0; base < s1; base += 32) {
         uint32_t i = base + lane;
@@ -427,9 +461,9 @@ __global__ void __launch_bounds__(kBlock) k_nbuild(NbArgs A, const GridParams* _
                         float dz = oi.z - oj.z - sh[2];
                         float d2 = dx * dx + dy * dy + dz * dz;
                         bool acc;
-                        if (prefilter && oi.w == 0.0f && oj.w == 0.0f && d2 < A.lo2) {
+                        if (prefilter && oi.w == 0.0f && oj.w == 0.0f && d2 < lo2) {
                             acc = true;
-                        } else if (prefilter && oi.w == 0.0f && oj.w == 0.0f && d2 > A.hi2) {
+                        } else if (prefilter && oi.w == 0.0f && oj.w == 0.0f && d2 > hi2) {
                             acc = false;
                         } else {
                             acc = are_neibs_exact(g, xi, yi, zi, rni, A.rx[j], A.ry[j], A.rz[j],
@@ -466,7 +500,10 @@ __global__ void __launch_bounds__(kBlock) k_nbuild(NbArgs A, const GridParams* _
             int padded = (cnt + 3) & ~3;
             for (int k = cnt; k < padded && k < A.K; ++k) A.nbr[nidx(k, i, A.np)] = i | kSelfCode;
             A.ncnt[i] = padded < A.K ? padded : A.K;
-            if (cnt > A.K) atomicOr(&A.st->flags, FLAG_OVERFLOW);
+            if (cnt > A.K) {
+                atomicOr(&A.st->flags, FLAG_OVERFLOW);
+                atomicOr(&A.st->build_flags, FLAG_OVERFLOW);
+            }
             atomicMax(&A.st->max_count, (uint32_t)cnt);
             A.r0x[i] = xi;
             A.r0y[i] = yi;
@@ -500,9 +537,9 @@ __global__ void k_optimize_rns(int n, int np, double kbuf, int have_list, const 
     rns[i] = kbuf * hmax;
 }
 
-__global__ void k_check_rns(int n, const double* __restrict__ rns, double r0, DevStatus* st) {
+__global__ void k_check_rns(int n, const double* __restrict__ rns, DevStatus* st) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && rns[i] != r0) atomicOr(&st->nonuniform, 1u);
+    if (i < n && rns[i] != rns[0]) atomicOr(&st->nonuniform, 1u);
 }
 
 // ---------------------------------------------------------------------------
@@ -510,10 +547,10 @@ __global__ void k_check_rns(int n, const double* __restrict__ rns, double r0, De
 // ---------------------------------------------------------------------------
 static inline int nblk(size_t n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
-static int ensure_bins(mdg_system* sys, int nbins) {
+static int ensure_bins(mdg_system* sys, long long nbins) {
     if ((size_t)nbins + 1 <= sys->bin_cap) return MDG_OK;
     size_t cap = (size_t)nbins + 1;
-    cap = cap + cap / 4 + 1024;
+    cap = cap + cap / 8 + 4096;
     cudaFree(sys->bin_count);
     cudaFree(sys->bin_start);
     cudaFree(sys->scan_tmp);
@@ -522,34 +559,234 @@ static int ensure_bins(mdg_system* sys, int nbins) {
     MDG_CUDA(cudaMalloc(&sys->bin_start, cap * sizeof(uint32_t)));
     MDG_CUDA(cudaMalloc(&sys->scan_tmp, (cap / (kScanT * kScanItems) + 2) * sizeof(uint32_t)));
     sys->bin_cap = cap;
+    sys->cap_version++;
     return MDG_OK;
 }
 
 static int ensure_list(mdg_system* sys, int K) {
+    K = (K + 3) & ~3;
     if (K <= sys->K && sys->nbr) return MDG_OK;
     cudaFree(sys->nbr);
     sys->nbr = nullptr;
     MDG_CUDA(cudaMalloc(&sys->nbr, (size_t)K * sys->np * sizeof(uint32_t)));
     sys->K = K;
+    sys->cap_version++;
     return MDG_OK;
 }
 
-static int launch_scan(mdg_system* sys, int nb) {
-    cudaStream_t st = sys->ctx->stream;
-    int nblk_scan = (nb + kScanT * kScanItems - 1) / (kScanT * kScanItems);
-    if (nblk_scan > kScanT * kScanItems) {
+static DomainDev domain_dev(const mdg_system* sys) {
+    DomainDev d;
+    for (int a = 0; a < 3; ++a) {
+        d.bmin[a] = sys->dom.bmin[a];
+        d.bmax[a] = sys->dom.bmax[a];
+        d.size[a] = sys->dom.bmax[a] - sys->dom.bmin[a];
+        d.periodic[a] = sys->dom.periodic[a] ? 1 : 0;
+    }
+    d.dim = sys->dim;
+    return d;
+}
+
+static int nparts_of(const mdg_system* sys) {
+    return std::min(nblk(sys->n), 8 * std::max(sys->ctx->num_sms, 1));
+}
+
+static int ensure_parts(mdg_system* sys) {
+    int nparts = nparts_of(sys);
+    if ((size_t)nparts > sys->part_cap) {
+        cudaFree(sys->part);
+        sys->part = nullptr;
+        MDG_CUDA(cudaMalloc(&sys->part, (size_t)nparts * 8 * sizeof(double)));
+        sys->part_cap = nparts;
+    }
+    return MDG_OK;
+}
+
+// Sizes the bin arrays and the list capacity from one synchronous bounds
+// pass (positions are wrapped by it exactly as by a rebuild).
+int nlist_capacity(mdg_system* sys, int half) {
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    const int n = (int)sys->n;
+    int rc = ensure_parts(sys);
+    if (rc) return rc;
+    int nparts = nparts_of(sys);
+    DomainDev d = domain_dev(sys);
+    int c = sys->cur;
+    k_wrap_bounds<<<nparts, kBlock, 0, st>>>(n, sys->f64[RX][c], sys->f64[RY][c], sys->f64[RZ][c],
+                                             sys->f64[RNS][c], d, sys->part);
+    MDG_LAUNCHED(ctx);
+    k_grid_finalize<<<1, kBlock, 0, st>>>(sys->part, nparts, d, sys->dgrid, 1LL << 40, sys->dstat);
+    MDG_LAUNCHED(ctx);
+    MDG_CUDA(cudaMemcpyAsync(sys->hgrid, sys->dgrid, sizeof(GridParams), cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    GridParams g = *sys->hgrid;
+    if (g.empty == -1) {
+        set_error("neighbour search radius rns must be positive");
+        return MDG_ERR_INVALID;
+    }
+    if (g.empty == -2) {
+        set_error("cell grid too large (more than 1023 cells on an axis)");
+        return MDG_ERR_INVALID;
+    }
+    // periodic axes keep their grid; open axes get room to grow
+    long long want = g.nbins;
+    bool open = false;
+    for (int a = 0; a < sys->dim; ++a) open = open || !sys->dom.periodic[a];
+    if (open) want = want * 2;
+    rc = ensure_bins(sys, want);
+    if (rc) return rc;
+    if (sys->K == 0 || sys->half != half) {
+        double vol = 1.0;
+        for (int a = 0; a < sys->dim; ++a) vol *= g.cs[a] * g.num[a];
+        double dens = (double)n / std::max(vol, 1e-300);
+        double rn = g.max_rns;
+        // neighbours within rns at the mean density of the local grid (an open
+        // system's grid also holds empty space: the retry grows K if needed)
+        double est = sys->dim == 3 ? 4.18879020478639 * rn * rn * rn * dens
+                   : sys->dim == 2 ? 3.14159265358979 * rn * rn * dens : 2.0 * rn * dens;
+        if (open) est *= 2.0;
+        if (half) est *= 0.5;
+        int K = (int)(est * 1.35) + 16;
+        K = std::min(std::max(K, 16), n + 4);
+        rc = ensure_list(sys, K);
+        if (rc) return rc;
+    }
+    sys->half = half;
+    sys->cap_ready = 1;
+    return MDG_OK;
+}
+
+// Enqueues a whole rebuild on the context stream with no host
+// synchronisation: every size comes from the device grid parameters, and a
+// grid or list that outgrows the capacities raises FLAG_OVERFLOW in
+// build_flags (the kernels of an invalid grid return early).
+int nlist_enqueue(mdg_system* sys) {
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    const int n = (int)sys->n;
+    if (n == 0) return MDG_OK;
+    int nparts = nparts_of(sys);
+    DomainDev d = domain_dev(sys);
+    const int c = sys->cur, alt = c ^ 1;
+    MDG_CUDA(cudaMemsetAsync(&sys->dstat->max_count, 0, 3 * sizeof(uint32_t), st));  // max_count, nonuniform, build_flags
+    k_wrap_bounds<<<nparts, kBlock, 0, st>>>(n, sys->f64[RX][c], sys->f64[RY][c], sys->f64[RZ][c],
+                                             sys->f64[RNS][c], d, sys->part);
+    MDG_LAUNCHED(ctx);
+    k_grid_finalize<<<1, kBlock, 0, st>>>(sys->part, nparts, d, sys->dgrid, (long long)sys->bin_cap, sys->dstat);
+    MDG_LAUNCHED(ctx);
+    k_check_rns<<<nblk(n), kBlock, 0, st>>>(n, sys->f64[RNS][c], sys->dstat);
+    MDG_LAUNCHED(ctx);
+    MDG_CUDA(cudaMemsetAsync(sys->bin_count, 0, sys->bin_cap * sizeof(uint32_t), st));
+    k_bin_count<<<nblk(n), kBlock, 0, st>>>(n, sys->f64[RX][c], sys->f64[RY][c], sys->f64[RZ][c], sys->dgrid,
+                                            sys->key, sys->rank, sys->bin_count, sys->dstat);
+    MDG_LAUNCHED(ctx);
+    int nscan = (int)((sys->bin_cap + kScanT * kScanItems - 1) / (kScanT * kScanItems));
+    if (nscan > kScanT * kScanItems) {
         set_error("too many cell bins for the scan");
         return MDG_ERR_INVALID;
     }
-    k_scan_partial<<<nblk_scan, kScanT, 0, st>>>(sys->bin_count, nb, sys->scan_tmp);
-    MDG_LAUNCHED(sys->ctx);
-    k_scan_top<<<1, kScanT, 0, st>>>(sys->scan_tmp, nblk_scan);
-    MDG_LAUNCHED(sys->ctx);
-    k_scan_final<<<nblk_scan, kScanT, 0, st>>>(sys->bin_count, nb, sys->scan_tmp, sys->bin_start);
-    MDG_LAUNCHED(sys->ctx);
+    k_scan_partial<<<nscan, kScanT, 0, st>>>(sys->bin_count, sys->dgrid, sys->scan_tmp);
+    MDG_LAUNCHED(ctx);
+    k_scan_top<<<1, kScanT, 0, st>>>(sys->scan_tmp, sys->dgrid);
+    MDG_LAUNCHED(ctx);
+    k_scan_final<<<nscan, kScanT, 0, st>>>(sys->bin_count, sys->dgrid, sys->scan_tmp, sys->bin_start);
+    MDG_LAUNCHED(ctx);
+    k_scatter<<<nblk(n), kBlock, 0, st>>>(n, sys->key, sys->rank, sys->bin_start, sys->src, sys->dgrid);
+    MDG_LAUNCHED(ctx);
+    k_bin_sort<<<nblk(sys->bin_cap), kBlock, 0, st>>>(sys->dgrid, sys->bin_start, sys->src, sys->u32[ORIG][c]);
+    MDG_LAUNCHED(ctx);
+    // permute every per-atom field into the spare buffers, then copy back
+    {
+        GatherSet<12, double> a, b, a2, b2;
+        for (int f = 0; f < 12; ++f) {
+            a.in[f] = sys->f64[f][c];
+            a.out[f] = sys->f64[f][alt];
+            b.in[f] = sys->f64[12 + f][c];
+            b.out[f] = sys->f64[12 + f][alt];
+            a2.in[f] = a.out[f];
+            a2.out[f] = sys->f64[f][c];
+            b2.in[f] = b.out[f];
+            b2.out[f] = sys->f64[12 + f][c];
+        }
+        GatherSet<3, float> fc, fc2;
+        for (int f = 0; f < 3; ++f) {
+            fc.in[f] = sys->f32[f][c];
+            fc.out[f] = sys->f32[f][alt];
+            fc2.in[f] = fc.out[f];
+            fc2.out[f] = sys->f32[f][c];
+        }
+        GatherSet<2, uint32_t> u, u2;
+        GatherSet<2, uint16_t> h, h2;
+        for (int f = 0; f < 2; ++f) {
+            u.in[f] = sys->u32[f][c];
+            u.out[f] = sys->u32[f][alt];
+            u2.in[f] = u.out[f];
+            u2.out[f] = sys->u32[f][c];
+            h.in[f] = sys->u16[f][c];
+            h.out[f] = sys->u16[f][alt];
+            h2.in[f] = h.out[f];
+            h2.out[f] = sys->u16[f][c];
+        }
+        k_gather<12, double><<<nblk(n), kBlock, 0, st>>>(n, sys->src, a, sys->dgrid);
+        MDG_LAUNCHED(ctx);
+        k_gather<12, double><<<nblk(n), kBlock, 0, st>>>(n, sys->src, b, sys->dgrid);
+        MDG_LAUNCHED(ctx);
+        k_gather<3, float><<<nblk(n), kBlock, 0, st>>>(n, sys->src, fc, sys->dgrid);
+        MDG_LAUNCHED(ctx);
+        k_gather<2, uint32_t><<<nblk(n), kBlock, 0, st>>>(n, sys->src, u, sys->dgrid);
+        MDG_LAUNCHED(ctx);
+        k_gather<2, uint16_t><<<nblk(n), kBlock, 0, st>>>(n, sys->src, h, sys->dgrid);
+        MDG_LAUNCHED(ctx);
+        k_copy<12, double><<<nblk(n), kBlock, 0, st>>>(n, a2, sys->dgrid);
+        MDG_LAUNCHED(ctx);
+        k_copy<12, double><<<nblk(n), kBlock, 0, st>>>(n, b2, sys->dgrid);
+        MDG_LAUNCHED(ctx);
+        k_copy<3, float><<<nblk(n), kBlock, 0, st>>>(n, fc2, sys->dgrid);
+        MDG_LAUNCHED(ctx);
+        k_copy<2, uint32_t><<<nblk(n), kBlock, 0, st>>>(n, u2, sys->dgrid);
+        MDG_LAUNCHED(ctx);
+        k_copy<2, uint16_t><<<nblk(n), kBlock, 0, st>>>(n, h2, sys->dgrid);
+        MDG_LAUNCHED(ctx);
+    }
+    k_cells<<<nblk(n), kBlock, 0, st>>>(n, sys->f64[RX][c], sys->f64[RY][c], sys->f64[RZ][c], sys->dgrid,
+                                        sys->cellp, sys->Rc[0], sys->Rc[1], sys->Rc[2], sys->pos32, sys->o0,
+                                        sys->u32[ORIG][c], sys->slot_of);
+    MDG_LAUNCHED(ctx);
+    NbArgs A;
+    A.n = n;
+    A.np = (int)sys->np;
+    A.K = sys->K;
+    A.half = sys->half;
+    A.rx = sys->f64[RX][c];
+    A.ry = sys->f64[RY][c];
+    A.rz = sys->f64[RZ][c];
+    A.rns = sys->f64[RNS][c];
+    A.rcut = sys->f64[RCUT][c];
+    A.orig = sys->u32[ORIG][c];
+    A.uid = sys->u32[UID][c];
+    A.cellp = sys->cellp;
+    A.bin_start = sys->bin_start;
+    A.o0 = sys->o0;
+    A.nbr = sys->nbr;
+    A.ncnt = sys->ncnt;
+    A.r0x = sys->r0[0];
+    A.r0y = sys->r0[1];
+    A.r0z = sys->r0[2];
+    A.saved_rcut = sys->saved_rcut;
+    A.saved_rns = sys->saved_rns;
+    A.saved_uid = sys->saved_uid;
+    A.st = sys->dstat;
+    size_t warps = sys->bin_cap;  // one warp per bin; the live bins come from the device grid
+    k_nbuild<<<nblk(warps * 32), kBlock, 0, st>>>(A, sys->dgrid);
+    MDG_LAUNCHED(ctx);
     return MDG_OK;
 }
 
+int launch_trig(mdg_system* sys);
+
+// VerletList::update (verlet-list.cxx:41-55) for the API: enqueue, wait,
+// and rebuild again with larger capacities when the grid or a list outgrew
+// them.
 int nlist_build(mdg_system* sys, double kbuf, int half) {
     mdg_ctx* ctx = sys->ctx;
     cudaStream_t st = ctx->stream;
@@ -560,172 +797,47 @@ int nlist_build(mdg_system* sys, double kbuf, int half) {
         sys->dirty = 0;
         return MDG_OK;
     }
-    int cur = sys->cur;
+    int c = sys->cur;
     if (kbuf > 0.0) {
-        k_optimize_rns<<<nblk(n), kBlock, 0, st>>>(n, (int)sys->np, kbuf, sys->have_list, sys->nbr,
-                                                   sys->ncnt, sys->f64[RCUT][cur], sys->f64[RNS][cur]);
+        k_optimize_rns<<<nblk(n), kBlock, 0, st>>>(n, (int)sys->np, kbuf, sys->have_list, sys->nbr, sys->ncnt,
+                                                   sys->f64[RCUT][c], sys->f64[RNS][c]);
         MDG_LAUNCHED(ctx);
+        sys->cap_ready = 0;  // rns changed: re-size the grid
     }
-    DomainDev d;
-    for (int a = 0; a < 3; ++a) {
-        d.bmin[a] = sys->dom.bmin[a];
-        d.bmax[a] = sys->dom.bmax[a];
-        d.size[a] = sys->dom.bmax[a] - sys->dom.bmin[a];
-        d.periodic[a] = sys->dom.periodic[a] ? 1 : 0;
-    }
-    d.dim = sys->dim;
-    int nparts = std::min(nblk(n), 8 * std::max(ctx->num_sms, 1));
-    if ((size_t)nparts > sys->part_cap) {
-        cudaFree(sys->part);
-        sys->part = nullptr;
-        MDG_CUDA(cudaMalloc(&sys->part, (size_t)nparts * 8 * sizeof(double)));
-        sys->part_cap = nparts;
-    }
-    k_wrap_bounds<<<nparts, kBlock, 0, st>>>(n, sys->f64[RX][cur], sys->f64[RY][cur], sys->f64[RZ][cur],
-                                             sys->f64[RNS][cur], d, sys->part);
-    MDG_LAUNCHED(ctx);
-    k_grid_finalize<<<1, kBlock, 0, st>>>(sys->part, nparts, d, sys->dgrid);
-    MDG_LAUNCHED(ctx);
-    // uniform rns check against atom 0; per-build flags cleared
-    MDG_CUDA(cudaMemsetAsync(&sys->dstat->nonuniform, 0, 2 * sizeof(uint32_t), st));
-    double rns0 = 0.0;
-    MDG_CUDA(cudaMemcpyAsync(&rns0, sys->f64[RNS][cur], sizeof(double), cudaMemcpyDeviceToHost, st));
-    MDG_CUDA(cudaStreamSynchronize(st));
-    k_check_rns<<<nblk(n), kBlock, 0, st>>>(n, sys->f64[RNS][cur], rns0, sys->dstat);
-    MDG_LAUNCHED(ctx);
-    MDG_CUDA(cudaMemcpyAsync(sys->hgrid, sys->dgrid, sizeof(GridParams), cudaMemcpyDeviceToHost, st));
-    MDG_CUDA(cudaMemcpyAsync(sys->hstat, sys->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
-    MDG_CUDA(cudaStreamSynchronize(st));
-    GridParams g = *sys->hgrid;
-    int uniform = sys->hstat->nonuniform == 0;
-    if (g.empty == -1) {
-        set_error("neighbour search radius rns must be positive");
-        return MDG_ERR_INVALID;
-    }
-    if (g.empty == -2) {
-        set_error("cell grid too large (more than 1023 cells on an axis)");
-        return MDG_ERR_INVALID;
-    }
-    sys->grid = g;
-    int rc = ensure_bins(sys, g.nbins);
-    if (rc) return rc;
-
-    // bin count, scan, scatter, in-bin sort
-    MDG_CUDA(cudaMemsetAsync(sys->bin_count, 0, (size_t)g.nbins * sizeof(uint32_t), st));
-    k_bin_count<<<nblk(n), kBlock, 0, st>>>(n, sys->f64[RX][cur], sys->f64[RY][cur], sys->f64[RZ][cur],
-                                            sys->dgrid, sys->key, sys->rank, sys->bin_count, sys->dstat);
-    MDG_LAUNCHED(ctx);
-    rc = launch_scan(sys, g.nbins);
-    if (rc) return rc;
-    k_scatter<<<nblk(n), kBlock, 0, st>>>(n, sys->key, sys->rank, sys->bin_start, sys->src);
-    MDG_LAUNCHED(ctx);
-    k_bin_sort<<<nblk(g.nbins), kBlock, 0, st>>>(g.nbins, sys->bin_start, sys->src, sys->u32[ORIG][cur]);
-    MDG_LAUNCHED(ctx);
-
-    // permute every per-atom field into the new slot order
-    int nxt = cur ^ 1;
-    {
-        GatherSet<12, double> a, b;
-        for (int f = 0; f < 12; ++f) {
-            a.in[f] = sys->f64[f][cur];
-            a.out[f] = sys->f64[f][nxt];
-        }
-        for (int f = 0; f < 12; ++f) {
-            b.in[f] = sys->f64[12 + f][cur];
-            b.out[f] = sys->f64[12 + f][nxt];
-        }
-        k_gather<12, double><<<nblk(n), kBlock, 0, st>>>(n, sys->src, a);
-        MDG_LAUNCHED(ctx);
-        k_gather<12, double><<<nblk(n), kBlock, 0, st>>>(n, sys->src, b);
-        MDG_LAUNCHED(ctx);
-        GatherSet<3, float> c;
-        for (int f = 0; f < 3; ++f) {
-            c.in[f] = sys->f32[f][cur];
-            c.out[f] = sys->f32[f][nxt];
-        }
-        k_gather<3, float><<<nblk(n), kBlock, 0, st>>>(n, sys->src, c);
-        MDG_LAUNCHED(ctx);
-        GatherSet<2, uint32_t> u;
-        for (int f = 0; f < 2; ++f) {
-            u.in[f] = sys->u32[f][cur];
-            u.out[f] = sys->u32[f][nxt];
-        }
-        k_gather<2, uint32_t><<<nblk(n), kBlock, 0, st>>>(n, sys->src, u);
-        MDG_LAUNCHED(ctx);
-        GatherSet<2, uint16_t> h;
-        for (int f = 0; f < 2; ++f) {
-            h.in[f] = sys->u16[f][cur];
-            h.out[f] = sys->u16[f][nxt];
-        }
-        k_gather<2, uint16_t><<<nblk(n), kBlock, 0, st>>>(n, sys->src, h);
-        MDG_LAUNCHED(ctx);
-    }
-    sys->cur = cur = nxt;
-    k_cells<<<nblk(n), kBlock, 0, st>>>(n, sys->f64[RX][cur], sys->f64[RY][cur], sys->f64[RZ][cur], sys->dgrid,
-                                        sys->cellp, sys->Rc[0], sys->Rc[1], sys->Rc[2], sys->pos32, sys->o0,
-                                        sys->u32[ORIG][cur], sys->slot_of);
-    MDG_LAUNCHED(ctx);
-
-    // list capacity: estimate from the density, then grow on overflow
-    if (sys->K == 0 || sys->half != half) {
-        double vol = 1.0;
-        for (int a = 0; a < sys->dim; ++a) vol *= g.cs[a] * g.num[a];
-        double dens = (double)n / std::max(vol, 1e-300);
-        double est = 4.18879020478639 * g.max_rns * g.max_rns * g.max_rns * dens;
-        if (half) est *= 0.5;
-        int K = (int)(est * 1.35) + 16;
-        K = std::min(std::max(K, 16), n + 1);
-        K = (K + 3) & ~3;
-        rc = ensure_list(sys, K);
+    int rc;
+    if (!sys->cap_ready || sys->half != half) {
+        rc = nlist_capacity(sys, half);
         if (rc) return rc;
     }
-    double rn = g.max_rns;
-    NbArgs A;
-    A.n = n;
-    A.np = (int)sys->np;
-    A.half = half;
-    A.uniform_rns = uniform;
-    A.lo2 = (float)(rn * rn * (1.0 - 1e-5));
-    A.hi2 = (float)(rn * rn * (1.0 + 1e-5));
-    A.rx = sys->f64[RX][cur];
-    A.ry = sys->f64[RY][cur];
-    A.rz = sys->f64[RZ][cur];
-    A.rns = sys->f64[RNS][cur];
-    A.rcut = sys->f64[RCUT][cur];
-    A.orig = sys->u32[ORIG][cur];
-    A.uid = sys->u32[UID][cur];
-    A.cellp = sys->cellp;
-    A.bin_start = sys->bin_start;
-    A.o0 = sys->o0;
-    A.ncnt = sys->ncnt;
-    A.r0x = sys->r0[0];
-    A.r0y = sys->r0[1];
-    A.r0z = sys->r0[2];
-    A.saved_rcut = sys->saved_rcut;
-    A.saved_rns = sys->saved_rns;
-    A.saved_uid = sys->saved_uid;
-    A.st = sys->dstat;
-    for (int attempt = 0; attempt < 3; ++attempt) {
-        A.K = sys->K;
-        A.nbr = sys->nbr;
-        MDG_CUDA(cudaMemsetAsync(&sys->dstat->max_count, 0, sizeof(uint32_t), st));
-        int warps = g.nbins;
-        k_nbuild<<<nblk((size_t)warps * 32), kBlock, 0, st>>>(A, sys->dgrid);
-        MDG_LAUNCHED(ctx);
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        rc = nlist_enqueue(sys);
+        if (rc) return rc;
+        rc = launch_trig(sys);
+        if (rc) return rc;
         MDG_CUDA(cudaMemcpyAsync(sys->hstat, sys->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+        MDG_CUDA(cudaMemcpyAsync(sys->hgrid, sys->dgrid, sizeof(GridParams), cudaMemcpyDeviceToHost, st));
         MDG_CUDA(cudaStreamSynchronize(st));
-        uint32_t mc = sys->hstat->max_count;
-        if ((int)mc <= sys->K) break;
-        int K = (int)(mc * 1.2) + 8;
-        K = (K + 3) & ~3;
-        rc = ensure_list(sys, K);
-        if (rc) return rc;
-        // overflow of this attempt is resolved by the retry
+        if (!(sys->hstat->build_flags & FLAG_OVERFLOW)) break;
+        // grow what overflowed and rebuild (the positions are already wrapped
+        // and sorted, so a repeated rebuild gives the same order)
+        GridParams g = *sys->hgrid;
+        if (g.empty == -3) {
+            rc = nlist_capacity(sys, half);
+            if (rc) return rc;
+        }
+        if ((int)sys->hstat->max_count > sys->K) {
+            rc = ensure_list(sys, (int)(sys->hstat->max_count * 1.2) + 8);
+            if (rc) return rc;
+        }
         uint32_t clear = sys->hstat->flags & ~FLAG_OVERFLOW;
         MDG_CUDA(cudaMemcpyAsync(&sys->dstat->flags, &clear, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        if (attempt == 3) {
+            set_error("neighbour list capacity could not be sized");
+            return MDG_ERR_OVERFLOW;
+        }
     }
+    sys->grid = *sys->hgrid;
     sys->have_list = 1;
-    sys->half = half;
     sys->dirty = 0;
     sys->rebuilds++;
     if (sys->hstat->build_flags & FLAG_RANGE) {
