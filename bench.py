@@ -27,6 +27,9 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# the serving loop runs one stream per slot: give each its own hardware
+# queue (read when the CUDA context is created)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 WORKLOAD = ("EAM Cu fcc 63^3 = 1,000,188 atoms, periodic cube 22.77 nm, Finnis-Sinclair-type analytic tables "
             "(5000-point splines), rc 5.0 A, skin 0.5 A, 1% jitter, 300 K, dt 1 fs")
@@ -44,6 +47,11 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=4096)
+    ap.add_argument("--serve-slots", type=int, default=32)
+    ap.add_argument("--serve-steps", type=int, default=1000)
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-only", action="store_true", help="only the serving stream (prints its summary)")
     return ap.parse_args()
 
 
@@ -191,6 +199,46 @@ def peaks():
         return {}
 
 
+SERVE_WORKLOAD = ("serving stream: Poisson arrivals at 2000/s, 60% LJ argon (rc 2.5 sigma, skin 0.3 A, dt 2 fs) / "
+                  "40% EAM Cu (rc 5 A, skin 0.5 A, dt 1 fs), fcc boxes of 256-32768 atoms (log-uniform), "
+                  "1% jitter, 300 K, mixed precision, periodic")
+
+
+def run_serving(args, device):
+    """The serving stream through mdg_server: latency from arrival to the
+    result on the host, and aggregate atom-steps/s over the whole stream."""
+    import mdcraft_gb300 as mdg
+    from mdcraft_gb300 import serving as SV
+    from mdcraft_gb300 import workloads as W
+    specs = W.serving_stream(count=args.serve_requests, steps=args.serve_steps)
+    solv = SV.solvers("mixed")
+    reqs = SV.prepare(specs)
+    srv = mdg.Server(device=device, slots=args.serve_slots, max_atoms=32768)
+    # warm-up: one request of each kind (pool pages, potential tables)
+    for kind in ("lj", "eam"):
+        s = next(x for x in specs if x["kind"] == kind)
+        atoms, box = W.serving_atoms(s)
+        rid = srv.submit(solv[kind], SV.periodic_domain(box), atoms, s["dt"], 10)
+        srv.wait(rid, 120.0)
+        srv.result(rid, atoms=False)
+    l0 = srv.stats()["launches"]
+    clocks = Clocks(device)
+    clocks.start()
+    summary, _ = SV.replay(srv, reqs, solv, release_inputs=True)
+    ck = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    summary.update({"workload": SERVE_WORKLOAD, "slots": args.serve_slots, "steps_per_request": args.serve_steps,
+                    "arrival_rate_per_s": 2000.0, "budget_bytes": st["budget"], "peak_bytes": st["peak"],
+                    "gpu_launches": st["launches"] - l0, "clocks": ck,
+                    "host_s": {"admit": st["host_admit_s"], "graph": st["host_graph_s"],
+                               "retire": st["host_retire_s"],
+                               "retire_detail": dict(zip(("bookkeeping", "gather", "graph_release", "memory_release"),
+                                                         st["host_detail_s"]))},
+                    "latency": "arrival to result atoms on the host"})
+    return summary
+
+
 def run_mdg(args, rank, world, local):
     import torch
 
@@ -199,6 +247,11 @@ def run_mdg(args, rank, world, local):
 
     B.build()
     dist = Dist(world, local)
+    if args.serve_only:
+        if rank == 0:
+            print(json.dumps({"serving": run_serving(args, local)}), flush=True)
+        dist.close()
+        return
     atoms, box, _, p = make_workload(args.ncell)
     t = p["tables"]
     n = len(atoms)
@@ -306,6 +359,10 @@ def run_mdg(args, rank, world, local):
             "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
             "bytes_per_atom": bytes_atom, "launch_ms": force_launch_ms}
 
+    serving = None
+    if not args.no_serve:
+        serving = run_serving(args, local)
+
     if rank == 0:
         cb = None
         if not args.no_cpu and world == 1:
@@ -330,6 +387,7 @@ def run_mdg(args, rank, world, local):
             "roofline": roof,
             "cpu_baseline": cb,
             "clocks": ck,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     dist.close()

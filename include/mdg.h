@@ -228,6 +228,79 @@ int mdg_measure_static(const double* d_m, const double* d_v, const double* d_Ep,
  * bit 3 non-finite force); clears them. */
 int mdg_system_flags(mdg_system* sys, uint32_t* flags);
 
+/* ---- serving: continuous batching of independent systems ------------------------
+ * No counterpart in the reference, whose drivers run one system per process
+ * (test/python/solver/test-EAM.py:101-200). A server keeps up to `slots`
+ * systems resident on one GPU, each on its own stream running its whole
+ * driver loop (mdg_run) as one graph launch, so the work of different
+ * requests overlaps on the device. A request (atoms, domain, solver, dt,
+ * steps) waits in a FIFO until a slot is free and its device footprint fits
+ * in the budget left by the running ones; when it finishes its slot and
+ * memory go to the next. System memory comes stream-ordered from a pool
+ * owned by the server, so admitting and retiring a request never waits for
+ * the whole device. Results do not depend on what else runs: every kernel
+ * reads only its own system, in a fixed order. A server is used by one host
+ * thread at a time; the solvers it is given must outlive their requests. */
+typedef struct mdg_server mdg_server;
+
+typedef struct mdg_server_config {
+    int slots;          /* systems on the GPU at once (>= 1) */
+    size_t hbm_budget;  /* device bytes the live systems may hold; 0 = half the free memory */
+    size_t max_atoms;   /* largest request accepted (sizes the pinned staging) */
+} mdg_server_config;
+
+typedef struct mdg_request_info {
+    int status;         /* MDG_OK or the error that ended the request */
+    int done;           /* 1 once the result is available */
+    double t_submit;    /* server clock (s): submitted, admitted to a slot, finished */
+    double t_admit;
+    double t_done;
+    uint64_t rebuilds;  /* list rebuilds during the run */
+    size_t footprint;   /* device bytes the request held */
+} mdg_request_info;
+
+typedef struct mdg_server_stats {
+    size_t budget, used, peak; /* device bytes: budget, held now, most held at once */
+    size_t queued, running, finished;
+    uint64_t admitted;
+    uint64_t launches;  /* kernels launched for all requests so far */
+    double host_admit_s;  /* host seconds spent admitting (set-up, first list, graph) */
+    double host_graph_s;  /* of which capturing and instantiating step-loop graphs */
+    double host_retire_s; /* host seconds spent retiring (result copy, release) */
+    uint64_t rechecked;   /* requests repeated on the checked path (first list outgrew its sizing) */
+    double host_detail_s[4]; /* of retiring: run bookkeeping, result gather, graph release, memory release */
+} mdg_server_stats;
+
+int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out);
+/* Waits for running requests, then frees everything. */
+int mdg_server_destroy(mdg_server* srv);
+/* Queues a request; copies the atoms (caller order, 208 B records). The
+ * solver's precision at submission is used. Fails with MDG_ERR_NOMEM when
+ * the request alone would exceed the budget and MDG_ERR_INVALID when n >
+ * max_atoms. Does not wait for the device. */
+int mdg_server_submit(mdg_server* srv, mdg_solver* solver, const mdg_domain* domain, const mdg_atom* atoms,
+                      size_t n, double dt, long steps, uint64_t* id);
+/* Retires finished requests and admits queued ones; does not block on
+ * running work. `running` (optional) gets the number of busy slots. */
+int mdg_server_progress(mdg_server* srv, size_t* running);
+/* progress(), then hands out up to `cap` ids of requests finished since the
+ * last poll. */
+int mdg_server_poll(mdg_server* srv, uint64_t* ids, size_t cap, size_t* count);
+/* Drives progress until request `id` is finished or `timeout_s` passes
+ * (MDG_ERR_TIMEOUT). */
+int mdg_server_wait(mdg_server* srv, uint64_t id, double timeout_s);
+/* Copies a finished request's atoms (positions, velocities, forces after
+ * the last step; caller order) and its record, then forgets the request.
+ * `atoms` may be NULL to read only the record. MDG_ERR_STATE if it is not
+ * finished. */
+int mdg_server_result(mdg_server* srv, uint64_t id, mdg_atom* atoms, size_t n, mdg_request_info* info);
+int mdg_server_stats_get(mdg_server* srv, mdg_server_stats* out);
+/* Seconds since the server was created (the clock of mdg_request_info). */
+int mdg_server_clock(mdg_server* srv, double* t);
+/* Device bytes a request of n atoms with `neighbours` list entries per atom
+ * is charged at admission. */
+size_t mdg_server_footprint(size_t n, int neighbours);
+
 #ifdef __cplusplus
 }
 #endif

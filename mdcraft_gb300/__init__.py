@@ -18,7 +18,7 @@ import numpy as np
 
 __all__ = [
     "ATOM_DTYPE", "Context", "Domain", "System", "VerletList", "LJsCut", "EAM", "Single", "Multi", "Verlet",
-    "MDGError", "new_atoms", "lib", "lib_path", "PREC_FP64", "PREC_MIXED",
+    "MDGError", "new_atoms", "lib", "lib_path", "PREC_FP64", "PREC_MIXED", "Server",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -91,6 +91,14 @@ def lib():
         "mdg_solver_stages": ([vp, vp], ip), "mdg_verlet_make_step": ([vp, vp, dp], ip),
         "mdg_run": ([vp, vp, dp, C.c_long], ip), "mdg_run_host": ([vp, vp, dp, C.c_long, vp, vp, vp], ip),
         "mdg_system_measure": ([vp, vp], ip), "mdg_system_flags": ([vp, C.POINTER(C.c_uint32)], ip),
+        "mdg_server_create": ([ip, vp, pp], ip), "mdg_server_destroy": ([vp], ip),
+        "mdg_server_submit": ([vp, vp, vp, vp, sz, dp, C.c_long, u64p], ip),
+        "mdg_server_progress": ([vp, C.POINTER(C.c_size_t)], ip),
+        "mdg_server_poll": ([vp, vp, sz, C.POINTER(C.c_size_t)], ip),
+        "mdg_server_wait": ([vp, C.c_uint64, dp], ip),
+        "mdg_server_result": ([vp, C.c_uint64, vp, sz, vp], ip),
+        "mdg_server_stats_get": ([vp, vp], ip), "mdg_server_clock": ([vp, C.POINTER(C.c_double)], ip),
+        "mdg_server_footprint": ([sz, ip], sz),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -427,3 +435,99 @@ class Verlet:
     def run_host(self, sys: System, dt: float, steps: int, pos, vel, force=None):
         fp = _ptr(force) if force is not None else None
         _check(lib().mdg_run_host(self.solver.h, sys.h, dt, int(steps), _ptr(pos), _ptr(vel), fp), allow=(-4,))
+
+
+class _ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int), ("hbm_budget", C.c_size_t), ("max_atoms", C.c_size_t)]
+
+
+class _RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("done", C.c_int), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("rebuilds", C.c_uint64), ("footprint", C.c_size_t)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [("budget", C.c_size_t), ("used", C.c_size_t), ("peak", C.c_size_t), ("queued", C.c_size_t),
+                ("running", C.c_size_t), ("finished", C.c_size_t), ("admitted", C.c_uint64),
+                ("launches", C.c_uint64), ("host_admit_s", C.c_double), ("host_graph_s", C.c_double),
+                ("host_retire_s", C.c_double), ("rechecked", C.c_uint64), ("host_detail_s", C.c_double * 4)]
+
+
+class Server:
+    """Continuous batching of independent systems on one GPU (mdg_server_*).
+
+    Each request is a whole driver loop (``steps`` velocity-Verlet steps with
+    the list rebuilt on decide()) over its own atoms, domain and solver. Up to
+    ``slots`` requests run at once, each on its own stream, admitted in FIFO
+    order as slots and device memory (``hbm_budget`` bytes) free up.
+    """
+
+    def __init__(self, device: int = 0, slots: int = 16, hbm_budget: int = 0, max_atoms: int = 1 << 16):
+        cfg = _ServerConfig(slots, hbm_budget, max_atoms)
+        h = C.c_void_p()
+        _check(lib().mdg_server_create(device, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._solvers = {}  # keep solvers alive while their requests run
+        self._sizes = {}
+
+    def submit(self, solver: "_Solver", domain: Domain, atoms: np.ndarray, dt: float, steps: int) -> int:
+        atoms = np.ascontiguousarray(atoms, dtype=ATOM_DTYPE)
+        rid = C.c_uint64()
+        _check(lib().mdg_server_submit(self.h, solver.h, C.byref(domain.c), _ptr(atoms), len(atoms), dt, steps,
+                                       C.byref(rid)))
+        self._solvers[rid.value] = solver
+        self._sizes[rid.value] = len(atoms)
+        return rid.value
+
+    def progress(self) -> int:
+        k = C.c_size_t()
+        _check(lib().mdg_server_progress(self.h, C.byref(k)))
+        return k.value
+
+    def poll(self, cap: int = 1024) -> list:
+        ids = np.zeros(cap, dtype=np.uint64)
+        k = C.c_size_t()
+        _check(lib().mdg_server_poll(self.h, _ptr(ids), cap, C.byref(k)))
+        return [int(x) for x in ids[:k.value]]
+
+    def wait(self, rid: int, timeout: float = 60.0):
+        _check(lib().mdg_server_wait(self.h, rid, timeout))
+
+    def result(self, rid: int, atoms: bool = True):
+        """(atoms or None, info dict) of a finished request; forgets it."""
+        info = _RequestInfo()
+        out = new_atoms(self._sizes[rid]) if atoms else None
+        _check(lib().mdg_server_result(self.h, rid, _ptr(out) if atoms else None, len(out) if atoms else 0,
+                                       C.byref(info)))
+        self._solvers.pop(rid, None)
+        self._sizes.pop(rid, None)
+        d = {k: getattr(info, k) for k, _ in _RequestInfo._fields_}
+        return out, d
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        _check(lib().mdg_server_stats_get(self.h, C.byref(st)))
+        d = {k: getattr(st, k) for k, _ in _ServerStats._fields_}
+        d["host_detail_s"] = list(d["host_detail_s"])
+        return d
+
+    def clock(self) -> float:
+        t = C.c_double()
+        _check(lib().mdg_server_clock(self.h, C.byref(t)))
+        return t.value
+
+    @staticmethod
+    def footprint(n: int, neighbours: int) -> int:
+        return int(lib().mdg_server_footprint(n, neighbours))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mdg_server_destroy(self.h)
+            self.h = None
+            self._solvers.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -175,6 +176,10 @@ void timer_end(mdg_ctx* ctx, int which, cudaEvent_t start) {
 
 int ensure_pinned(mdg_system* sys, size_t bytes) {
     if (bytes <= sys->pin_bytes) return MDG_OK;
+    if (sys->host_borrowed) {
+        set_error("transfer larger than the owner's pinned staging");
+        return MDG_ERR_INVALID;
+    }
     if (sys->pin) cudaFreeHost(sys->pin);
     sys->pin = nullptr;
     MDG_CUDA(cudaMallocHost(&sys->pin, bytes));
@@ -182,8 +187,42 @@ int ensure_pinned(mdg_system* sys, size_t bytes) {
     return MDG_OK;
 }
 
-// device scratch for host transfers (one per host thread and device)
+int sys_malloc(mdg_system* sys, void** p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    if (sys->pool)
+        MDG_CUDA(cudaMallocFromPoolAsync(p, bytes, sys->pool, sys->ctx->stream));
+    else
+        MDG_CUDA(cudaMalloc(p, bytes));
+    sys->dev_bytes += bytes;
+    return MDG_OK;
+}
+
+void sys_free(mdg_system* sys, void* p, size_t bytes) {
+    if (!p) return;
+    if (bytes == 0) bytes = 16;
+    if (sys->pool)
+        cudaFreeAsync(p, sys->ctx->stream);
+    else
+        cudaFree(p);
+    sys->dev_bytes -= std::min(bytes, sys->dev_bytes);
+}
+
+// device scratch for host transfers (one per host thread and device; per
+// system for pooled systems, whose transfers may overlap other streams)
 static int xfer_buffer(mdg_system* sys, size_t bytes, void** out) {
+    if (sys->pool) {
+        if (bytes > sys->xfer_bytes) {
+            sys_free(sys, sys->xfer, sys->xfer_bytes);
+            sys->xfer = nullptr;
+            sys->xfer_bytes = 0;
+            int rc = sys_malloc(sys, &sys->xfer, bytes);
+            if (rc) return rc;
+            sys->xfer_bytes = bytes;
+        }
+        *out = sys->xfer;
+        return MDG_OK;
+    }
     static thread_local void* buf = nullptr;
     static thread_local size_t cap = 0;
     static thread_local int dev = -1;
@@ -199,53 +238,65 @@ static int xfer_buffer(mdg_system* sys, size_t bytes, void** out) {
     return MDG_OK;
 }
 
-template <typename T>
-static int dalloc(T** p, size_t count) {
-    *p = nullptr;
-    if (count == 0) count = 1;
-    MDG_CUDA(cudaMalloc((void**)p, count * sizeof(T)));
-    return MDG_OK;
+// The per-atom buffers of a system, with their element counts (one table
+// for allocation, release and footprint accounting).
+template <typename F>
+static void for_each_buffer(mdg_system* sys, F&& f) {
+    size_t np = std::max<size_t>(sys->np, 32);
+    for (int q = 0; q < NF64; ++q)
+        for (int b = 0; b < 2; ++b) f((void**)&sys->f64[q][b], np * sizeof(double));
+    for (int q = 0; q < 3; ++q)
+        for (int b = 0; b < 2; ++b) f((void**)&sys->f32[q][b], np * sizeof(float));
+    for (int q = 0; q < NU32; ++q)
+        for (int b = 0; b < 2; ++b) f((void**)&sys->u32[q][b], np * sizeof(uint32_t));
+    for (int q = 0; q < NU16; ++q)
+        for (int b = 0; b < 2; ++b) f((void**)&sys->u16[q][b], np * sizeof(uint16_t));
+    for (int a = 0; a < 3; ++a) {
+        f((void**)&sys->Rc[a], np * sizeof(double));
+        f((void**)&sys->r0[a], np * sizeof(double));
+    }
+    f((void**)&sys->cellp, np * sizeof(uint32_t));
+    f((void**)&sys->pos32, 2 * np * sizeof(float4));
+    f((void**)&sys->o0, np * sizeof(float4));
+    f((void**)&sys->saved_rcut, np * sizeof(double));
+    f((void**)&sys->saved_rns, np * sizeof(double));
+    f((void**)&sys->saved_uid, np * sizeof(uint32_t));
+    f((void**)&sys->slot_of, np * sizeof(uint32_t));
+    f((void**)&sys->bc, np * sizeof(uint8_t));
+    f((void**)&sys->Fp64, (size_t)kMaxKinds * np * sizeof(double));
+    f((void**)&sys->Fp32, (size_t)kMaxKinds * np * sizeof(float));
+    f((void**)&sys->trig32, np * sizeof(float));
+    f((void**)&sys->key, np * sizeof(uint32_t));
+    f((void**)&sys->rank, np * sizeof(uint32_t));
+    f((void**)&sys->src, np * sizeof(uint32_t));
+    f((void**)&sys->ncnt, np * sizeof(uint32_t));
+    f((void**)&sys->dstat, sizeof(DevStatus));
+    f((void**)&sys->dgrid, sizeof(GridParams));
+    f((void**)&sys->red, 16 * sizeof(double));
+}
+
+// Device bytes a system of n atoms holds before its first list (the bin,
+// list and transfer buffers come on top).
+size_t system_base_bytes(size_t n) {
+    mdg_system probe;
+    probe.np = (n + 31) & ~size_t(31);
+    size_t total = 0;
+    for_each_buffer(&probe, [&](void**, size_t b) { total += b; });
+    return total;
 }
 
 int system_alloc(mdg_system* sys) {
-    size_t np = std::max<size_t>(sys->np, 32);
-    int rc;
-#define TRY(x) \
-    if ((rc = (x)) != MDG_OK) return rc
-    for (int f = 0; f < NF64; ++f)
-        for (int b = 0; b < 2; ++b) TRY(dalloc(&sys->f64[f][b], np));
-    for (int f = 0; f < 3; ++f)
-        for (int b = 0; b < 2; ++b) TRY(dalloc(&sys->f32[f][b], np));
-    for (int f = 0; f < NU32; ++f)
-        for (int b = 0; b < 2; ++b) TRY(dalloc(&sys->u32[f][b], np));
-    for (int f = 0; f < NU16; ++f)
-        for (int b = 0; b < 2; ++b) TRY(dalloc(&sys->u16[f][b], np));
-    for (int a = 0; a < 3; ++a) {
-        TRY(dalloc(&sys->Rc[a], np));
-        TRY(dalloc(&sys->r0[a], np));
+    int rc = MDG_OK;
+    for_each_buffer(sys, [&](void** p, size_t b) {
+        if (rc == MDG_OK) rc = sys_malloc(sys, p, b);
+    });
+    if (rc) return rc;
+    if (!sys->host_borrowed) {
+        MDG_CUDA(cudaMallocHost((void**)&sys->hgrid, sizeof(GridParams)));
+        MDG_CUDA(cudaMallocHost((void**)&sys->hstat, sizeof(DevStatus)));
+        MDG_CUDA(cudaMallocHost((void**)&sys->hred, 16 * sizeof(double)));
     }
-    TRY(dalloc(&sys->cellp, np));
-    TRY(dalloc(&sys->pos32, 2 * np));
-    TRY(dalloc(&sys->o0, np));
-    TRY(dalloc(&sys->saved_rcut, np));
-    TRY(dalloc(&sys->saved_rns, np));
-    TRY(dalloc(&sys->saved_uid, np));
-    TRY(dalloc(&sys->slot_of, np));
-    TRY(dalloc(&sys->bc, np));
-    TRY(dalloc(&sys->Fp64, (size_t)kMaxKinds * np));
-    TRY(dalloc(&sys->Fp32, (size_t)kMaxKinds * np));
-    TRY(dalloc(&sys->trig32, np));
-    TRY(dalloc(&sys->key, np));
-    TRY(dalloc(&sys->rank, np));
-    TRY(dalloc(&sys->src, np));
-    TRY(dalloc(&sys->ncnt, np));
-    TRY(dalloc(&sys->dstat, 1));
-    TRY(dalloc(&sys->dgrid, 1));
-    TRY(dalloc(&sys->red, 16));
-#undef TRY
-    MDG_CUDA(cudaMallocHost((void**)&sys->hgrid, sizeof(GridParams)));
-    MDG_CUDA(cudaMallocHost((void**)&sys->hstat, sizeof(DevStatus)));
-    MDG_CUDA(cudaMallocHost((void**)&sys->hred, 16 * sizeof(double)));
+    size_t np = std::max<size_t>(sys->np, 32);
     cudaStream_t st = sys->ctx->stream;
     MDG_CUDA(cudaMemsetAsync(sys->dstat, 0, sizeof(DevStatus), st));
     MDG_CUDA(cudaMemsetAsync(sys->ncnt, 0, np * sizeof(uint32_t), st));
@@ -257,35 +308,34 @@ int system_alloc(mdg_system* sys) {
         k_iota<<<nblk(sys->n), kBlock, 0, st>>>((int)sys->n, sys->u32[ORIG][0], sys->slot_of);
         MDG_LAUNCHED(sys->ctx);
     }
-    MDG_CUDA(cudaStreamSynchronize(st));
+    // a pooled system's buffers are stream-ordered: nothing to wait for
+    if (!sys->pool) MDG_CUDA(cudaStreamSynchronize(st));
     return MDG_OK;
 }
 
 void system_free(mdg_system* sys) {
     if (sys->run_exec) cudaGraphExecDestroy(sys->run_exec);
     if (sys->run_graph) cudaGraphDestroy(sys->run_graph);
-    cudaFree(sys->dcounter);
-    for (int f = 0; f < NF64; ++f)
-        for (int b = 0; b < 2; ++b) cudaFree(sys->f64[f][b]);
-    for (int f = 0; f < 3; ++f)
-        for (int b = 0; b < 2; ++b) cudaFree(sys->f32[f][b]);
-    for (int f = 0; f < NU32; ++f)
-        for (int b = 0; b < 2; ++b) cudaFree(sys->u32[f][b]);
-    for (int f = 0; f < NU16; ++f)
-        for (int b = 0; b < 2; ++b) cudaFree(sys->u16[f][b]);
-    for (int a = 0; a < 3; ++a) {
-        cudaFree(sys->Rc[a]);
-        cudaFree(sys->r0[a]);
+    sys->run_exec = nullptr;
+    sys->run_graph = nullptr;
+    sys_free(sys, sys->dcounter, sizeof(unsigned long long));
+    for_each_buffer(sys, [&](void** p, size_t b) {
+        sys_free(sys, *p, b);
+        *p = nullptr;
+    });
+    sys_free(sys, sys->bin_count, sys->bin_cap * sizeof(uint32_t));
+    sys_free(sys, sys->bin_start, sys->bin_cap * sizeof(uint32_t));
+    sys_free(sys, sys->scan_tmp, sys->scan_cap * sizeof(uint32_t));
+    sys_free(sys, sys->part, sys->part_cap * 8 * sizeof(double));
+    sys_free(sys, sys->nbr, (size_t)sys->K * sys->np * sizeof(uint32_t));
+    sys_free(sys, sys->xfer, sys->xfer_bytes);
+    if (!sys->host_borrowed) {
+        if (sys->hcounter) cudaFreeHost(sys->hcounter);
+        cudaFreeHost(sys->hgrid);
+        cudaFreeHost(sys->hstat);
+        cudaFreeHost(sys->hred);
+        if (sys->pin) cudaFreeHost(sys->pin);
     }
-    void* ps[] = {sys->cellp, sys->pos32, sys->o0, sys->saved_rcut, sys->saved_rns, sys->saved_uid,
-                  sys->slot_of, sys->bc, sys->Fp64, sys->Fp32, sys->trig32, sys->key, sys->rank, sys->src,
-                  sys->bin_count, sys->bin_start, sys->scan_tmp, sys->part, sys->nbr, sys->ncnt, sys->dstat,
-                  sys->dgrid, sys->red};
-    for (void* p : ps) cudaFree(p);
-    cudaFreeHost(sys->hgrid);
-    cudaFreeHost(sys->hstat);
-    cudaFreeHost(sys->hred);
-    if (sys->pin) cudaFreeHost(sys->pin);
 }
 
 // ---------------------------------------------------------------------------
@@ -577,8 +627,11 @@ int mdg_ctx_stage_time(mdg_ctx* ctx, int which, double* total_ms, uint64_t* laun
     return MDG_OK;
 }
 
-int mdg_system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n, mdg_system** out) {
-    if (!ctx || !domain || !out) return MDG_ERR_INVALID;
+}  // extern "C"
+
+namespace mdg {
+
+int system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n, const SystemMemory* mem, mdg_system** out) {
     *out = nullptr;
     if (n >= kMaxAtoms) {
         set_error("system too large: at most 2^25 - 1 atoms per system");
@@ -592,6 +645,16 @@ int mdg_system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n, mdg_syst
     s->dim = std::fabs(-zs) > 1e-15 ? 3 : std::fabs(-ys) > 1e-15 ? 2 : 1;
     s->n = n;
     s->np = (n + 31) & ~size_t(31);
+    if (mem) {
+        s->pool = mem->pool;
+        s->host_borrowed = 1;
+        s->hgrid = mem->hgrid;
+        s->hstat = mem->hstat;
+        s->hred = mem->hred;
+        s->hcounter = mem->hcounter;
+        s->pin = mem->pin;
+        s->pin_bytes = mem->pin_bytes;
+    }
     int rc = system_alloc(s);
     if (rc) {
         system_free(s);
@@ -603,14 +666,29 @@ int mdg_system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n, mdg_syst
     return MDG_OK;
 }
 
-int mdg_system_destroy(mdg_system* sys) {
-    if (!sys) return MDG_ERR_INVALID;
+// Frees a system without waiting: pooled buffers are released in stream
+// order behind its last work.
+void system_release(mdg_system* sys) {
     mdg_ctx* ctx = sys->ctx;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    if (!sys->pool) cudaStreamSynchronize(ctx->stream);
     system_free(sys);
     delete sys;
     ctx_release(ctx);
+}
+
+}  // namespace mdg
+
+extern "C" {
+
+int mdg_system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n, mdg_system** out) {
+    if (!ctx || !domain || !out) return MDG_ERR_INVALID;
+    return system_create(ctx, domain, n, nullptr, out);
+}
+
+int mdg_system_destroy(mdg_system* sys) {
+    if (!sys) return MDG_ERR_INVALID;
+    system_release(sys);
     return MDG_OK;
 }
 
@@ -620,13 +698,16 @@ int mdg_system_size(mdg_system* sys, size_t* n) {
     return MDG_OK;
 }
 
-int mdg_system_upload_atoms(mdg_system* sys, const mdg_atom* atoms, size_t n) {
-    if (!sys || (!atoms && n) || n != sys->n) {
-        set_error("atom count differs from the system size");
-        return MDG_ERR_INVALID;
-    }
-    if (n == 0) return MDG_OK;
-    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+static int sync_forces64(mdg_system* sys);
+
+}  // extern "C"
+
+namespace mdg {
+
+// Stages the atoms through the system's pinned buffer and scatters them on
+// the device; does not wait (the pinned buffer is busy until the stream has
+// passed this point).
+int upload_atoms_enqueue(mdg_system* sys, const mdg_atom* atoms, size_t n) {
     cudaStream_t st = sys->ctx->stream;
     size_t bytes = n * sizeof(mdg_atom);
     void* dbuf;
@@ -643,7 +724,41 @@ int mdg_system_upload_atoms(mdg_system* sys, const mdg_atom* atoms, size_t n) {
         rc = launch_offsets(sys);
         if (rc) return rc;
     }
-    MDG_CUDA(cudaStreamSynchronize(st));
+    return MDG_OK;
+}
+
+// Gathers the atoms (caller order, FP64 forces) into the system's pinned
+// buffer; does not wait.
+int download_atoms_enqueue(mdg_system* sys, size_t n) {
+    cudaStream_t st = sys->ctx->stream;
+    size_t bytes = n * sizeof(mdg_atom);
+    void* dbuf;
+    int rc = ensure_pinned(sys, bytes);
+    if (rc) return rc;
+    rc = xfer_buffer(sys, bytes, &dbuf);
+    if (rc) return rc;
+    rc = sync_forces64(sys);
+    if (rc) return rc;
+    k_atoms_out<<<nblk(n), kBlock, 0, st>>>(xfer_args(sys), sys->bc, (mdg_atom*)dbuf);
+    MDG_LAUNCHED(sys->ctx);
+    MDG_CUDA(cudaMemcpyAsync(sys->pin, dbuf, bytes, cudaMemcpyDeviceToHost, st));
+    return MDG_OK;
+}
+
+}  // namespace mdg
+
+extern "C" {
+
+int mdg_system_upload_atoms(mdg_system* sys, const mdg_atom* atoms, size_t n) {
+    if (!sys || (!atoms && n) || n != sys->n) {
+        set_error("atom count differs from the system size");
+        return MDG_ERR_INVALID;
+    }
+    if (n == 0) return MDG_OK;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    int rc = upload_atoms_enqueue(sys, atoms, n);
+    if (rc) return rc;
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
     return MDG_OK;
 }
 
@@ -660,20 +775,10 @@ int mdg_system_download_atoms(mdg_system* sys, mdg_atom* atoms, size_t n) {
     if (!sys || (!atoms && n) || n != sys->n) return MDG_ERR_INVALID;
     if (n == 0) return MDG_OK;
     MDG_CUDA(cudaSetDevice(sys->ctx->device));
-    cudaStream_t st = sys->ctx->stream;
-    size_t bytes = n * sizeof(mdg_atom);
-    void* dbuf;
-    int rc = ensure_pinned(sys, bytes);
+    int rc = download_atoms_enqueue(sys, n);
     if (rc) return rc;
-    rc = xfer_buffer(sys, bytes, &dbuf);
-    if (rc) return rc;
-    rc = sync_forces64(sys);
-    if (rc) return rc;
-    k_atoms_out<<<nblk(n), kBlock, 0, st>>>(xfer_args(sys), sys->bc, (mdg_atom*)dbuf);
-    MDG_LAUNCHED(sys->ctx);
-    MDG_CUDA(cudaMemcpyAsync(sys->pin, dbuf, bytes, cudaMemcpyDeviceToHost, st));
-    MDG_CUDA(cudaStreamSynchronize(st));
-    memcpy(atoms, sys->pin, bytes);
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    memcpy(atoms, sys->pin, n * sizeof(mdg_atom));
     return MDG_OK;
 }
 
@@ -1247,15 +1352,16 @@ static void graph_free(mdg_system* sys) {
     sys->run_graph = nullptr;
 }
 
-// kernels launched by one step / one rebuild (launch accounting)
-static int g_step_kernels = 0, g_rebuild_kernels = 0;
 
 static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt) {
     graph_free(sys);
     mdg_ctx* ctx = sys->ctx;
     cudaStream_t st = ctx->stream;
     int prec = s->precision;
-    if (!sys->dcounter) MDG_CUDA(cudaMalloc(&sys->dcounter, sizeof(unsigned long long)));
+    if (!sys->dcounter) {
+        int rc = sys_malloc(sys, (void**)&sys->dcounter, sizeof(unsigned long long));
+        if (rc) return rc;
+    }
     cudaGraph_t g = nullptr;
     MDG_CUDA(cudaGraphCreate(&g, 0));
     sys->run_graph = g;
@@ -1307,7 +1413,7 @@ static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, dou
     cudaError_t e2 = cudaStreamEndCapture(st, &out);
     if (rc) return rc;
     if (e2 != cudaSuccess) return cuda_status(e2, "step capture");
-    g_step_kernels = (int)(ctx->launches - l0);
+    sys->run_step_kernels = (int)(ctx->launches - l0);
 
     l0 = ctx->launches;
     MDG_CUDA(cudaStreamBeginCaptureToGraph(st, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
@@ -1317,53 +1423,197 @@ static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, dou
     e2 = cudaStreamEndCapture(st, &out);
     if (rc) return rc;
     if (e2 != cudaSuccess) return cuda_status(e2, "rebuild capture");
-    g_rebuild_kernels = (int)(ctx->launches - l0);
-    ctx->launches -= (uint64_t)g_step_kernels + (uint64_t)g_rebuild_kernels;  // counted when run
+    sys->run_rebuild_kernels = (int)(ctx->launches - l0);
+    ctx->launches -= (uint64_t)sys->run_step_kernels + (uint64_t)sys->run_rebuild_kernels;  // counted when run
     MDG_CUDA(cudaGraphInstantiate(&sys->run_exec, g, 0));
     return MDG_OK;
 }
 
-static int run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt, long steps) {
+// Enqueues `left` steps as one graph launch plus the read-back of the
+// remaining-step counter and the status words into pinned memory; does not
+// wait.
+int run_graph_launch(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt, long left) {
     mdg_ctx* ctx = sys->ctx;
     cudaStream_t st = ctx->stream;
+    uint64_t dtbits;
+    memcpy(&dtbits, &dt, sizeof(dtbits));
+    uint64_t key[4] = {(uint64_t)(uintptr_t)s, dtbits, (uint64_t)s->precision + 2 * (uint64_t)ext(s)->version,
+                       sys->cap_version};
+    if (!sys->run_exec || memcmp(key, sys->run_key, sizeof(key)) != 0) {
+        auto t0 = std::chrono::steady_clock::now();
+        int rc = build_run_graph(s, sys, ps, dt);
+        if (rc) {
+            graph_free(sys);
+            return rc;
+        }
+        memcpy(sys->run_key, key, sizeof(key));
+        sys->graph_build_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (!sys->hcounter) MDG_CUDA(cudaMallocHost((void**)&sys->hcounter, sizeof(unsigned long long)));
+    k_set_counter<<<1, 32, 0, st>>>(sys->dcounter, (unsigned long long)left, sys->dstat);
+    MDG_LAUNCHED(ctx);
+    MDG_CUDA(cudaGraphLaunch(sys->run_exec, st));
+    MDG_CUDA(cudaMemcpyAsync(sys->hcounter, sys->dcounter, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaMemcpyAsync(sys->hstat, sys->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+    sys->run_launched = left;
+    return MDG_OK;
+}
+
+// After the stream work of run_graph_launch completed: bookkeeping, and the
+// capacity growth (host path) when the last rebuild overflowed. *left gets
+// the steps still to run.
+int run_graph_finish(mdg_solver* s, mdg_system* sys, long* left) {
+    mdg_ctx* ctx = sys->ctx;
+    long rem = (long)*sys->hcounter;
+    long done = sys->run_launched - rem;
+    uint32_t nreb = sys->hstat->pad[0];
+    sys->rebuilds += nreb;
+    ctx->launches += (uint64_t)done * sys->run_step_kernels + (uint64_t)nreb * sys->run_rebuild_kernels;
+    sys->force_prec = s->precision;
+    *left = rem;
+    if (sys->hstat->build_flags & FLAG_OVERFLOW) {
+        // the last step's rebuild outgrew a capacity: rebuild on the host
+        // path, which grows it, then resume
+        sys->rebuilds--;
+        int rc = nlist_build(sys, -1.0, sys->half);
+        if (rc && rc != MDG_ERR_RANGE) return rc;
+        rc = launch_trig(sys);
+        if (rc) return rc;
+    }
+    return MDG_OK;
+}
+
+static int run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt, long steps) {
     long left = steps;
     for (int round = 0; left > 0 && round < 64; ++round) {
-        uint64_t dtbits;
-        memcpy(&dtbits, &dt, sizeof(dtbits));
-        uint64_t key[4] = {(uint64_t)(uintptr_t)s, dtbits, (uint64_t)s->precision + 2 * (uint64_t)ext(s)->version,
-                           sys->cap_version};
-        if (!sys->run_exec || memcmp(key, sys->run_key, sizeof(key)) != 0) {
-            int rc = build_run_graph(s, sys, ps, dt);
-            if (rc) {
-                graph_free(sys);
-                return rc;
-            }
-            memcpy(sys->run_key, key, sizeof(key));
-        }
-        k_set_counter<<<1, 32, 0, st>>>(sys->dcounter, (unsigned long long)left, sys->dstat);
-        MDG_LAUNCHED(ctx);
-        MDG_CUDA(cudaGraphLaunch(sys->run_exec, st));
-        unsigned long long rem = 0;
-        MDG_CUDA(cudaMemcpyAsync(&rem, sys->dcounter, sizeof(rem), cudaMemcpyDeviceToHost, st));
-        MDG_CUDA(cudaMemcpyAsync(sys->hstat, sys->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
-        MDG_CUDA(cudaStreamSynchronize(st));
-        long done = left - (long)rem;
-        uint32_t nreb = sys->hstat->pad[0];
-        sys->rebuilds += nreb;
-        ctx->launches += (uint64_t)done * g_step_kernels + (uint64_t)nreb * g_rebuild_kernels;
-        sys->force_prec = s->precision;
-        left = (long)rem;
-        if (sys->hstat->build_flags & FLAG_OVERFLOW) {
-            // the last step's rebuild outgrew a capacity: rebuild on the host
-            // path, which grows it, then resume
-            sys->rebuilds--;
-            int rc = nlist_build(sys, -1.0, sys->half);
-            if (rc && rc != MDG_ERR_RANGE) return rc;
-            rc = launch_trig(sys);
-            if (rc) return rc;
-        }
+        int rc = run_graph_launch(s, sys, ps, dt, left);
+        if (rc) return rc;
+        MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+        rc = run_graph_finish(s, sys, &left);
+        if (rc) return rc;
     }
     return left > 0 ? MDG_ERR_OVERFLOW : MDG_OK;
+}
+
+}  // namespace mdg
+
+extern "C" {
+
+}  // extern "C"
+
+namespace mdg {
+
+// Before the graph loop: the mixed form prepares rcut and the boundary flags
+// once, rebuilds when that or an upload invalidated the list, and refreshes
+// the offsets; forces are brought into the solver's arithmetic.
+static int graph_prologue(mdg_solver* s, mdg_system* sys) {
+    int rc;
+    if (s->precision == MDG_PREC_MIXED) {
+        rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
+        if (rc) return rc;
+        int need = 0;
+        rc = mdg_nlist_decide(sys, &need);
+        if (rc) return rc;
+        if (need) {
+            rc = mdg_nlist_update(sys, -1.0, 0);
+            if (rc && rc != MDG_ERR_RANGE) return rc;
+        }
+        rc = launch_offsets(sys);
+        if (rc) return rc;
+    }
+    if (sys->force_prec != s->precision) {
+        rc = launch_force_copy(sys, s->precision == MDG_PREC_FP64);
+        if (rc) return rc;
+        sys->force_prec = s->precision;
+    }
+    return MDG_OK;
+}
+
+int run_async_begin(mdg_solver* s, mdg_system* sys, double dt, long steps) {
+    PotSet ps;
+    int rc = check_ready(s, sys, &ps);
+    if (rc) return rc;
+    if (sys->ctx->timing || sys->n == 0 || sys->half) {
+        set_error("overlapped runs need a non-empty system with full lists and timing off");
+        return MDG_ERR_STATE;
+    }
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    rc = graph_prologue(s, sys);
+    if (rc) return rc;
+    sys->run_launched = 0;
+    if (steps <= 0) return MDG_OK;
+    return run_graph_launch(s, sys, ps, dt, steps);
+}
+
+// The whole driver of one request, enqueued on the system's stream with no
+// host wait: upload, prepare (rcut, boundary flags), the first list build
+// (capacities sized on the host from the same atoms), the initial forces,
+// then the graph loop. `first_status` receives the device status right after
+// the first build (pinned; valid once the stream passes it): a capacity
+// overflow there voids the run and the caller repeats it on the checked
+// path. Same operations, in the same order on the device, as
+// upload + update(-1) + prepare + stages + mdg_run.
+int request_begin(mdg_solver* s, mdg_system* sys, const mdg_atom* atoms, double dt, long steps,
+                  DevStatus* first_status) {
+    if (!s || s->nstages == 0) {
+        set_error("solver has no potential");
+        return MDG_ERR_STATE;
+    }
+    if (sys->n == 0 || sys->ctx->timing) {
+        set_error("overlapped runs need a non-empty system and timing off");
+        return MDG_ERR_STATE;
+    }
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    cudaStream_t st = sys->ctx->stream;
+    int rc = upload_atoms_enqueue(sys, atoms, sys->n);
+    if (rc) return rc;
+    rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
+    if (rc) return rc;
+    rc = nlist_capacity_host(sys, atoms, sys->n, 0);
+    if (rc) return rc;
+    sys->grid = *sys->hgrid;
+    rc = nlist_enqueue(sys);
+    if (rc) return rc;
+    rc = launch_trig(sys);
+    if (rc) return rc;
+    sys->have_list = 1;
+    sys->dirty = 0;
+    sys->rebuilds++;
+    MDG_CUDA(cudaMemcpyAsync(first_status, sys->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
+    PotSet ps;
+    rc = check_ready(s, sys, &ps);
+    if (rc) return rc;
+    if (s->precision == MDG_PREC_MIXED) {
+        rc = launch_offsets(sys);
+        if (rc) return rc;
+    }
+    rc = launch_zero(sys, ps.any_eam);
+    if (rc) return rc;
+    rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
+    if (rc) return rc;
+    for (int k = 0; k < s->nstages; ++k) {
+        rc = stage_impl(s, sys, ps, s->stages[k], s->precision);
+        if (rc) return rc;
+    }
+    sys->run_launched = 0;
+    if (steps <= 0) return MDG_OK;
+    return run_graph_launch(s, sys, ps, dt, steps);
+}
+
+int run_async_end(mdg_solver* s, mdg_system* sys, double dt, int* relaunched) {
+    *relaunched = 0;
+    if (sys->run_launched <= 0) return MDG_OK;
+    long left = 0;
+    int rc = run_graph_finish(s, sys, &left);
+    if (rc) return rc;
+    if (left <= 0) return MDG_OK;
+    PotSet ps;
+    rc = check_ready(s, sys, &ps);
+    if (rc) return rc;
+    rc = run_graph_launch(s, sys, ps, dt, left);
+    if (rc) return rc;
+    *relaunched = 1;
+    return MDG_OK;
 }
 
 }  // namespace mdg
@@ -1376,24 +1626,8 @@ int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
     if (rc) return rc;
     if (steps <= 0) return MDG_OK;
     if (!sys->ctx->timing && sys->n > 0 && !sys->half) {
-        if (s->precision == MDG_PREC_MIXED) {
-            rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
-            if (rc) return rc;
-            int need = 0;
-            rc = mdg_nlist_decide(sys, &need);
-            if (rc) return rc;
-            if (need) {
-                rc = mdg_nlist_update(sys, -1.0, 0);
-                if (rc && rc != MDG_ERR_RANGE) return rc;
-            }
-            rc = launch_offsets(sys);
-            if (rc) return rc;
-        }
-        if (sys->force_prec != s->precision) {
-            rc = launch_force_copy(sys, s->precision == MDG_PREC_FP64);
-            if (rc) return rc;
-            sys->force_prec = s->precision;
-        }
+        rc = graph_prologue(s, sys);
+        if (rc) return rc;
         return run_graph(s, sys, ps, dt, steps);
     }
     cudaStream_t st = sys->ctx->stream;

@@ -413,9 +413,11 @@ int launch_measure(mdg_system* sys, double out[11]) {
     A.vz = sys->f64[VZ][c];
     int nparts = std::min(std::max(nblk(sys->n), 1), 4 * std::max(ctx->num_sms, 1));
     if ((size_t)nparts > sys->part_cap) {
-        cudaFree(sys->part);
+        sys_free(sys, sys->part, sys->part_cap * 8 * sizeof(double));
         sys->part = nullptr;
-        MDG_CUDA(cudaMalloc(&sys->part, (size_t)nparts * 8 * sizeof(double)));
+        sys->part_cap = 0;
+        int rc = sys_malloc(sys, (void**)&sys->part, (size_t)nparts * 8 * sizeof(double));
+        if (rc) return rc;
         sys->part_cap = nparts;
     }
     A.part = sys->part;

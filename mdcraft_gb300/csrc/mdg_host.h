@@ -127,6 +127,7 @@ struct mdg_system {
     uint32_t* bin_start = nullptr;  // nbins + 1
     uint32_t* scan_tmp = nullptr;
     size_t bin_cap = 0;
+    size_t scan_cap = 0;  // scan_tmp elements
     double* part = nullptr;  // per-block bounds partials
     size_t part_cap = 0;
 
@@ -146,6 +147,11 @@ struct mdg_system {
     cudaGraph_t run_graph = nullptr;
     uint64_t run_key[4] = {0, 0, 0, 0};
     unsigned long long* dcounter = nullptr;  // steps left (device)
+    unsigned long long* hcounter = nullptr;  // its read-back (pinned)
+    long run_launched = 0;                   // steps handed to the last graph launch
+    int run_step_kernels = 0;                // kernels per step / per rebuild in the graph
+    int run_rebuild_kernels = 0;
+    double graph_build_s = 0.0;              // host seconds spent building run graphs
 
     // device status + grid
     mdg::DevStatus* dstat = nullptr;
@@ -161,6 +167,17 @@ struct mdg_system {
     void* pin = nullptr;
     size_t pin_bytes = 0;
 
+    // Allocation mode. With a pool, every device buffer of the system comes
+    // stream-ordered from it and is released with cudaFreeAsync, so creating
+    // and destroying systems never waits for the whole device; the pinned
+    // host buffers then belong to the owner (host_borrowed) and the transfer
+    // staging is per system (xfer).
+    cudaMemPool_t pool = nullptr;
+    int host_borrowed = 0;
+    void* xfer = nullptr;
+    size_t xfer_bytes = 0;
+    size_t dev_bytes = 0;  // device bytes held now
+
     double* cur64(int f) { return f64[f][cur]; }
     float* cur32(int c) { return f32[c][cur]; }
     uint32_t* curu32(int f) { return u32[f][cur]; }
@@ -168,8 +185,35 @@ struct mdg_system {
 };
 
 namespace mdg {
+// Device buffers of a system (pool-ordered on its stream when it has a pool).
+int sys_malloc(mdg_system* sys, void** p, size_t bytes);
+void sys_free(mdg_system* sys, void* p, size_t bytes);
 int system_alloc(mdg_system* sys);
 void system_free(mdg_system* sys);
+// Memory a system is given instead of allocating its own: a device pool and
+// the owner's pinned status words and transfer staging.
+struct SystemMemory {
+    cudaMemPool_t pool = nullptr;
+    GridParams* hgrid = nullptr;
+    DevStatus* hstat = nullptr;
+    double* hred = nullptr;  // 16 doubles
+    unsigned long long* hcounter = nullptr;
+    void* pin = nullptr;
+    size_t pin_bytes = 0;
+};
+int system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n, const SystemMemory* mem, mdg_system** out);
+void system_release(mdg_system* sys);
+size_t system_base_bytes(size_t n);
+// Graph-driven run split for callers that overlap systems: begin checks the
+// system, prepares it and launches `steps` steps without waiting; end runs
+// once the stream's work is complete and relaunches what an overflowed
+// rebuild left (returns 1 when it relaunched, 0 when the run is finished).
+int run_async_begin(mdg_solver* s, mdg_system* sys, double dt, long steps);
+int run_async_end(mdg_solver* s, mdg_system* sys, double dt, int* relaunched);
+int request_begin(mdg_solver* s, mdg_system* sys, const mdg_atom* atoms, double dt, long steps,
+                  DevStatus* first_status);
+int download_atoms_enqueue(mdg_system* sys, size_t n);
+int nlist_capacity_host(mdg_system* sys, const mdg_atom* atoms, size_t n, int half);
 int nlist_build(mdg_system* sys, double kbuf, int half);
 int nlist_capacity(mdg_system* sys, int half);
 int nlist_enqueue(mdg_system* sys);

@@ -68,35 +68,18 @@ __global__ void k_wrap_bounds(int n, double* __restrict__ rx, double* __restrict
     if (t < 7) part[blockIdx.x * 8 + t] = sh[t][0];
 }
 
-__global__ void k_grid_finalize(const double* __restrict__ part, int nparts, DomainDev d,
-                                GridParams* __restrict__ out, long long bin_cap, DevStatus* st) {
-    __shared__ double sh[7][kBlock];
-    int t = threadIdx.x;
-    double v[7] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308,
-                   -1.7976931348623157e308, -1.7976931348623157e308, -1.7976931348623157e308, 0.0};
-    for (int b = t; b < nparts; b += blockDim.x) {
-        for (int k = 0; k < 3; ++k) v[k] = fmin(v[k], part[b * 8 + k]);
-        for (int k = 3; k < 7; ++k) v[k] = fmax(v[k], part[b * 8 + k]);
-    }
-    for (int k = 0; k < 7; ++k) sh[k][t] = v[k];
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (t < s) {
-            for (int k = 0; k < 3; ++k) sh[k][t] = fmin(sh[k][t], sh[k][t + s]);
-            for (int k = 3; k < 7; ++k) sh[k][t] = fmax(sh[k][t], sh[k][t + s]);
-        }
-        __syncthreads();
-    }
-    if (t != 0) return;
-    GridParams g;
+// Grid::build (grid.cxx:43-95) from the reduced bounds and the largest rns;
+// shared by the device rebuild and the host-side capacity sizing, so both
+// get the same parameters bit for bit.
+__host__ __device__ void grid_from_bounds(const DomainDev& d, const double lo_in[3], const double hi_in[3],
+                                          double cell, GridParams& g) {
     memset(&g, 0, sizeof(g));
     g.dim = d.dim;
     double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     for (int i = 0; i < d.dim; ++i) {
-        lo[i] = sh[i][0];
-        hi[i] = sh[3 + i][0];
+        lo[i] = lo_in[i];
+        hi[i] = hi_in[i];
     }
-    double cell = sh[6][0];
     g.max_rns = cell;
     for (int i = 0; i < 3; ++i) {
         g.bmin[i] = d.bmin[i];
@@ -108,10 +91,8 @@ __global__ void k_grid_finalize(const double* __restrict__ part, int nparts, Dom
     }
     if (!(cell > 0.0)) {
         g.empty = -1;
-        *out = g;
         return;
     }
-    // Grid::build (grid.cxx:43-95)
     for (int i = 0; i < d.dim; ++i) {
         double q = floor(d.size[i] / cell);
         int c = q > 1.0e9 ? 1000000000 : (int)q;
@@ -144,6 +125,36 @@ __global__ void k_grid_finalize(const double* __restrict__ part, int nparts, Dom
     if (nb > (1LL << 30)) g.empty = -2;
     g.ncells = (int)nc;
     g.nbins = (int)nb;
+}
+
+__global__ void k_grid_finalize(const double* __restrict__ part, int nparts, DomainDev d,
+                                GridParams* __restrict__ out, long long bin_cap, DevStatus* st) {
+    __shared__ double sh[7][kBlock];
+    int t = threadIdx.x;
+    double v[7] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308,
+                   -1.7976931348623157e308, -1.7976931348623157e308, -1.7976931348623157e308, 0.0};
+    for (int b = t; b < nparts; b += blockDim.x) {
+        for (int k = 0; k < 3; ++k) v[k] = fmin(v[k], part[b * 8 + k]);
+        for (int k = 3; k < 7; ++k) v[k] = fmax(v[k], part[b * 8 + k]);
+    }
+    for (int k = 0; k < 7; ++k) sh[k][t] = v[k];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (t < s) {
+            for (int k = 0; k < 3; ++k) sh[k][t] = fmin(sh[k][t], sh[k][t + s]);
+            for (int k = 3; k < 7; ++k) sh[k][t] = fmax(sh[k][t], sh[k][t + s]);
+        }
+        __syncthreads();
+    }
+    if (t != 0) return;
+    GridParams g;
+    double lo[3] = {sh[0][0], sh[1][0], sh[2][0]}, hi[3] = {sh[3][0], sh[4][0], sh[5][0]};
+    grid_from_bounds(d, lo, hi, sh[6][0], g);
+    if (g.empty == -1) {
+        *out = g;
+        return;
+    }
+    long long nb = g.nbins;
     // the bin arrays were sized on the host; a grid that outgrew them
     // invalidates this rebuild (every later kernel of it returns early)
     if (g.empty == 0 && nb + 1 > bin_cap) {
@@ -551,14 +562,18 @@ static int ensure_bins(mdg_system* sys, long long nbins) {
     if ((size_t)nbins + 1 <= sys->bin_cap) return MDG_OK;
     size_t cap = (size_t)nbins + 1;
     cap = cap + cap / 8 + 4096;
-    cudaFree(sys->bin_count);
-    cudaFree(sys->bin_start);
-    cudaFree(sys->scan_tmp);
+    sys_free(sys, sys->bin_count, sys->bin_cap * sizeof(uint32_t));
+    sys_free(sys, sys->bin_start, sys->bin_cap * sizeof(uint32_t));
+    sys_free(sys, sys->scan_tmp, sys->scan_cap * sizeof(uint32_t));
     sys->bin_count = sys->bin_start = sys->scan_tmp = nullptr;
-    MDG_CUDA(cudaMalloc(&sys->bin_count, cap * sizeof(uint32_t)));
-    MDG_CUDA(cudaMalloc(&sys->bin_start, cap * sizeof(uint32_t)));
-    MDG_CUDA(cudaMalloc(&sys->scan_tmp, (cap / (kScanT * kScanItems) + 2) * sizeof(uint32_t)));
+    sys->bin_cap = sys->scan_cap = 0;
+    size_t scan = cap / (kScanT * kScanItems) + 2;
+    int rc = sys_malloc(sys, (void**)&sys->bin_count, cap * sizeof(uint32_t));
+    if (!rc) rc = sys_malloc(sys, (void**)&sys->bin_start, cap * sizeof(uint32_t));
+    if (!rc) rc = sys_malloc(sys, (void**)&sys->scan_tmp, scan * sizeof(uint32_t));
+    if (rc) return rc;
     sys->bin_cap = cap;
+    sys->scan_cap = scan;
     sys->cap_version++;
     return MDG_OK;
 }
@@ -566,9 +581,11 @@ static int ensure_bins(mdg_system* sys, long long nbins) {
 static int ensure_list(mdg_system* sys, int K) {
     K = (K + 3) & ~3;
     if (K <= sys->K && sys->nbr) return MDG_OK;
-    cudaFree(sys->nbr);
+    sys_free(sys, sys->nbr, (size_t)sys->K * sys->np * sizeof(uint32_t));
     sys->nbr = nullptr;
-    MDG_CUDA(cudaMalloc(&sys->nbr, (size_t)K * sys->np * sizeof(uint32_t)));
+    sys->K = 0;
+    int rc = sys_malloc(sys, (void**)&sys->nbr, (size_t)K * sys->np * sizeof(uint32_t));
+    if (rc) return rc;
     sys->K = K;
     sys->cap_version++;
     return MDG_OK;
@@ -593,13 +610,17 @@ static int nparts_of(const mdg_system* sys) {
 static int ensure_parts(mdg_system* sys) {
     int nparts = nparts_of(sys);
     if ((size_t)nparts > sys->part_cap) {
-        cudaFree(sys->part);
+        sys_free(sys, sys->part, sys->part_cap * 8 * sizeof(double));
         sys->part = nullptr;
-        MDG_CUDA(cudaMalloc(&sys->part, (size_t)nparts * 8 * sizeof(double)));
+        sys->part_cap = 0;
+        int rc = sys_malloc(sys, (void**)&sys->part, (size_t)nparts * 8 * sizeof(double));
+        if (rc) return rc;
         sys->part_cap = nparts;
     }
     return MDG_OK;
 }
+
+int size_from_grid(mdg_system* sys, const GridParams& g, int half);
 
 // Sizes the bin arrays and the list capacity from one synchronous bounds
 // pass (positions are wrapped by it exactly as by a rebuild).
@@ -619,7 +640,39 @@ int nlist_capacity(mdg_system* sys, int half) {
     MDG_LAUNCHED(ctx);
     MDG_CUDA(cudaMemcpyAsync(sys->hgrid, sys->dgrid, sizeof(GridParams), cudaMemcpyDeviceToHost, st));
     MDG_CUDA(cudaStreamSynchronize(st));
-    GridParams g = *sys->hgrid;
+    return size_from_grid(sys, *sys->hgrid, half);
+}
+
+// The same sizing from atoms still on the host (before they are uploaded):
+// the bounds pass is repeated on the host with the device's arithmetic, so
+// the grid is the one the first rebuild will compute. Nothing waits for the
+// device.
+int nlist_capacity_host(mdg_system* sys, const mdg_atom* atoms, size_t n, int half) {
+    int rc = ensure_parts(sys);
+    if (rc) return rc;
+    DomainDev d = domain_dev(sys);
+    double lo[3] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308};
+    double hi[3] = {-1.7976931348623157e308, -1.7976931348623157e308, -1.7976931348623157e308};
+    double mr = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        for (int a = 0; a < 3; ++a) {
+            double v = atoms[i].r[a];
+            if (d.periodic[a]) v = v < d.bmin[a] ? v + d.size[a] : v > d.bmax[a] ? v - d.size[a] : v;
+            lo[a] = std::min(lo[a], v);
+            hi[a] = std::max(hi[a], v);
+        }
+        mr = std::max(mr, atoms[i].rns);
+    }
+    GridParams g;
+    grid_from_bounds(d, lo, hi, mr, g);
+    *sys->hgrid = g;
+    return size_from_grid(sys, g, half);
+}
+
+// Bin arrays and list capacity for grid g (the grid of the next rebuild).
+int size_from_grid(mdg_system* sys, const GridParams& g, int half) {
+    const int n = (int)sys->n;
+    int rc;
     if (g.empty == -1) {
         set_error("neighbour search radius rns must be positive");
         return MDG_ERR_INVALID;

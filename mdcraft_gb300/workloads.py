@@ -209,3 +209,78 @@ def lj_liquid(nx=128, ny=128, nz=256, seed=4, rho_star=0.8442, T_star=0.72):
     atoms["v"] = maxwell_boltzmann(rng, atoms["m"].copy(), T)
     params = dict(kind="lj", a=eps, s=sigma, rcut=rc, skin=skin, dt=0.005 * tau, steps=200)
     return (*_finish(atoms, (0, 0, 0), (Lx, Ly, Lz)), params)
+
+
+# ---------------------------------------------------------------------------
+# Serving stream: independent requests of uneven size
+# ---------------------------------------------------------------------------
+SERVE_LJ = dict(kind="lj", a=0.526, mass=AR_MASS, eps=0.0104 * EV, sigma=0.3405, rcut=2.5 * 0.3405, skin=0.03,
+                dt=0.002)
+SERVE_EAM = dict(kind="eam", a=0.3615, mass=CU_MASS, re=0.2556, rcut=0.5, skin=0.05, dt=0.001)
+
+
+def serve_eam_tables():
+    """The EAM Cu tables of the serving stream (those of eam_cu_fcc)."""
+    p = SERVE_EAM
+    return fs_tables(0.2, 9.0, p["re"], p["rcut"], rho_max=2.0 * fcc_density(p["a"], p["re"], p["rcut"]))
+
+
+def _serve_dims(n_target, min_cells):
+    """fcc nx*ny*nz cells, near-cubic, 4*nx*ny*nz close to n_target, every
+    dimension at least min_cells (box edge >= 2 rns)."""
+    c = n_target / 4.0
+    nx = max(min_cells, int(round(c ** (1.0 / 3.0))))
+    ny = max(min_cells, int(round(math.sqrt(c / nx))))
+    nz = max(min_cells, int(round(c / (nx * ny))))
+    return nx, ny, nz
+
+
+def serving_stream(count=4096, rate=2000.0, seed=5, steps=1000, n_min=256, n_max=32768, lj_share=0.6):
+    """Request specs of the serving workload: Poisson arrivals at `rate`/s,
+    60% LJ argon / 40% EAM Cu, atom count log-uniform in [n_min, n_max]
+    rounded to fcc nx*ny*nz cells. Atoms are made per request by
+    serving_atoms (seeded by the request index)."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=count))
+    kinds = np.where(rng.random(count) < lj_share, "lj", "eam")
+    logn = rng.uniform(math.log(n_min), math.log(n_max), size=count)
+    out = []
+    for i in range(count):
+        p = SERVE_LJ if kinds[i] == "lj" else SERVE_EAM
+        min_cells = int(math.ceil(2.0 * (p["rcut"] + p["skin"]) / p["a"]))
+        dims = _serve_dims(math.exp(logn[i]), min_cells)
+        out.append(dict(index=i, kind=str(kinds[i]), dims=dims, n=4 * dims[0] * dims[1] * dims[2],
+                        t_arrival=float(t[i]), steps=steps, dt=p["dt"], seed=seed * 1_000_003 + i))
+    return out
+
+
+_SERVE_TEMPLATES = {}
+
+
+def serving_atoms(spec, jitter=0.01, T=300.0):
+    """Atoms and domain of one serving request: fcc lattice with a seeded
+    Gaussian jitter (sigma = jitter * a) and Maxwell-Boltzmann velocities."""
+    p = SERVE_LJ if spec["kind"] == "lj" else SERVE_EAM
+    nx, ny, nz = spec["dims"]
+    key = (spec["kind"], nx, ny, nz)
+    tpl = _SERVE_TEMPLATES.get(key)
+    a = p["a"]
+    L = np.array([nx * a, ny * a, nz * a])
+    if tpl is None:
+        base = fcc_positions(nx, ny, nz, a) + 0.25 * a
+        t = new_atoms(len(base))
+        t["m"] = p["mass"]
+        t["rcut"] = p["rcut"]
+        t["rns"] = p["rcut"] + p["skin"]
+        t["uid"] = np.arange(1, len(base) + 1)
+        t["kind"] = 0
+        tpl = (base, t)
+        if len(_SERVE_TEMPLATES) < 4096:
+            _SERVE_TEMPLATES[key] = tpl
+    base, t = tpl
+    rng = np.random.default_rng(spec["seed"])
+    atoms = t.copy()
+    r = base + rng.standard_normal(base.shape) * (jitter * a)
+    atoms["r"] = np.stack([_wrap_inside(r[:, k], 0.0, L[k]) for k in range(3)], 1)
+    atoms["v"] = maxwell_boltzmann(rng, atoms["m"].copy(), T)
+    return atoms, (0.0, L[0], 0.0, L[1], 0.0, L[2])
