@@ -48,8 +48,10 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=4096)
-    ap.add_argument("--serve-slots", type=int, default=32)
+    ap.add_argument("--serve-slots", type=int, default=320)
     ap.add_argument("--serve-steps", type=int, default=1000)
+    ap.add_argument("--serve-block-threads", type=int, default=512,
+                    help="threads of the fused per-system block (256, 512, 1024; -1: a graph loop per request)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="only the serving stream (prints its summary)")
     return ap.parse_args()
@@ -213,7 +215,7 @@ def run_serving(args, device):
     specs = W.serving_stream(count=args.serve_requests, steps=args.serve_steps)
     solv = SV.solvers("mixed")
     reqs = SV.prepare(specs)
-    srv = mdg.Server(device=device, slots=args.serve_slots, max_atoms=32768)
+    srv = mdg.Server(device=device, slots=args.serve_slots, max_atoms=32768, block_threads=args.serve_block_threads)
     # warm-up: one request of each kind (pool pages, potential tables)
     for kind in ("lj", "eam"):
         s = next(x for x in specs if x["kind"] == kind)
@@ -221,7 +223,7 @@ def run_serving(args, device):
         rid = srv.submit(solv[kind], SV.periodic_domain(box), atoms, s["dt"], 10)
         srv.wait(rid, 120.0)
         srv.result(rid, atoms=False)
-    l0 = srv.stats()["launches"]
+    st0 = srv.stats()
     clocks = Clocks(device)
     clocks.start()
     summary, _ = SV.replay(srv, reqs, solv, release_inputs=True)
@@ -229,8 +231,12 @@ def run_serving(args, device):
     st = srv.stats()
     srv.close()
     summary.update({"workload": SERVE_WORKLOAD, "slots": args.serve_slots, "steps_per_request": args.serve_steps,
+                    "block_threads": args.serve_block_threads,
                     "arrival_rate_per_s": 2000.0, "budget_bytes": st["budget"], "peak_bytes": st["peak"],
-                    "gpu_launches": st["launches"] - l0, "clocks": ck,
+                    # the persistent kernel launched for the warm-up may still be the one that
+                    # serves the stream: count every launch of the server
+                    "gpu_launches": st["launches"], "gpu_launches_in_stream": st["launches"] - st0["launches"],
+                    "clocks": ck,
                     "host_s": {"admit": st["host_admit_s"], "graph": st["host_graph_s"],
                                "retire": st["host_retire_s"],
                                "retire_detail": dict(zip(("bookkeeping", "gather", "graph_release", "memory_release"),

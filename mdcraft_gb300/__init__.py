@@ -438,7 +438,8 @@ class Verlet:
 
 
 class _ServerConfig(C.Structure):
-    _fields_ = [("slots", C.c_int), ("hbm_budget", C.c_size_t), ("max_atoms", C.c_size_t)]
+    _fields_ = [("slots", C.c_int), ("hbm_budget", C.c_size_t), ("max_atoms", C.c_size_t),
+                ("block_threads", C.c_int)]
 
 
 class _RequestInfo(C.Structure):
@@ -462,8 +463,9 @@ class Server:
     order as slots and device memory (``hbm_budget`` bytes) free up.
     """
 
-    def __init__(self, device: int = 0, slots: int = 16, hbm_budget: int = 0, max_atoms: int = 1 << 16):
-        cfg = _ServerConfig(slots, hbm_budget, max_atoms)
+    def __init__(self, device: int = 0, slots: int = 16, hbm_budget: int = 0, max_atoms: int = 1 << 16,
+                 block_threads: int = 0):
+        cfg = _ServerConfig(slots, hbm_budget, max_atoms, block_threads)
         h = C.c_void_p()
         _check(lib().mdg_server_create(device, C.byref(cfg), C.byref(h)))
         self.h = h

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmdg.so")
-SOURCES = ["nlist.cu", "forces.cu", "integrate.cu", "capi.cu", "measure_static.cu", "serve.cu"]
+SOURCES = ["nlist.cu", "forces.cu", "integrate.cu", "capi.cu", "measure_static.cu", "serve.cu", "solo.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

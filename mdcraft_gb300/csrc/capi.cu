@@ -298,6 +298,7 @@ int system_alloc(mdg_system* sys) {
     }
     size_t np = std::max<size_t>(sys->np, 32);
     cudaStream_t st = sys->ctx->stream;
+    if (sys->lazy_init) return MDG_OK;
     MDG_CUDA(cudaMemsetAsync(sys->dstat, 0, sizeof(DevStatus), st));
     MDG_CUDA(cudaMemsetAsync(sys->ncnt, 0, np * sizeof(uint32_t), st));
     MDG_CUDA(cudaMemsetAsync(sys->bc, 0, np, st));
@@ -646,6 +647,7 @@ int system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n, const System
     s->n = n;
     s->np = (n + 31) & ~size_t(31);
     if (mem) {
+        s->lazy_init = mem->lazy_init;
         s->pool = mem->pool;
         s->host_borrowed = 1;
         s->hgrid = mem->hgrid;
@@ -1598,6 +1600,11 @@ int request_begin(mdg_solver* s, mdg_system* sys, const mdg_atom* atoms, double 
     sys->run_launched = 0;
     if (steps <= 0) return MDG_OK;
     return run_graph_launch(s, sys, ps, dt, steps);
+}
+
+const PotSet* solver_potsets(mdg_solver* s, PotSet* host) {
+    if (host) *host = ext(s)->d.host;
+    return ext(s)->d.dev;
 }
 
 int run_async_end(mdg_solver* s, mdg_system* sys, double dt, int* relaunched) {

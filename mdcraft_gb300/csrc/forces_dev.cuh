@@ -1,0 +1,301 @@
+// forces_dev.cuh — per-atom bodies of the mixed-precision force stages,
+// shared by the per-stage kernels (forces.cu) and the fused per-system loop
+// (solo.cu), so both give the same forces bit for bit.
+//
+// LJsCut::compute / EAM::charge and forces (mdcraft/solver/potential/
+// LJs-cut.cxx:22-131, EAM.cxx:141-601) in FP32 pair arithmetic on cell-centred
+// offsets, with compensated per-atom sums.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mdg_internal.cuh"
+
+namespace mdg {
+
+struct FArgs {
+    int n, np;
+    const double *rx, *ry, *rz, *rns;
+    const uint32_t *nbr, *ncnt;
+    const uint16_t *kind, *tag;
+    const uint8_t* bc;
+    double L[3];
+    int periodic[3];
+    float csf[3];
+    // outputs / intermediate
+    double *fx, *fy, *fz;
+    float *gx, *gy, *gz;  // mixed forces
+    double* nc;
+    double* Fp64;
+    float* Fp32;
+    const float4* pos32;
+    float4* pos32b;
+    double *Ep, *Em;
+    double* V[9];
+    DevStatus* st;
+};
+
+// ---------------------------------------------------------------------------
+// mixed precision
+// ---------------------------------------------------------------------------
+struct Kahan3 {
+    float s[3] = {0.f, 0.f, 0.f};
+    float c[3] = {0.f, 0.f, 0.f};
+    __device__ __forceinline__ void add(int k, float v) {
+        float y = v - c[k];
+        float t = s[k] + y;
+        c[k] = (t - s[k]) - y;
+        s[k] = t;
+    }
+};
+
+__device__ __forceinline__ float ksum_add(float& s, float& c, float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+    return s;
+}
+
+// Pair vector r_j - r_i of a list entry, from cell-centred offsets.
+__device__ __forceinline__ void pair_vec32(uint32_t e, const float4& pi, const float4& pj,
+                                           const float csf[3], float& dx, float& dy, float& dz) {
+    dx = (pj.x - pi.x) + image_shift(e, 0, csf[0]);
+    dy = (pj.y - pi.y) + image_shift(e, 1, csf[1]);
+    dz = (pj.z - pi.z) + image_shift(e, 2, csf[2]);
+}
+
+__device__ __forceinline__ float cubic(const float4 c, float u) {
+    return fmaf(u, fmaf(u, fmaf(u, c.w, c.z), c.y), c.x);
+}
+__device__ __forceinline__ float dcubic(const float4 c, float u) {
+    return fmaf(u, fmaf(u, 3.0f * c.w, 2.0f * c.z), c.y);
+}
+
+// Pair entries whose image crossed a periodic face contribute only with
+// the Periodic boundary (without it the reference's raw distance is beyond
+// the cutoff); bit 31 marks them.
+constexpr uint32_t kWrapBit = 1u << 31;
+
+// Cutoff membership of a pair. The FP32 r^2 decides unless it lies within
+// 1e-5 (relative) of rc^2; those rare pairs are decided on the FP64
+// positions, so the mixed form cuts exactly the pairs the FP64 form cuts
+// (the potentials are discontinuous at rc, so a flipped pair would change
+// forces by a whole pair term).
+__device__ __forceinline__ bool cut_in(const FArgs& A, int i, uint32_t j, float r2, float r2c, double R2cut) {
+    if (r2 < 1e-15f) return false;
+    float band = 1e-5f * r2c;
+    if (r2 < r2c - band) return true;
+    if (r2 > r2c + band) return false;
+    double dx = shortest1(A.rx[j] - A.rx[i], A.L[0], A.periodic[0]);
+    double dy = shortest1(A.ry[j] - A.ry[i], A.L[1], A.periodic[1]);
+    double dz = shortest1(A.rz[j] - A.rz[i], A.L[2], A.periodic[2]);
+    return dx * dx + dy * dy + dz * dz <= R2cut;
+}
+
+// Cutoff membership from the FP32 r^2, with the rare pairs inside the
+// 1e-5 band around rc^2 (and entries that crossed a periodic face when the
+// solver has no Periodic boundary) settled exactly.
+__device__ __forceinline__ bool pair_in(const FArgs& A, int i, uint32_t e, float r2, float r2c, double R2c,
+                                        bool per) {
+    bool in = r2 >= 1e-15f && r2 <= r2c;
+    if (fabsf(r2 - r2c) <= 1e-5f * r2c) in = cut_in(A, i, e & kJMask, r2, r2c, R2c);
+    return in && (per || !(e & kWrapBit));
+}
+
+// The pair loops below read four list entries with one 16-byte load, then
+// the four neighbour records, so the loads of a group overlap; the four
+// contributions are summed in FP32 and the group sum enters a Kahan sum.
+
+template <bool MULTI>
+__device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
+    if (A.tag[i] == 0) return;
+    const float4 pi = A.pos32[i];
+    const int ng = A.ncnt[i] >> 2;
+    const int ki = MULTI ? (A.kind[i] & 3) : 0;
+    const bool per = ps->periodic;
+    const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
+    const PotParams& P0 = ps->p[ki][0];
+    float r2c = P0.r2cut_f, l1 = P0.lj1_f, l2 = P0.lj2_f, mh = P0.mhf_f;
+    double R2c = P0.R2cut;
+    Kahan3 acc;
+    const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
+    for (int g = 0; g < ng; ++g) {
+        const uint4 e4 = __ldg(row + (size_t)g * A.np);
+        const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+        float4 pj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32 + (e[q] & kJMask));
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (MULTI) {
+                const PotParams& P = ps->p[ki][A.kind[e[q] & kJMask] & 3];
+                r2c = P.r2cut_f; l1 = P.lj1_f; l2 = P.lj2_f; mh = P.mhf_f; R2c = P.R2cut;
+            }
+            float dx, dy, dz;
+            pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            bool in = pair_in(A, i, e[q], r2, r2c, R2c, per);
+            float r2inv = __frcp_rn(fmaxf(r2, 1e-12f));
+            float r6inv = r2inv * r2inv * r2inv;
+            float pref = in ? mh * fmaf(l1, r6inv, -l2) * r6inv * r2inv : 0.f;
+            fx = fmaf(dx, pref, fx);
+            fy = fmaf(dy, pref, fy);
+            fz = fmaf(dz, pref, fz);
+        }
+        acc.add(0, fx);
+        acc.add(1, fy);
+        acc.add(2, fz);
+    }
+    A.gx[i] = acc.s[0];
+    A.gy[i] = acc.s[1];
+    A.gz[i] = acc.s[2];
+}
+
+__device__ __forceinline__ void embed32(const PotParams& P, float rho, float* F, float* dF,
+                                        DevStatus* st) {
+    float t = rho * P.inv_drh_f;
+    if (!(t >= 0.0f) || t >= (float)(P.Nrh1 - 1)) {
+        atomicOr(&st->flags, FLAG_TABLE);
+        t = fminf(fmaxf(t, 0.0f), (float)(P.Nrh1 - 1) - 1e-3f);
+    }
+    int nn = (int)t;
+    float u = t - (float)nn;
+    float4 c = __ldg(P.f_c + nn);
+    *F = cubic(c, u);
+    *dF = dcubic(c, u) * P.inv_drh_f;
+}
+
+template <bool MULTI>
+__device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
+    const float4 pi = A.pos32[i];
+    const int ki = MULTI ? (A.kind[i] & 3) : 0;
+    const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
+    const bool per = ps->periodic;
+    float s = 0.f, c = 0.f;
+    if (A.tag[i] != 0) {
+        const int ng = A.ncnt[i] >> 2;
+        const PotParams* P = &ps->p[ki][0];
+        float r2c = P->r2cut_f, idr = P->inv_dr_f;
+        double R2c = P->R2cut;
+        int Nr1 = P->Nr1;
+        const float4* tab = P->rho_c;
+        const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
+        for (int g = 0; g < ng; ++g) {
+            const uint4 e4 = __ldg(row + (size_t)g * A.np);
+            const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+            float4 pj[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32 + (e[q] & kJMask));
+            float part = 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                bool eam = true;
+                if (MULTI) {
+                    P = &ps->p[ki][A.kind[e[q] & kJMask] & 3];
+                    r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; tab = P->rho_c; R2c = P->R2cut;
+                    eam = P->type == 2;
+                }
+                float dx, dy, dz;
+                pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+                float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                bool in = eam && pair_in(A, i, e[q], r2, r2c, R2c, per);
+                float t = sqrtf(r2) * idr;
+                int nn = (int)t;
+                in = in && nn < Nr1;
+                nn = in ? nn : 0;
+                float u = t - (float)nn;
+                float v = in ? cubic(__ldg(tab + nn), u) : 0.f;
+                part += v;
+            }
+            ksum_add(s, c, part);
+        }
+    }
+    float rho = s;
+    float Fp0 = 0.f;
+    for (int b = 0; b < ps->nkinds; ++b) {
+        const PotParams& P = ps->p[ki][b];
+        float F = 0.f, dF = 0.f;
+        if (P.type == 2) embed32(P, rho, &F, &dF, A.st);
+        if (b == 0) Fp0 = dF;
+        if (MULTI) A.Fp32[(size_t)b * A.np + i] = dF;
+    }
+    A.pos32b[i] = make_float4(pi.x, pi.y, pi.z, Fp0);
+}
+
+template <bool MULTI>
+__device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
+    if (A.tag[i] == 0) return;
+    const float4 pi = A.pos32b[i];
+    const int ng = A.ncnt[i] >> 2;
+    const int ki = MULTI ? (A.kind[i] & 3) : 0;
+    const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
+    const bool per = ps->periodic;
+    const PotParams* P = &ps->p[ki][0];
+    float r2c = P->r2cut_f, idr = P->inv_dr_f;
+    double R2c = P->R2cut;
+    int Nr1 = P->Nr1;
+    const float4* rt = P->rho_c;
+    const float4* vt = P->v_c;
+    Kahan3 acc;
+    const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
+    for (int g = 0; g < ng; ++g) {
+        const uint4 e4 = __ldg(row + (size_t)g * A.np);
+        const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+        float4 pj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32b + (e[q] & kJMask));
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float Fpi = pi.w, Fpj = pj[q].w;
+            bool eam = true;
+            if (MULTI) {
+                uint32_t j = e[q] & kJMask;
+                int kj = A.kind[j] & 3;
+                P = &ps->p[ki][kj];
+                eam = P->type == 2;
+                r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; rt = P->rho_c; vt = P->v_c; R2c = P->R2cut;
+                Fpj = A.Fp32[(size_t)ki * A.np + j];
+                Fpi = A.Fp32[(size_t)kj * A.np + i];
+            }
+            float dx, dy, dz;
+            pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+            float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            bool in = eam && pair_in(A, i, e[q], r2, r2c, R2c, per);
+            float r = sqrtf(r2);
+            float t = r * idr;
+            int nn = (int)t;
+            in = in && nn < Nr1;
+            nn = in ? nn : 0;
+            float u = t - (float)nn;
+            float4 cr = __ldg(rt + nn);
+            float4 cv = __ldg(vt + nn);
+            float drho = dcubic(cr, u) * idr;
+            float V = cubic(cv, u);
+            float dV = dcubic(cv, u) * idr;
+            float rinv = __frcp_rn(fmaxf(r, 1e-6f));
+            float FF = fmaf(Fpi + Fpj, drho, (dV * r - V) * (rinv * rinv)) * rinv;
+            FF = in ? FF : 0.f;
+            fx = fmaf(FF, dx, fx);
+            fy = fmaf(FF, dy, fy);
+            fz = fmaf(FF, dz, fz);
+        }
+        acc.add(0, fx);
+        acc.add(1, fy);
+        acc.add(2, fz);
+    }
+    A.gx[i] = acc.s[0];
+    A.gy[i] = acc.s[1];
+    A.gz[i] = acc.s[2];
+}
+
+}  // namespace mdg
+
+struct mdg_system;
+
+namespace mdg {
+// Argument block of a system's force stages (forces.cu).
+FArgs force_args(mdg_system* sys);
+}  // namespace mdg

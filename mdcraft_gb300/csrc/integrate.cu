@@ -16,85 +16,18 @@
 #include <cuda_runtime.h>
 
 #include "mdg_host.h"
+#include "integrate_dev.cuh"
 
 namespace mdg {
 
-struct IArgs {
-    int n;
-    double dt;
-    double *rx, *ry, *rz, *vx, *vy, *vz;
-    const double *fx, *fy, *fz;
-    const float *gx, *gy, *gz;
-    const double* m;
-    const uint16_t* tag;
-    double* rcut;
-    const double* rns;
-    const uint32_t* uid;
-    const double *r0x, *r0y, *r0z, *saved_rcut, *saved_rns;
-    const uint32_t* saved_uid;
-    uint8_t* bc;
-    double pot_rcut;  // < 0: leave rcut (Multi::prepare_one does not set it)
-    int periodic_boundary;
-    double bmin[3], bmax[3], L[3];
-    int periodic[3];
-    // mixed
-    const double *Rx, *Ry, *Rz;
-    float4* pos32;
-    const float4* o0;
-    const float* trig;
-    DevStatus* st;
-};
 
-__device__ __forceinline__ void flag_need(bool need, DevStatus* st) {
-    unsigned b = __ballot_sync(__activemask(), need);
-    if (b && (threadIdx.x & 31) == (__ffs(b) - 1)) atomicOr(&st->need_rebuild, 1u);
-}
 
-// VerletList::decide per atom (verlet-list.cxx:135-154), exact FP64.
-__device__ __forceinline__ bool decide_one(const IArgs& A, int i, double x, double y, double z) {
-    if (A.uid[i] != A.saved_uid[i] || A.rcut[i] != A.saved_rcut[i] || A.rns[i] != A.saved_rns[i]) return true;
-    double skin = dsub(A.saved_rns[i], A.saved_rcut[i]);
-    if (skin <= 0.0) return true;
-    double dx = shortest1(dsub(x, A.r0x[i]), A.L[0], A.periodic[0]);
-    double dy = shortest1(dsub(y, A.r0y[i]), A.L[1], A.periodic[1]);
-    double dz = shortest1(dsub(z, A.r0z[i]), A.L[2], A.periodic[2]);
-    double trigger2 = dmul(dmul(0.25, skin), skin);
-    return sq3_exact(dx, dy, dz) > trigger2;
-}
 
 // step_one_coords + prepare + decide (FP64 form). drift = 0 runs only the
 // prepare + decide part (Pair::prepare called on its own).
 __global__ void k_drift64(IArgs A, int drift, int check) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool need = false;
-    if (i < A.n) {
-        double r[3] = {A.rx[i], A.ry[i], A.rz[i]};
-        uint16_t tg = A.tag[i];
-        if (drift && tg != 0) {
-            double f[3] = {A.fx[i], A.fy[i], A.fz[i]};
-            double v[3] = {A.vx[i], A.vy[i], A.vz[i]};
-            double m = A.m[i];
-            for (int k = 0; k < 3; ++k) {
-                double a = __ddiv_rn(f[k], m);
-                v[k] = dadd(v[k], dmul(dmul(a, A.dt), 0.5));
-                r[k] = dadd(r[k], dmul(v[k], A.dt));
-            }
-            A.rx[i] = r[0]; A.ry[i] = r[1]; A.rz[i] = r[2];
-            A.vx[i] = v[0]; A.vy[i] = v[1]; A.vz[i] = v[2];
-        }
-        if (tg != 0 && A.pot_rcut >= 0.0) A.rcut[i] = A.pot_rcut;
-        uint8_t bc = 0;
-        if (A.periodic_boundary && tg != 0) {
-            double rn = A.rns[i];
-            for (int a = 0; a < 3; ++a) {
-                if (!A.periodic[a]) continue;
-                double d0 = fabs(dsub(r[a], A.bmin[a])), d1 = fabs(dsub(r[a], A.bmax[a]));
-                if ((d0 < d1 ? d0 : d1) < rn) bc = 1;
-            }
-        }
-        A.bc[i] = bc;
-        if (check) need = decide_one(A, i, r[0], r[1], r[2]);
-    }
+    bool need = i < A.n ? drift64_one(A, i, drift, check) : false;
     if (check) flag_need(need, A.st);
 }
 
@@ -122,47 +55,20 @@ __global__ void k_kick64(IArgs A) {
 // Mixed form: kick + drift, cell-offset refresh, half-skin test.
 __global__ void k_drift_mixed(IArgs A) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool need = false;
-    if (i < A.n) {
-        double r[3] = {A.rx[i], A.ry[i], A.rz[i]};
-        if (A.tag[i] != 0) {
-            float hm = (0.5f * (float)A.dt) * __frcp_rn((float)A.m[i]);
-            float g[3] = {A.gx[i], A.gy[i], A.gz[i]};
-            double* v[3] = {A.vx, A.vy, A.vz};
-            for (int k = 0; k < 3; ++k) {
-                double vk = v[k][i] + (double)(g[k] * hm);
-                v[k][i] = vk;
-                r[k] = fma(vk, A.dt, r[k]);
-            }
-            A.rx[i] = r[0]; A.ry[i] = r[1]; A.rz[i] = r[2];
-        }
-        float o[3] = {(float)(r[0] - A.Rx[i]), (float)(r[1] - A.Ry[i]), (float)(r[2] - A.Rz[i])};
-        A.pos32[i] = make_float4(o[0], o[1], o[2], 0.0f);
-        float4 q = A.o0[i];
-        float dx = o[0] - q.x, dy = o[1] - q.y, dz = o[2] - q.z;
-        float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        need = d2 > A.trig[i];
-    }
+    bool need = i < A.n ? drift_mixed_one(A, i) : false;
     flag_need(need, A.st);
 }
 
 __global__ void k_kick_mixed(IArgs A) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= A.n || A.tag[i] == 0) return;
-    float hm = (0.5f * (float)A.dt) * __frcp_rn((float)A.m[i]);
-    A.vx[i] += (double)(A.gx[i] * hm);
-    A.vy[i] += (double)(A.gy[i] * hm);
-    A.vz[i] += (double)(A.gz[i] * hm);
+    if (i < A.n) kick_mixed_one(A, i);
 }
 
-// Half-skin threshold per atom for the mixed test: (skin/2)^2 shrunk by
-// 1e-6 so that FP32 rounding can only trigger a rebuild early.
+// Half-skin threshold per atom for the mixed test (trig_one).
 __global__ void k_trig(int n, const double* __restrict__ saved_rns, const double* __restrict__ saved_rcut,
                        float* __restrict__ trig) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double skin = saved_rns[i] - saved_rcut[i];
-    trig[i] = skin <= 0.0 ? -1.0f : (float)(0.25 * skin * skin * (1.0 - 1e-6));
+    if (i < n) trig_one(i, saved_rns, saved_rcut, trig);
 }
 
 // Refresh of the FP32 offsets from FP64 positions (after uploads).
@@ -281,7 +187,7 @@ __global__ void k_measure_final(const double* __restrict__ part, int nparts, int
 // ---------------------------------------------------------------------------
 static inline int nblk(size_t n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
-static IArgs make_iargs(mdg_system* sys, double dt) {
+IArgs integrator_args(mdg_system* sys, double dt) {
     IArgs A;
     memset(&A, 0, sizeof(A));
     int c = sys->cur;
@@ -320,7 +226,7 @@ int launch_drift(mdg_system* sys, double dt, int precision, double pot_rcut, int
                  int drift, int check) {
     if (sys->n == 0) return MDG_OK;
     mdg_ctx* ctx = sys->ctx;
-    IArgs A = make_iargs(sys, dt);
+    IArgs A = integrator_args(sys, dt);
     A.pot_rcut = pot_rcut;
     A.periodic_boundary = periodic_boundary;
     if (precision == MDG_PREC_MIXED && drift) k_drift_mixed<<<nblk(sys->n), kBlock, 0, ctx->stream>>>(A);
@@ -331,7 +237,7 @@ int launch_drift(mdg_system* sys, double dt, int precision, double pot_rcut, int
 
 int launch_decide(mdg_system* sys) {
     if (sys->n == 0) return MDG_OK;
-    IArgs A = make_iargs(sys, 0.0);
+    IArgs A = integrator_args(sys, 0.0);
     k_decide<<<nblk(sys->n), kBlock, 0, sys->ctx->stream>>>(A);
     MDG_LAUNCHED(sys->ctx);
     return MDG_OK;
@@ -340,7 +246,7 @@ int launch_decide(mdg_system* sys) {
 int launch_kick(mdg_system* sys, double dt, int precision) {
     if (sys->n == 0) return MDG_OK;
     mdg_ctx* ctx = sys->ctx;
-    IArgs A = make_iargs(sys, dt);
+    IArgs A = integrator_args(sys, dt);
     if (precision == MDG_PREC_MIXED) k_kick_mixed<<<nblk(sys->n), kBlock, 0, ctx->stream>>>(A);
     else k_kick64<<<nblk(sys->n), kBlock, 0, ctx->stream>>>(A);
     MDG_LAUNCHED(ctx);

@@ -152,6 +152,7 @@ struct mdg_system {
     int run_step_kernels = 0;                // kernels per step / per rebuild in the graph
     int run_rebuild_kernels = 0;
     double graph_build_s = 0.0;              // host seconds spent building run graphs
+    int solo_threads = 0;                    // > 0: run loops as one block of this many threads (solo.cu)
 
     // device status + grid
     mdg::DevStatus* dstat = nullptr;
@@ -177,6 +178,7 @@ struct mdg_system {
     void* xfer = nullptr;
     size_t xfer_bytes = 0;
     size_t dev_bytes = 0;  // device bytes held now
+    int lazy_init = 0;     // buffers cleared by their first kernel (fused loop), not on the stream
 
     double* cur64(int f) { return f64[f][cur]; }
     float* cur32(int c) { return f32[c][cur]; }
@@ -200,6 +202,7 @@ struct SystemMemory {
     unsigned long long* hcounter = nullptr;
     void* pin = nullptr;
     size_t pin_bytes = 0;
+    int lazy_init = 0;  // leave clearing the buffers to the system's first kernel
 };
 int system_create(mdg_ctx* ctx, const mdg_domain* domain, size_t n, const SystemMemory* mem, mdg_system** out);
 void system_release(mdg_system* sys);
@@ -213,7 +216,34 @@ int run_async_end(mdg_solver* s, mdg_system* sys, double dt, int* relaunched);
 int request_begin(mdg_solver* s, mdg_system* sys, const mdg_atom* atoms, double dt, long steps,
                   DevStatus* first_status);
 int download_atoms_enqueue(mdg_system* sys, size_t n);
+// A solver's potential parameters on the device (valid after a check on a
+// system of that device) and, optionally, their host copy.
+const PotSet* solver_potsets(mdg_solver* s, PotSet* host);
 int nlist_capacity_host(mdg_system* sys, const mdg_atom* atoms, size_t n, int half);
+// The fused one-block driver loop (solo.cu): small mixed-precision systems,
+// one request per block of a persistent kernel fed through a queue.
+constexpr int kSoloRing = 4096;
+struct SoloQueue {              // host-mapped
+    volatile uint32_t tail;     // entries published
+    volatile uint32_t stop;     // 1: blocks exit when they find no entry
+    uint32_t pad[14];
+    int ring[kSoloRing];        // argument-record index of each entry
+};
+int solo_eligible(const mdg_solver* s, const mdg_system* sys);
+size_t solo_args_bytes();
+size_t solo_out_bytes();
+// Fills the argument record at `args` (host-mapped) of a fresh system's
+// whole request: its block clears the system's buffers, loads the atoms from
+// atoms_in_dev, builds the first list, computes the initial forces and runs
+// `steps` steps; it writes the result atoms to atoms_out_dev and its
+// completion record (done = seq) to out_dev (device views of host-mapped
+// memory; in and out may be the same buffer).
+void solo_fill(void* args, mdg_system* sys, const PotSet* dps, int any_eam, double pot_rcut, int periodic,
+               double dt, long steps, const void* atoms_in_dev, void* out_dev, void* atoms_out_dev, uint32_t seq);
+int solo_out_read(const void* out_host, uint32_t* done, unsigned long long* left, DevStatus* st);
+int solo_persistent_launch(cudaStream_t stream, int threads, int blocks, const void* desc_dev, SoloQueue* q_dev,
+                           uint32_t* head, int idle_limit);
+int solo_blocks_per_sm(int threads, int* blocks);
 int nlist_build(mdg_system* sys, double kbuf, int half);
 int nlist_capacity(mdg_system* sys, int half);
 int nlist_enqueue(mdg_system* sys);

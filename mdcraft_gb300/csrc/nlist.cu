@@ -18,6 +18,7 @@
 #include <cstring>
 
 #include "mdg_host.h"
+#include "nlist_dev.cuh"
 
 namespace mdg {
 
@@ -25,11 +26,6 @@ namespace mdg {
 // bounds + wrap (Domain::fit_in_period, domain.cxx:41-47; Grid::find_bounds,
 // grid.cxx:209-243)
 // ---------------------------------------------------------------------------
-struct DomainDev {
-    double bmin[3], bmax[3], size[3];
-    int periodic[3];
-    int dim;
-};
 
 __global__ void k_wrap_bounds(int n, double* __restrict__ rx, double* __restrict__ ry,
                               double* __restrict__ rz, const double* __restrict__ rns,
@@ -38,17 +34,12 @@ __global__ void k_wrap_bounds(int n, double* __restrict__ rx, double* __restrict
     double lo[3] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308};
     double hi[3] = {-1.7976931348623157e308, -1.7976931348623157e308, -1.7976931348623157e308};
     double mr = 0.0;
-    double* r[3] = {rx, ry, rz};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double v[3];
+        wrap_one(d, rx, ry, rz, i, v);
         for (int a = 0; a < 3; ++a) {
-            double v = r[a][i];
-            if (d.periodic[a]) {
-                double w = v < d.bmin[a] ? dadd(v, d.size[a]) : v > d.bmax[a] ? dsub(v, d.size[a]) : v;
-                if (w != v) r[a][i] = w;
-                v = w;
-            }
-            lo[a] = fmin(lo[a], v);
-            hi[a] = fmax(hi[a], v);
+            lo[a] = fmin(lo[a], v[a]);
+            hi[a] = fmax(hi[a], v[a]);
         }
         double q = rns[i];
         mr = mr < q ? q : mr;
@@ -68,64 +59,6 @@ __global__ void k_wrap_bounds(int n, double* __restrict__ rx, double* __restrict
     if (t < 7) part[blockIdx.x * 8 + t] = sh[t][0];
 }
 
-// Grid::build (grid.cxx:43-95) from the reduced bounds and the largest rns;
-// shared by the device rebuild and the host-side capacity sizing, so both
-// get the same parameters bit for bit.
-__host__ __device__ void grid_from_bounds(const DomainDev& d, const double lo_in[3], const double hi_in[3],
-                                          double cell, GridParams& g) {
-    memset(&g, 0, sizeof(g));
-    g.dim = d.dim;
-    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    for (int i = 0; i < d.dim; ++i) {
-        lo[i] = lo_in[i];
-        hi[i] = hi_in[i];
-    }
-    g.max_rns = cell;
-    for (int i = 0; i < 3; ++i) {
-        g.bmin[i] = d.bmin[i];
-        g.bmax[i] = d.bmax[i];
-        g.size[i] = d.size[i];
-        g.periodic[i] = d.periodic[i];
-        g.dom_n[i] = 1;
-        g.cs[i] = d.size[i];
-    }
-    if (!(cell > 0.0)) {
-        g.empty = -1;
-        return;
-    }
-    for (int i = 0; i < d.dim; ++i) {
-        double q = floor(d.size[i] / cell);
-        int c = q > 1.0e9 ? 1000000000 : (int)q;
-        g.dom_n[i] = c > 1 ? c : 1;
-    }
-    for (int i = 0; i < d.dim; ++i) g.cs[i] = d.size[i] / (double)g.dom_n[i];
-    int up[3] = {0, 0, 0};
-    for (int i = 0; i < d.dim; ++i) {
-        g.offset[i] = (int)floor((lo[i] - d.bmin[i]) / g.cs[i]);
-        up[i] = (int)floor((hi[i] - d.bmin[i]) / g.cs[i]);
-        int u = up[i] + 1;
-        up[i] = u < g.dom_n[i] ? u : g.dom_n[i];
-    }
-    for (int i = 0; i < 3; ++i) g.num[i] = 1;
-    for (int i = 0; i < d.dim; ++i) g.num[i] = up[i] - g.offset[i];
-    g.small_box = 0;
-    for (int i = 0; i < 3; ++i) {
-        g.gmin[i] = d.bmin[i];
-        if (i < d.dim) g.gmin[i] = d.bmin[i] + g.cs[i] * g.offset[i];
-        g.bricks[i] = (g.num[i] + 3) / 4;
-        g.csf[i] = (float)g.cs[i];
-        g.Lf[i] = (float)d.size[i];
-        if (d.periodic[i] && i < d.dim &&
-            (g.dom_n[i] <= 3 || g.offset[i] != 0 || g.num[i] != g.dom_n[i]))
-            g.small_box = 1;
-        if (g.num[i] < 1 || g.num[i] > 1023) g.empty = -2;
-    }
-    long long nc = (long long)g.num[0] * g.num[1] * g.num[2];
-    long long nb = 64LL * g.bricks[0] * g.bricks[1] * g.bricks[2];
-    if (nb > (1LL << 30)) g.empty = -2;
-    g.ncells = (int)nc;
-    g.nbins = (int)nb;
-}
 
 __global__ void k_grid_finalize(const double* __restrict__ part, int nparts, DomainDev d,
                                 GridParams* __restrict__ out, long long bin_cap, DevStatus* st) {
@@ -168,18 +101,6 @@ __global__ void k_grid_finalize(const double* __restrict__ part, int nparts, Dom
 // ---------------------------------------------------------------------------
 // binning: Grid::local_index3D + cell_index (grid.cxx:107-136) -> bin keys
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void local_cell(const GridParams& g, double x, double y, double z,
-                                           int c[3], bool& clamped) {
-    double r[3] = {x, y, z};
-    clamped = false;
-    for (int a = 0; a < 3; ++a) {
-        int v = 0;
-        if (a < g.dim) v = (int)floor(__ddiv_rn(dsub(r[a], g.bmin[a]), g.cs[a])) - g.offset[a];
-        if (v < 0) { v = 0; clamped = true; }
-        if (v >= g.num[a]) { v = g.num[a] - 1; clamped = true; }
-        c[a] = v;
-    }
-}
 
 __global__ void k_bin_count(int n, const double* __restrict__ rx, const double* __restrict__ ry,
                             const double* __restrict__ rz, const GridParams* __restrict__ gp,
@@ -188,16 +109,7 @@ __global__ void k_bin_count(int n, const double* __restrict__ rx, const double* 
     const GridParams g = *gp;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || g.empty) return;
-    int c[3];
-    bool cl;
-    local_cell(g, rx[i], ry[i], rz[i], c, cl);
-    if (cl) {
-        atomicOr(&st->flags, FLAG_RANGE);
-        atomicOr(&st->build_flags, FLAG_RANGE);
-    }
-    uint32_t k = (uint32_t)bin_key(g, c[0], c[1], c[2]);
-    key[i] = k;
-    rank[i] = atomicAdd(&bin_count[k], 1u);
+    bin_count_one(g, i, rx, ry, rz, key, rank, bin_count, st);
 }
 
 // Exclusive scan of nb uint32 counts into start[0..nb] (start[nb] = total),
@@ -205,30 +117,6 @@ __global__ void k_bin_count(int n, const double* __restrict__ rx, const double* 
 // then per-block scans with offsets.
 constexpr int kScanT = 1024, kScanItems = 4;
 
-__device__ uint32_t block_excl_scan(uint32_t v, uint32_t* sh, uint32_t* total) {
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) sh[w] = x;
-    __syncthreads();
-    if (w == 0) {
-        uint32_t s = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0u;
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-            if (lane >= o) s += y;
-        }
-        sh[lane] = s;
-    }
-    __syncthreads();
-    uint32_t base = w > 0 ? sh[w - 1] : 0u;
-    uint32_t tot = sh[(blockDim.x >> 5) - 1];
-    __syncthreads();
-    if (total) *total = tot;
-    return base + x - v;
-}
 
 // Number of bins of the current rebuild (0 when the grid is invalid).
 __device__ __forceinline__ int live_bins(const GridParams* gp) { return gp->empty ? 0 : gp->nbins; }
@@ -299,25 +187,10 @@ __global__ void k_bin_sort(const GridParams* __restrict__ gp, const uint32_t* __
                            uint32_t* __restrict__ src, const uint32_t* __restrict__ orig) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= live_bins(gp)) return;
-    uint32_t s = start[b], e = start[b + 1];
-    for (uint32_t k = s + 1; k < e; ++k) {
-        uint32_t v = src[k];
-        uint32_t ov = orig[v];
-        uint32_t m = k;
-        while (m > s && orig[src[m - 1]] > ov) {
-            src[m] = src[m - 1];
-            --m;
-        }
-        src[m] = v;
-    }
+    bin_sort_one(b, start, src, orig);
 }
 
 // Permutation of the per-atom fields: dst[k] = src_field[src[k]].
-template <int NF, typename T>
-struct GatherSet {
-    const T* in[NF];
-    T* out[NF];
-};
 
 template <int NF, typename T>
 __global__ void k_gather(int n, const uint32_t* __restrict__ src, GatherSet<NF, T> gs,
@@ -348,59 +221,13 @@ __global__ void k_cells(int n, const double* __restrict__ rx, const double* __re
     const GridParams g = *gp;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || g.empty) return;
-    double r[3] = {rx[i], ry[i], rz[i]};
-    int c[3];
-    bool cl;
-    local_cell(g, r[0], r[1], r[2], c, cl);
-    cellp[i] = pack_cell(c[0], c[1], c[2]);
-    double R[3];
-    float o[3];
-    bool outlier = cl;
-    for (int a = 0; a < 3; ++a) {
-        R[a] = g.gmin[a] + ((double)c[a] + 0.5) * g.cs[a];
-        if (a >= g.dim) R[a] = r[a];
-        o[a] = (float)(r[a] - R[a]);
-        if (fabsf(o[a]) > 0.75f * g.csf[a] && a < g.dim) outlier = true;
-    }
-    Rx[i] = R[0];
-    Ry[i] = R[1];
-    Rz[i] = R[2];
-    float4 p = make_float4(o[0], o[1], o[2], 0.0f);
-    pos32[i] = p;
-    o0[i] = make_float4(o[0], o[1], o[2], outlier ? 1.0f : 0.0f);
-    slot_of[orig[i]] = (uint32_t)i;
+    cells_one(g, i, rx, ry, rz, cellp, Rx, Ry, Rz, pos32, o0, orig, slot_of);
 }
 
 // ---------------------------------------------------------------------------
 // Verlet list: one warp per cell, lanes over the cell's atoms
 // ---------------------------------------------------------------------------
-struct NbArgs {
-    int n, np, K, half;
-    const double *rx, *ry, *rz, *rns, *rcut;
-    const uint32_t *orig, *uid, *cellp, *bin_start;
-    const float4* o0;
-    uint32_t *nbr, *ncnt;
-    double *r0x, *r0y, *r0z, *saved_rcut, *saved_rns;
-    uint32_t* saved_uid;
-    DevStatus* st;
-};
 
-// VerletList::are_neibs (verlet-list.cxx:373-400), FP64 without contraction.
-__device__ __forceinline__ bool are_neibs_exact(const GridParams& g, double xa, double ya, double za,
-                                                double ra, double xb, double yb, double zb, double rb,
-                                                const bool edge[3]) {
-    double dd = ra < rb ? rb : ra;
-    double d2 = dmul(dd, dd);
-    double drx = dsub(xa, xb), dry = dsub(ya, yb), drz = dsub(za, zb);
-    double xs = g.size[0], ys = g.size[1], zs = g.size[2];
-    if (edge[0] && g.periodic[0] && (2 * drx < -xs)) drx = dadd(drx, xs);
-    if (edge[0] && g.periodic[0] && (2 * drx > xs)) drx = dsub(drx, xs);
-    if (edge[1] && g.periodic[1] && (2 * dry < -ys)) dry = dadd(dry, ys);
-    if (edge[1] && g.periodic[1] && (2 * dry > ys)) dry = dsub(dry, ys);
-    if (edge[2] && g.periodic[2] && (2 * drz < -zs)) drz = dadd(drz, zs);
-    if (edge[2] && g.periodic[2] && (2 * drz > zs)) drz = dsub(drz, zs);
-    return sq3_exact(drx, dry, drz) <= d2;
-}
 
 __global__ void __launch_bounds__(kBlock) k_nbuild(NbArgs A, const GridParams* __restrict__ gp) {
     __shared__ GridParams g;
@@ -409,121 +236,7 @@ __global__ void __launch_bounds__(kBlock) k_nbuild(NbArgs A, const GridParams* _
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (g.empty || warp >= g.nbins) return;
-    // prefilter band: rns^2 (1 -/+ 1e-5), valid when every atom has the same rns
-    const float lo2 = (float)(g.max_rns * g.max_rns * (1.0 - 1e-5));
-    const float hi2 = (float)(g.max_rns * g.max_rns * (1.0 + 1e-5));
-    const bool uniform_rns = A.st->nonuniform == 0;
-    uint32_t s0 = A.bin_start[warp], s1 = A.bin_start[warp + 1];
-    if (s0 == s1) return;
-    int cx, cy, cz;
-    unpack_cell(A.cellp[s0], cx, cy, cz);
-    int gc[3] = {cx + g.offset[0], cy + g.offset[1], cz + g.offset[2]};
-    if (g.dim < 3) gc[2] = 0;
-    if (g.dim < 2) gc[1] = 0;
-    bool edge[3] = {false, false, false};
-    for (int a = 0; a < g.dim; ++a) edge[a] = gc[a] == 0 || gc[a] == g.num[a] - 1;
-    const bool prefilter = uniform_rns && !g.small_box;
-
-    for (uint32_t base = s0; base < s1; base += 32) {
-        uint32_t i = base + lane;
-        bool active = i < s1;
-        double xi = 0, yi = 0, zi = 0, rni = 0;
-        float4 oi = make_float4(0, 0, 0, 0);
-        uint32_t origi = 0;
-        if (active) {
-            xi = A.rx[i]; yi = A.ry[i]; zi = A.rz[i]; rni = A.rns[i];
-            oi = A.o0[i];
-            origi = A.orig[i];
-        }
-        int cnt = 0;
-        for (int x = -1; x <= 1; ++x) {
-            if (g.periodic[0]) {
-                if (g.dom_n[0] == 1 && x != 0) continue;
-                if (g.dom_n[0] == 2 && x == 1) continue;
-            }
-            for (int y = -1; y <= 1; ++y) {
-                if (g.periodic[1]) {
-                    if (g.dom_n[1] == 1 && y != 0) continue;
-                    if (g.dom_n[1] == 2 && y == 1) continue;
-                }
-                for (int z = -1; z <= 1; ++z) {
-                    if (g.periodic[2]) {
-                        if (g.dom_n[2] == 1 && z != 0) continue;
-                        if (g.dom_n[2] == 2 && z == 1) continue;
-                    }
-                    int nb[3] = {gc[0] + x, gc[1] + y, gc[2] + z};
-                    for (int a = 0; a < 3; ++a)
-                        if (g.periodic[a]) nb[a] = (nb[a] + g.dom_n[a]) % g.dom_n[a];
-                    int lc[3] = {nb[0] - g.offset[0], nb[1] - g.offset[1], nb[2] - g.offset[2]};
-                    if (lc[0] < 0 || lc[0] >= g.num[0] || lc[1] < 0 || lc[1] >= g.num[1] ||
-                        lc[2] < 0 || lc[2] >= g.num[2])
-                        continue;
-                    int bk = bin_key(g, lc[0], lc[1], lc[2]);
-                    uint32_t j0 = A.bin_start[bk], j1 = A.bin_start[bk + 1];
-                    // image of the neighbour cell relative to this cell
-                    int dl[3] = {x, y, z};
-                    float sh[3] = {(float)x * g.csf[0], (float)y * g.csf[1], (float)z * g.csf[2]};
-                    for (uint32_t j = j0; j < j1; ++j) {
-                        float4 oj = A.o0[j];
-                        if (!active || j == i) continue;
-                        if (A.half && A.orig[j] < origi) continue;
-                        float dx = oi.x - oj.x - sh[0];
-                        float dy = oi.y - oj.y - sh[1];
-                        float dz = oi.z - oj.z - sh[2];
-                        float d2 = dx * dx + dy * dy + dz * dz;
-                        bool acc;
-                        if (prefilter && oi.w == 0.0f && oj.w == 0.0f && d2 < lo2) {
-                            acc = true;
-                        } else if (prefilter && oi.w == 0.0f && oj.w == 0.0f && d2 > hi2) {
-                            acc = false;
-                        } else {
-                            acc = are_neibs_exact(g, xi, yi, zi, rni, A.rx[j], A.ry[j], A.rz[j],
-                                                  A.rns[j], edge);
-                        }
-                        if (!acc) continue;
-                        // periodic image code: minimum image of j seen from i
-                        uint32_t code = 0;
-                        for (int a = 0; a < 3; ++a) {
-                            int dlt = dl[a];
-                            if (g.periodic[a] && a < g.dim && g.dom_n[a] <= 3) {
-                                float dd = -(a == 0 ? dx : a == 1 ? dy : dz);
-                                float half = 0.5f * g.Lf[a];
-                                if (dd > half) dlt -= g.dom_n[a];
-                                else if (dd < -half) dlt += g.dom_n[a];
-                            }
-                            if (dlt < -1 || dlt > 1) {
-                                atomicOr(&A.st->flags, FLAG_IMAGE);
-                                dlt = dlt < -1 ? -1 : 1;
-                            }
-                            code |= (uint32_t)(dlt + 1) << (2 * a);
-                            // the image crossed a periodic face
-                            int own[3] = {cx, cy, cz};
-                            if (dlt != lc[a] - own[a]) code |= 1u << 6;
-                        }
-                        if (cnt < A.K) A.nbr[nidx(cnt, i, A.np)] = j | (code << kJBits);
-                        ++cnt;
-                    }
-                }
-            }
-        }
-        if (active) {
-            // pad to a multiple of four with self entries
-            int padded = (cnt + 3) & ~3;
-            for (int k = cnt; k < padded && k < A.K; ++k) A.nbr[nidx(k, i, A.np)] = i | kSelfCode;
-            A.ncnt[i] = padded < A.K ? padded : A.K;
-            if (cnt > A.K) {
-                atomicOr(&A.st->flags, FLAG_OVERFLOW);
-                atomicOr(&A.st->build_flags, FLAG_OVERFLOW);
-            }
-            atomicMax(&A.st->max_count, (uint32_t)cnt);
-            A.r0x[i] = xi;
-            A.r0y[i] = yi;
-            A.r0z[i] = zi;
-            A.saved_rcut[i] = A.rcut[i];
-            A.saved_rns[i] = rni;
-            A.saved_uid[i] = A.uid[i];
-        }
-    }
+    nbuild_bin(A, g, warp, lane, A.st->nonuniform == 0);
 }
 
 // VerletList::optimize_search_radius (verlet-list.cxx:72-92):
@@ -713,6 +426,69 @@ int size_from_grid(mdg_system* sys, const GridParams& g, int half) {
 // synchronisation: every size comes from the device grid parameters, and a
 // grid or list that outgrows the capacities raises FLAG_OVERFLOW in
 // build_flags (the kernels of an invalid grid return early).
+GatherAll gather_sets(const mdg_system* sys) {
+    const int c = sys->cur, alt = c ^ 1;
+    GatherAll G;
+    for (int f = 0; f < 12; ++f) {
+        G.a.in[f] = sys->f64[f][c];
+        G.a.out[f] = sys->f64[f][alt];
+        G.b.in[f] = sys->f64[12 + f][c];
+        G.b.out[f] = sys->f64[12 + f][alt];
+        G.a2.in[f] = G.a.out[f];
+        G.a2.out[f] = sys->f64[f][c];
+        G.b2.in[f] = G.b.out[f];
+        G.b2.out[f] = sys->f64[12 + f][c];
+    }
+    for (int f = 0; f < 3; ++f) {
+        G.fc.in[f] = sys->f32[f][c];
+        G.fc.out[f] = sys->f32[f][alt];
+        G.fc2.in[f] = G.fc.out[f];
+        G.fc2.out[f] = sys->f32[f][c];
+    }
+    for (int f = 0; f < 2; ++f) {
+        G.u.in[f] = sys->u32[f][c];
+        G.u.out[f] = sys->u32[f][alt];
+        G.u2.in[f] = G.u.out[f];
+        G.u2.out[f] = sys->u32[f][c];
+        G.h.in[f] = sys->u16[f][c];
+        G.h.out[f] = sys->u16[f][alt];
+        G.h2.in[f] = G.h.out[f];
+        G.h2.out[f] = sys->u16[f][c];
+    }
+    return G;
+}
+
+NbArgs nb_args(const mdg_system* sys) {
+    const int c = sys->cur;
+    NbArgs A;
+    A.n = (int)sys->n;
+    A.np = (int)sys->np;
+    A.K = sys->K;
+    A.half = sys->half;
+    A.rx = sys->f64[RX][c];
+    A.ry = sys->f64[RY][c];
+    A.rz = sys->f64[RZ][c];
+    A.rns = sys->f64[RNS][c];
+    A.rcut = sys->f64[RCUT][c];
+    A.orig = sys->u32[ORIG][c];
+    A.uid = sys->u32[UID][c];
+    A.cellp = sys->cellp;
+    A.bin_start = sys->bin_start;
+    A.o0 = sys->o0;
+    A.nbr = sys->nbr;
+    A.ncnt = sys->ncnt;
+    A.r0x = sys->r0[0];
+    A.r0y = sys->r0[1];
+    A.r0z = sys->r0[2];
+    A.saved_rcut = sys->saved_rcut;
+    A.saved_rns = sys->saved_rns;
+    A.saved_uid = sys->saved_uid;
+    A.st = sys->dstat;
+    return A;
+}
+
+DomainDev domain_of(const mdg_system* sys) { return domain_dev(sys); }
+
 int nlist_enqueue(mdg_system* sys) {
     mdg_ctx* ctx = sys->ctx;
     cudaStream_t st = ctx->stream;
@@ -750,36 +526,9 @@ int nlist_enqueue(mdg_system* sys) {
     MDG_LAUNCHED(ctx);
     // permute every per-atom field into the spare buffers, then copy back
     {
-        GatherSet<12, double> a, b, a2, b2;
-        for (int f = 0; f < 12; ++f) {
-            a.in[f] = sys->f64[f][c];
-            a.out[f] = sys->f64[f][alt];
-            b.in[f] = sys->f64[12 + f][c];
-            b.out[f] = sys->f64[12 + f][alt];
-            a2.in[f] = a.out[f];
-            a2.out[f] = sys->f64[f][c];
-            b2.in[f] = b.out[f];
-            b2.out[f] = sys->f64[12 + f][c];
-        }
-        GatherSet<3, float> fc, fc2;
-        for (int f = 0; f < 3; ++f) {
-            fc.in[f] = sys->f32[f][c];
-            fc.out[f] = sys->f32[f][alt];
-            fc2.in[f] = fc.out[f];
-            fc2.out[f] = sys->f32[f][c];
-        }
-        GatherSet<2, uint32_t> u, u2;
-        GatherSet<2, uint16_t> h, h2;
-        for (int f = 0; f < 2; ++f) {
-            u.in[f] = sys->u32[f][c];
-            u.out[f] = sys->u32[f][alt];
-            u2.in[f] = u.out[f];
-            u2.out[f] = sys->u32[f][c];
-            h.in[f] = sys->u16[f][c];
-            h.out[f] = sys->u16[f][alt];
-            h2.in[f] = h.out[f];
-            h2.out[f] = sys->u16[f][c];
-        }
+        GatherAll G = gather_sets(sys);
+        auto& a = G.a; auto& b = G.b; auto& a2 = G.a2; auto& b2 = G.b2;
+        auto& fc = G.fc; auto& fc2 = G.fc2; auto& u = G.u; auto& u2 = G.u2; auto& h = G.h; auto& h2 = G.h2;
         k_gather<12, double><<<nblk(n), kBlock, 0, st>>>(n, sys->src, a, sys->dgrid);
         MDG_LAUNCHED(ctx);
         k_gather<12, double><<<nblk(n), kBlock, 0, st>>>(n, sys->src, b, sys->dgrid);
@@ -805,30 +554,7 @@ int nlist_enqueue(mdg_system* sys) {
                                         sys->cellp, sys->Rc[0], sys->Rc[1], sys->Rc[2], sys->pos32, sys->o0,
                                         sys->u32[ORIG][c], sys->slot_of);
     MDG_LAUNCHED(ctx);
-    NbArgs A;
-    A.n = n;
-    A.np = (int)sys->np;
-    A.K = sys->K;
-    A.half = sys->half;
-    A.rx = sys->f64[RX][c];
-    A.ry = sys->f64[RY][c];
-    A.rz = sys->f64[RZ][c];
-    A.rns = sys->f64[RNS][c];
-    A.rcut = sys->f64[RCUT][c];
-    A.orig = sys->u32[ORIG][c];
-    A.uid = sys->u32[UID][c];
-    A.cellp = sys->cellp;
-    A.bin_start = sys->bin_start;
-    A.o0 = sys->o0;
-    A.nbr = sys->nbr;
-    A.ncnt = sys->ncnt;
-    A.r0x = sys->r0[0];
-    A.r0y = sys->r0[1];
-    A.r0z = sys->r0[2];
-    A.saved_rcut = sys->saved_rcut;
-    A.saved_rns = sys->saved_rns;
-    A.saved_uid = sys->saved_uid;
-    A.st = sys->dstat;
+    NbArgs A = nb_args(sys);
     size_t warps = sys->bin_cap;  // one warp per bin; the live bins come from the device grid
     k_nbuild<<<nblk(warps * 32), kBlock, 0, st>>>(A, sys->dgrid);
     MDG_LAUNCHED(ctx);

@@ -2,22 +2,36 @@
 //
 // The reference runs one system per process, its driver loop on the host
 // (test/python/solver/test-EAM.py:101-200); there is no serving layer to
-// mirror. Here a request is a whole driver loop (mdg_run: `steps` x
-// make_step + decide/update) over its own system. The server owns `slots`
-// streams. A slot takes the head of the FIFO when it is free and the
-// request's device footprint fits in the budget left by the running ones;
-// the request's system is created from the server's stream-ordered memory
-// pool, its atoms uploaded, its first list built, and its loop launched as
-// one graph (WHILE over steps, IF over rebuilds). Slots run concurrently,
-// so small systems that fill a few SMs each share the GPU. Completion is
-// found by polling one event per slot; the result is copied out and the
-// system's buffers go back to the pool behind the slot's last work, with no
-// device-wide synchronisation anywhere on the admit/retire path.
+// mirror. Here a request is a whole driver loop (update(-1), prepare,
+// stages, then `steps` x {make_step; if decide(): update(-1)}) over its own
+// atoms. Requests wait in a FIFO; each takes a slot when one is free and its
+// device footprint fits in the budget left by the running ones. Two ways to
+// run a request:
 //
-// Results are independent of the mix: every kernel reads and writes only its
-// own system's buffers, sums in a fixed order and uses no atomics across
-// systems, so a request gives the same bits alone or among others.
+// Block mode (mixed precision, one kind, up to 65536 atoms): the request's
+// whole run, set-up included, is one thread block of a persistent kernel
+// (solo.cu). The host allocates the system's buffers (stream-ordered, from
+// the server's pool), sizes its capacities from the atoms and fills the
+// block's argument record in host-mapped memory; once the allocations have
+// passed it publishes the record in a queue. Blocks of the persistent kernel
+// claim queue entries as they finish their previous request, so requests
+// that arrive while others run start as soon as a block is free. Each
+// block writes its result atoms and a completion record into host-mapped
+// memory; the host polls those and never waits for the device. Idle blocks
+// exit after a bounded wait; the host relaunches the kernel when work is
+// queued and no block is left.
+//
+// Graph mode (everything else, or when block mode is off): the request's
+// system gets the slot's own stream; set-up and the loop (one graph launch)
+// are enqueued there, completion is an event, and the result comes back by
+// an asynchronous copy.
+//
+// Results are independent of the mix: every block or kernel reads and
+// writes only its own system's buffers, sums in a fixed order and uses no
+// atomics across systems, so a request gives the same bits alone or among
+// others, in either mode.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -46,27 +60,43 @@ struct Request {
     mdg_request_info info{};
 };
 
-// A slot's request goes RUN (set-up + graph loop enqueued) -> COPY (result
-// gather + device-to-host copy enqueued) -> finished; each transition is
-// taken when the slot's event has passed, so the host never waits.
-enum SlotState { IDLE = 0, RUN = 1, COPY = 2 };
+// IDLE -> ALLOC (buffers requested) -> BLOCK (queued or running in a block)
+// -> finished, or IDLE -> RUN (graph loop enqueued) -> COPY (result copy
+// enqueued) -> finished.
+enum SlotState { IDLE = 0, RUN = 1, COPY = 2, BLOCK = 3, ALLOC = 4 };
 
 struct Slot {
-    mdg_ctx* ctx = nullptr;
+    mdg_ctx* ctx = nullptr;  // the slot's own stream (graph mode), made on first use
     cudaEvent_t ev = nullptr;
     Request* req = nullptr;
     mdg_system* sys = nullptr;
     SystemMemory mem;
     int state = IDLE;
-    int checked = 0;                  // request set up on the synchronous, checked path
+    int checked = 0;                    // request set up on the synchronous, checked path
     DevStatus* first_status = nullptr;  // device status after the first list build (pinned)
-    void* hblock = nullptr;  // pinned status words of the slot's systems
-    void* pin = nullptr;     // pinned transfer staging of the slot (max_atoms records)
+    void* hblock = nullptr;             // pinned status words of the slot's systems
+    void* pin = nullptr;                // host-mapped staging: input atoms, then results
+    void* pin_dev = nullptr;            // its device view
+    uint32_t seq = 0;                   // completion value of the slot's last block
+};
+
+// Slots whose buffers were requested in one pass, published together once
+// the allocation stream has passed `ev`.
+struct AllocGroup {
+    cudaEvent_t ev = nullptr;
+    std::vector<int> slots;
 };
 
 // Neighbour entries per atom the admission estimate assumes when the atoms
 // give no better figure: a dense liquid or solid at rns = rc + skin.
 constexpr int kDefaultNeighbours = 96;
+
+// Executable graphs of finished requests held before they are destroyed.
+constexpr size_t kMaxSpentGraphs = 16384;
+
+// Polls (about a microsecond apart) after which an idle block of the
+// persistent kernel exits.
+constexpr int kIdlePolls = 20000;
 
 }  // namespace
 
@@ -75,16 +105,36 @@ struct mdg_server {
     cudaMemPool_t pool = nullptr;
     size_t budget = 0, used = 0, peak = 0;
     size_t max_atoms = 0;
+    int block_threads = 0;
     std::vector<Slot> slots;
+    mdg_ctx* alloc_ctx = nullptr;  // block-mode systems: allocations and releases
+    mdg_ctx* feed_ctx = nullptr;   // the persistent kernel
+    cudaEvent_t feed_ev = nullptr; // recorded after each persistent launch
+    int feed_launched = 0;
+    int threads = 512, blocks = 0; // persistent kernel shape
+    SoloQueue* q = nullptr;        // host-mapped request queue
+    SoloQueue* q_dev = nullptr;
+    uint32_t* head = nullptr;      // next entry to claim (device)
+    uint32_t published = 0;
+    std::deque<AllocGroup> alloc_groups;
+    std::vector<cudaEvent_t> free_events;
     std::deque<Request*> queue;
     std::unordered_map<uint64_t, Request*> reqs;
     std::deque<uint64_t> finished;
     uint64_t next_id = 1;
     uint64_t admitted = 0;
     size_t nfinished = 0;
+    void* desc = nullptr;       // host-mapped argument records, one per slot
+    void* desc_dev = nullptr;
+    void* outs = nullptr;       // host-mapped completion records, one per slot
+    void* outs_dev = nullptr;
+    size_t desc_stride = 0, out_stride = 0;
+    uint64_t kernel_launches = 0;
     double admit_s = 0.0, graph_s = 0.0, retire_s = 0.0;
     uint64_t rechecked = 0;
     double graph_destroy_s = 0.0, release_s = 0.0, end_s = 0.0, download_s = 0.0;
+    std::vector<cudaGraphExec_t> spent_execs;
+    std::vector<cudaGraph_t> spent_graphs;
     Clock::time_point t0;
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
@@ -126,6 +176,21 @@ int neighbours_of(const mdg_domain& d, const mdg_atom* a, size_t n) {
     return (int)std::min<double>(std::ceil(k) + 1.0, (double)n);
 }
 
+size_t running_of(const mdg_server* sv) {
+    size_t k = 0;
+    for (const Slot& sl : sv->slots) k += sl.req ? 1 : 0;
+    return k;
+}
+
+void destroy_spent(mdg_server* sv) {
+    double t = sv->now();
+    for (cudaGraphExec_t e : sv->spent_execs) cudaGraphExecDestroy(e);
+    for (cudaGraph_t g : sv->spent_graphs) cudaGraphDestroy(g);
+    sv->spent_execs.clear();
+    sv->spent_graphs.clear();
+    sv->graph_destroy_s += sv->now() - t;
+}
+
 void finish(mdg_server* sv, Request* r, int status) {
     r->info.status = status;
     r->info.done = 1;
@@ -134,12 +199,16 @@ void finish(mdg_server* sv, Request* r, int status) {
     sv->nfinished++;
 }
 
+// Releases the slot's system (stream-ordered behind its last work) and the
+// request's charge.
 void retire(mdg_server* sv, Slot& sl) {
     if (sl.sys) {
         sv->graph_s += sl.sys->graph_build_s;
         double t = sv->now();
-        if (sl.sys->run_exec) cudaGraphExecDestroy(sl.sys->run_exec);
-        if (sl.sys->run_graph) cudaGraphDestroy(sl.sys->run_graph);
+        // destroying an executable graph waits for the whole device: keep
+        // them until no request runs (or the server goes)
+        if (sl.sys->run_exec) sv->spent_execs.push_back(sl.sys->run_exec);
+        if (sl.sys->run_graph) sv->spent_graphs.push_back(sl.sys->run_graph);
         sl.sys->run_exec = nullptr;
         sl.sys->run_graph = nullptr;
         double t1 = sv->now();
@@ -152,45 +221,61 @@ void retire(mdg_server* sv, Slot& sl) {
         sv->used -= std::min(sv->used, sl.req->footprint);
         sl.req = nullptr;
     }
-}
-
-// Sets up the request on the slot and enqueues its whole run; on failure
-// the request is finished with the error and the slot freed.
-void admit_impl(mdg_server* sv, Slot& sl, Request* r, int checked);
-
-void admit(mdg_server* sv, Slot& sl, Request* r, int checked = 0) {
-    double t = sv->now();
-    admit_impl(sv, sl, r, checked);
-    sv->admit_s += sv->now() - t;
+    sl.state = IDLE;
 }
 
 void fail(mdg_server* sv, Slot& sl, int rc) {
     Request* r = sl.req;
     r->info.footprint = r->footprint;
     retire(sv, sl);
-    sl.state = IDLE;
     finish(sv, r, rc);
 }
 
-void admit_impl(mdg_server* sv, Slot& sl, Request* r, int checked) {
-    if (!sl.req) {
-        sl.req = r;
-        r->info.t_admit = sv->now();
-        sv->admitted++;
-        sv->used += r->footprint;
+bool block_mode(const mdg_server* sv, const Request* r) {
+    if (sv->block_threads < 0) return false;
+    const mdg_solver* s = r->solver;
+    return r->precision == MDG_PREC_MIXED && !s->multi && s->nstages >= 1 && r->atoms.size() <= 65536 &&
+           r->atoms.size() > 0;
+}
+
+void charge(mdg_server* sv, Slot& sl, Request* r) {
+    sl.req = r;
+    r->info.t_admit = sv->now();
+    sv->admitted++;
+    sv->used += r->footprint;
+    sv->peak = std::max(sv->peak, sv->used);
+}
+
+void charge_actual(mdg_server* sv, Slot& sl, Request* r) {
+    // charge what the system holds once its capacities are sized
+    if (sl.sys && sl.sys->dev_bytes > r->footprint) {
+        sv->used += sl.sys->dev_bytes - r->footprint;
+        r->footprint = sl.sys->dev_bytes;
         sv->peak = std::max(sv->peak, sv->used);
     }
+}
+
+int ensure_slot_ctx(mdg_server* sv, Slot& sl) {
+    if (sl.ctx) return MDG_OK;
+    int rc = mdg_ctx_create(sv->device, &sl.ctx);
+    if (rc) return rc;
+    MDG_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
+    return MDG_OK;
+}
+
+// Graph mode: set-up and loop enqueued on the slot's stream (checked = the
+// driver's calls one by one, each list build verified and grown).
+void admit_graph(mdg_server* sv, Slot& sl, Request* r, int checked) {
+    double t0 = sv->now();
     sl.checked = checked;
     size_t n = r->atoms.size();
-    int rc = system_create(sl.ctx, &r->dom, n, &sl.mem, &sl.sys);
+    int rc = ensure_slot_ctx(sv, sl);
+    if (rc == MDG_OK) rc = system_create(sl.ctx, &r->dom, n, &sl.mem, &sl.sys);
     int prec_saved = r->solver->precision;
     r->solver->precision = r->precision;
     if (rc == MDG_OK && !checked) {
-        // everything enqueued, nothing waited for
         rc = request_begin(r->solver, sl.sys, r->atoms.data(), r->dt, r->steps, sl.first_status);
     } else if (rc == MDG_OK) {
-        // the checked path: the driver's calls one by one, each list build
-        // verified (and grown) before the run goes on
         rc = mdg_system_upload_atoms(sl.sys, r->atoms.data(), n);
         if (rc == MDG_OK) {
             rc = mdg_nlist_update(sl.sys, -1.0, 0);
@@ -202,15 +287,11 @@ void admit_impl(mdg_server* sv, Slot& sl, Request* r, int checked) {
     }
     r->solver->precision = prec_saved;
     if (rc == MDG_OK) {
-        // charge what the system holds once its capacities are sized
-        if (sl.sys->dev_bytes > r->footprint) {
-            sv->used += sl.sys->dev_bytes - r->footprint;
-            r->footprint = sl.sys->dev_bytes;
-            sv->peak = std::max(sv->peak, sv->used);
-        }
+        charge_actual(sv, sl, r);
         cudaError_t e = cudaEventRecord(sl.ev, sl.ctx->stream);
         if (e != cudaSuccess) rc = cuda_status(e, "slot event");
     }
+    sv->admit_s += sv->now() - t0;
     if (rc != MDG_OK) {
         fail(sv, sl, rc);
         return;
@@ -218,16 +299,53 @@ void admit_impl(mdg_server* sv, Slot& sl, Request* r, int checked) {
     sl.state = RUN;
 }
 
-// The slot's event has passed: advance its request one state.
-void advance_impl(mdg_server* sv, Slot& sl);
-
-void advance(mdg_server* sv, Slot& sl) {
-    double t = sv->now();
-    advance_impl(sv, sl);
-    sv->retire_s += sv->now() - t;
+// Block mode: the system's buffers requested on the allocation stream and
+// its argument record filled; published once the allocations have passed.
+bool admit_block(mdg_server* sv, Slot& sl, Request* r) {
+    double t0 = sv->now();
+    size_t k = &sl - sv->slots.data();
+    size_t n = r->atoms.size();
+    SystemMemory mem = sl.mem;
+    mem.lazy_init = 1;
+    int rc = system_create(sv->alloc_ctx, &r->dom, n, &mem, &sl.sys);
+    PotSet ps;
+    int prec_saved = r->solver->precision;
+    r->solver->precision = r->precision;
+    if (rc == MDG_OK) {
+        memcpy(sl.pin, r->atoms.data(), n * sizeof(mdg_atom));
+        rc = nlist_capacity_host(sl.sys, r->atoms.data(), n, 0);
+    }
+    if (rc == MDG_OK) {
+        sl.sys->grid = *sl.sys->hgrid;
+        rc = potset_build(r->solver, sl.sys, &ps);
+    }
+    if (rc == MDG_OK) {
+        const mdg_solver* s = r->solver;
+        double pot_rcut = s->multi ? -1.0 : s->pot[0][0]->rcut;
+        sl.seq++;
+        solo_fill((char*)sv->desc + k * sv->desc_stride, sl.sys, solver_potsets(r->solver, nullptr), ps.any_eam,
+                  pot_rcut, s->periodic, r->dt, r->steps, sl.pin_dev, (char*)sv->outs_dev + k * sv->out_stride,
+                  sl.pin_dev, sl.seq);
+        sl.sys->have_list = 1;
+        sl.sys->dirty = 0;
+        sl.sys->rebuilds = 1;
+        sl.sys->force_prec = MDG_PREC_MIXED;
+        charge_actual(sv, sl, r);
+    }
+    r->solver->precision = prec_saved;
+    sv->admit_s += sv->now() - t0;
+    if (rc != MDG_OK) {
+        fail(sv, sl, rc);
+        return false;
+    }
+    sl.state = ALLOC;
+    sl.checked = 0;
+    return true;
 }
 
-void advance_impl(mdg_server* sv, Slot& sl) {
+// Graph mode: the slot's event has passed; advance its request one state.
+void advance_graph(mdg_server* sv, Slot& sl) {
+    double t = sv->now();
     Request* r = sl.req;
     if (sl.state == RUN) {
         if (!sl.checked && (sl.first_status->build_flags & FLAG_OVERFLOW)) {
@@ -239,7 +357,8 @@ void advance_impl(mdg_server* sv, Slot& sl) {
                 sl.sys = nullptr;
             }
             sv->rechecked++;
-            admit_impl(sv, sl, r, 1);
+            sv->retire_s += sv->now() - t;
+            admit_graph(sv, sl, r, 1);
             return;
         }
         int prec_saved = r->solver->precision;
@@ -258,9 +377,10 @@ void advance_impl(mdg_server* sv, Slot& sl) {
         }
         if (rc != MDG_OK) {
             fail(sv, sl, rc);
-            return;
+        } else if (!relaunched) {
+            sl.state = COPY;
         }
-        if (!relaunched) sl.state = COPY;
+        sv->retire_s += sv->now() - t;
         return;
     }
     // COPY: the result is in the slot's pinned staging
@@ -268,51 +388,154 @@ void advance_impl(mdg_server* sv, Slot& sl) {
     r->info.rebuilds = sl.sys->rebuilds;
     r->info.footprint = r->footprint;
     retire(sv, sl);
-    sl.state = IDLE;
     finish(sv, r, MDG_OK);
+    sv->retire_s += sv->now() - t;
+}
+
+// Block mode: the slot's block has written its completion record.
+void advance_block(mdg_server* sv, Slot& sl, unsigned long long left, const DevStatus& st) {
+    double t = sv->now();
+    Request* r = sl.req;
+    if (st.pad[1] != 0 || left != 0) {
+        // a list outgrew the capacities sized on the host: the run is void;
+        // repeat it on the checked path (graph mode, capacities grown there)
+        if (sl.sys) {
+            system_release(sl.sys);
+            sl.sys = nullptr;
+        }
+        sv->rechecked++;
+        sv->retire_s += sv->now() - t;
+        admit_graph(sv, sl, r, 1);
+        return;
+    }
+    memcpy(r->atoms.data(), sl.pin, r->atoms.size() * sizeof(mdg_atom));
+    sl.sys->rebuilds += st.pad[0];
+    r->info.rebuilds = sl.sys->rebuilds;
+    r->info.footprint = r->footprint;
+    retire(sv, sl);
+    finish(sv, r, MDG_OK);
+    sv->retire_s += sv->now() - t;
 }
 
 int progress(mdg_server* sv) {
     MDG_CUDA(cudaSetDevice(sv->device));
-    for (Slot& sl : sv->slots) {
-        if (!sl.req) continue;
+    for (size_t k = 0; k < sv->slots.size(); ++k) {
+        Slot& sl = sv->slots[k];
+        if (!sl.req || sl.state == ALLOC) continue;
+        if (sl.state == BLOCK) {
+            uint32_t done = 0;
+            unsigned long long left = 0;
+            DevStatus st;
+            solo_out_read((char*)sv->outs + k * sv->out_stride, &done, &left, &st);
+            if (done == sl.seq) advance_block(sv, sl, left, st);
+            continue;
+        }
         cudaError_t e = cudaEventQuery(sl.ev);
         if (e == cudaErrorNotReady) continue;
         if (e != cudaSuccess) {
             fail(sv, sl, cuda_status(e, "request"));
             continue;
         }
-        advance(sv, sl);
+        advance_graph(sv, sl);
     }
+    // publish the records whose allocations have passed
+    while (!sv->alloc_groups.empty()) {
+        AllocGroup& ag = sv->alloc_groups.front();
+        cudaError_t e = cudaEventQuery(ag.ev);
+        if (e == cudaErrorNotReady) break;
+        if (e != cudaSuccess) return cuda_status(e, "allocation event");
+        for (int k : ag.slots) {
+            Slot& sl = sv->slots[k];
+            if (sl.state != ALLOC) continue;
+            sv->q->ring[sv->published % kSoloRing] = k;
+            sv->published++;
+            sl.state = BLOCK;
+        }
+        std::atomic_thread_fence(std::memory_order_seq_cst);  // records and ring before the tail
+        sv->q->tail = sv->published;
+        sv->free_events.push_back(ag.ev);
+        sv->alloc_groups.pop_front();
+    }
+    // spent graphs go when the device is idle (or too many are held)
+    if (!sv->spent_execs.empty() &&
+        ((sv->queue.empty() && running_of(sv) == 0) || sv->spent_execs.size() >= kMaxSpentGraphs))
+        destroy_spent(sv);
     // FIFO admission: the head waits for memory rather than being overtaken
+    AllocGroup group;
     for (Slot& sl : sv->slots) {
         if (sv->queue.empty()) break;
         if (sl.req) continue;
         Request* r = sv->queue.front();
         if (sv->used + r->footprint > sv->budget && sv->used > 0) break;
         sv->queue.pop_front();
-        admit(sv, sl, r);
+        charge(sv, sl, r);
+        if (!block_mode(sv, r)) {
+            admit_graph(sv, sl, r, 0);
+            continue;
+        }
+        if (admit_block(sv, sl, r)) group.slots.push_back((int)(&sl - sv->slots.data()));
+    }
+    if (!group.slots.empty()) {
+        if (sv->free_events.empty()) {
+            cudaEvent_t ev;
+            MDG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            sv->free_events.push_back(ev);
+        }
+        group.ev = sv->free_events.back();
+        sv->free_events.pop_back();
+        MDG_CUDA(cudaEventRecord(group.ev, sv->alloc_ctx->stream));
+        sv->alloc_groups.push_back(std::move(group));
+    }
+    // the persistent kernel: (re)launched when requests are queued and none
+    // of its blocks is left
+    bool queued = false;
+    for (const Slot& sl : sv->slots) queued = queued || (sl.req && sl.state == BLOCK);
+    if (queued) {
+        bool running = false;
+        if (sv->feed_launched) {
+            cudaError_t e = cudaEventQuery(sv->feed_ev);
+            if (e == cudaErrorNotReady) running = true;
+            else if (e != cudaSuccess) return cuda_status(e, "persistent kernel");
+        }
+        if (!running) {
+            int rc = solo_persistent_launch(sv->feed_ctx->stream, sv->threads, sv->blocks, sv->desc_dev, sv->q_dev,
+                                            sv->head, kIdlePolls);
+            if (rc) return rc;
+            MDG_CUDA(cudaEventRecord(sv->feed_ev, sv->feed_ctx->stream));
+            sv->feed_launched = 1;
+            sv->kernel_launches++;
+        }
     }
     return MDG_OK;
 }
 
-size_t running_of(const mdg_server* sv) {
-    size_t k = 0;
-    for (const Slot& sl : sv->slots) k += sl.req ? 1 : 0;
-    return k;
-}
-
 void server_free(mdg_server* sv) {
     cudaSetDevice(sv->device);
+    if (sv->q) sv->q->stop = 1;
+    if (sv->feed_ctx) cudaStreamSynchronize(sv->feed_ctx->stream);
+    if (sv->alloc_ctx) cudaStreamSynchronize(sv->alloc_ctx->stream);
     for (Slot& sl : sv->slots) {
         if (sl.ctx) cudaStreamSynchronize(sl.ctx->stream);
         if (sl.sys) retire(sv, sl);
+    }
+    if (sv->alloc_ctx) cudaStreamSynchronize(sv->alloc_ctx->stream);
+    for (Slot& sl : sv->slots) {
         if (sl.ev) cudaEventDestroy(sl.ev);
         if (sl.hblock) cudaFreeHost(sl.hblock);
         if (sl.pin) cudaFreeHost(sl.pin);
         if (sl.ctx) mdg_ctx_destroy(sl.ctx);
     }
+    for (AllocGroup& ag : sv->alloc_groups) sv->free_events.push_back(ag.ev);
+    for (cudaEvent_t e : sv->free_events) cudaEventDestroy(e);
+    if (sv->feed_ev) cudaEventDestroy(sv->feed_ev);
+    if (sv->alloc_ctx) mdg_ctx_destroy(sv->alloc_ctx);
+    if (sv->feed_ctx) mdg_ctx_destroy(sv->feed_ctx);
+    destroy_spent(sv);
     for (auto& kv : sv->reqs) delete kv.second;
+    if (sv->desc) cudaFreeHost(sv->desc);
+    if (sv->outs) cudaFreeHost(sv->outs);
+    if (sv->q) cudaFreeHost(sv->q);
+    if (sv->head) cudaFree(sv->head);
     if (sv->pool) cudaMemPoolDestroy(sv->pool);
     delete sv;
 }
@@ -324,7 +547,10 @@ extern "C" {
 size_t mdg_server_footprint(size_t n, int neighbours) { return footprint_of(n, neighbours); }
 
 int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out) {
-    if (!cfg || !out || cfg->slots < 1 || cfg->slots > 1024 || cfg->max_atoms == 0 || cfg->max_atoms >= kMaxAtoms)
+    if (!cfg || !out || cfg->slots < 1 || cfg->slots > kSoloRing || cfg->max_atoms == 0 || cfg->max_atoms >= kMaxAtoms)
+        return MDG_ERR_INVALID;
+    if (cfg->block_threads > 0 && cfg->block_threads != 256 && cfg->block_threads != 512 &&
+        cfg->block_threads != 1024)
         return MDG_ERR_INVALID;
     *out = nullptr;
     int count = 0;
@@ -338,6 +564,7 @@ int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out
     sv->device = device;
     sv->t0 = Clock::now();
     sv->max_atoms = cfg->max_atoms;
+    sv->block_threads = cfg->block_threads;
     size_t free_b = 0, total_b = 0;
     cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
     if (e != cudaSuccess) {
@@ -357,21 +584,56 @@ int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out
         uint64_t keep = ~0ull;
         e = cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
+    if (e == cudaSuccess) {
+        // memory freed on one stream is not handed to another stream before
+        // the free has completed (no dependency between streams)
+        int no = 0;
+        e = cudaMemPoolSetAttribute(sv->pool, cudaMemPoolReuseAllowInternalDependencies, &no);
+    }
+    const size_t nslots = (size_t)cfg->slots;
+    if (e == cudaSuccess) {
+        sv->desc_stride = solo_args_bytes();  // the launch indexes the records as an array
+        sv->out_stride = (solo_out_bytes() + 255) & ~size_t(255);
+        e = cudaHostAlloc(&sv->desc, nslots * sv->desc_stride, cudaHostAllocMapped);
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer(&sv->desc_dev, sv->desc, 0);
+        if (e == cudaSuccess) e = cudaHostAlloc(&sv->outs, nslots * sv->out_stride, cudaHostAllocMapped);
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer(&sv->outs_dev, sv->outs, 0);
+        if (e == cudaSuccess) memset(sv->outs, 0, nslots * sv->out_stride);
+    }
     if (e != cudaSuccess) {
         int rc = cuda_status(e, "server memory");
         server_free(sv);
         return rc;
     }
-    sv->slots.resize(cfg->slots);
-    for (Slot& sl : sv->slots) {
-        int rc = mdg_ctx_create(device, &sl.ctx);
+    {
+        int rc = mdg_ctx_create(device, &sv->alloc_ctx);
+        if (rc == MDG_OK) rc = mdg_ctx_create(device, &sv->feed_ctx);
         if (rc == MDG_OK) {
-            e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
-            if (e == cudaSuccess) e = cudaMallocHost(&sl.hblock, 1024);
-            if (e == cudaSuccess) e = cudaMallocHost(&sl.pin, cfg->max_atoms * sizeof(mdg_atom));
-            if (e != cudaSuccess) rc = cuda_status(e, "slot");
+            e = cudaEventCreateWithFlags(&sv->feed_ev, cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaHostAlloc((void**)&sv->q, sizeof(SoloQueue), cudaHostAllocMapped);
+            if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&sv->q_dev, sv->q, 0);
+            if (e == cudaSuccess) memset((void*)sv->q, 0, sizeof(SoloQueue));
+            if (e == cudaSuccess) e = cudaMalloc(&sv->head, sizeof(uint32_t));
+            if (e == cudaSuccess) e = cudaMemset(sv->head, 0, sizeof(uint32_t));
+            if (e != cudaSuccess) rc = cuda_status(e, "server queue");
         }
+        // persistent kernel: block size, and as many blocks as fit on the GPU
+        sv->threads = cfg->block_threads > 0 ? cfg->block_threads : 512;
+        int per_sm = 0;
+        if (rc == MDG_OK) rc = solo_blocks_per_sm(sv->threads, &per_sm);
         if (rc != MDG_OK) {
+            server_free(sv);
+            return rc;
+        }
+        sv->blocks = std::max(1, per_sm) * std::max(1, sv->alloc_ctx->num_sms);
+    }
+    sv->slots.resize(nslots);
+    for (Slot& sl : sv->slots) {
+        e = cudaMallocHost(&sl.hblock, 1024);
+        if (e == cudaSuccess) e = cudaHostAlloc(&sl.pin, cfg->max_atoms * sizeof(mdg_atom), cudaHostAllocMapped);
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer(&sl.pin_dev, sl.pin, 0);
+        if (e != cudaSuccess) {
+            int rc = cuda_status(e, "slot");
             server_free(sv);
             return rc;
         }
@@ -491,10 +753,15 @@ int mdg_server_stats_get(mdg_server* srv, mdg_server_stats* out) {
     out->running = running_of(srv);
     out->finished = srv->nfinished;
     out->admitted = srv->admitted;
-    uint64_t total = 0;
+    uint64_t total = srv->kernel_launches;
     for (const Slot& sl : srv->slots) {
         uint64_t l = 0;
         if (sl.ctx) mdg_ctx_launch_count(sl.ctx, &l);
+        total += l;
+    }
+    for (mdg_ctx* c : {srv->alloc_ctx, srv->feed_ctx}) {
+        uint64_t l = 0;
+        if (c) mdg_ctx_launch_count(c, &l);
         total += l;
     }
     out->launches = total;

@@ -208,3 +208,29 @@ def test_first_list_overflow_takes_checked_path():
     mdg.Verlet(solv["lj"]).run(s, p["dt"], 30)
     assert _same(out, s.download())
     s.close()
+
+
+@pytest.mark.parametrize("threads", [256, 512, 1024])
+def test_fused_block_loop_matches_graph_loop(threads):
+    """The fused one-block loop (every pass of every step, rebuilds included,
+    in one block per system) gives the same bits as the graph loop, for LJ
+    and EAM, from the smallest box (n = 2 cell rule) up."""
+    _ensure_built()
+    solv = SV.solvers("mixed")
+    specs = [dict(index=0, kind=k, dims=d, n=4 * d[0] * d[1] * d[2], t_arrival=0.0, steps=120,
+                  dt=(W.SERVE_LJ if k == "lj" else W.SERVE_EAM)["dt"], seed=900 + j)
+             for j, (k, d) in enumerate((("lj", (4, 4, 4)), ("eam", (4, 4, 4)), ("lj", (9, 8, 10)),
+                                         ("eam", (12, 12, 11))))]
+    reqs = SV.prepare(specs)
+    out = {}
+    for bt in (-1, threads):
+        srv = mdg.Server(slots=4, max_atoms=8192, block_threads=bt)
+        ids = [srv.submit(solv[s["kind"]], d, a, s["dt"], s["steps"]) for s, a, d in reqs]
+        for k, rid in enumerate(ids):
+            srv.wait(rid, 120.0)
+            out[(bt, k)], info = srv.result(rid)
+            assert info["status"] == 0
+            assert info["rebuilds"] >= 2, (k, info)
+        srv.close()
+    for k in range(len(specs)):
+        assert _same(out[(-1, k)], out[(threads, k)]), f"request {k}"
