@@ -223,11 +223,13 @@ int nlist_capacity_host(mdg_system* sys, const mdg_atom* atoms, size_t n, int ha
 // The fused one-block driver loop (solo.cu): small mixed-precision systems,
 // one request per block of a persistent kernel fed through a queue.
 constexpr int kSoloRing = 4096;
+constexpr int kSoloMaxBlocks = 4096;
 struct SoloQueue {              // host-mapped
     volatile uint32_t tail;     // entries published
     volatile uint32_t stop;     // 1: blocks exit when they find no entry
     uint32_t pad[14];
     int ring[kSoloRing];        // argument-record index of each entry
+    volatile uint32_t live[2][kSoloMaxBlocks];  // per launch generation: block running
 };
 int solo_eligible(const mdg_solver* s, const mdg_system* sys);
 size_t solo_args_bytes();
@@ -242,7 +244,7 @@ void solo_fill(void* args, mdg_system* sys, const PotSet* dps, int any_eam, doub
                double dt, long steps, const void* atoms_in_dev, void* out_dev, void* atoms_out_dev, uint32_t seq);
 int solo_out_read(const void* out_host, uint32_t* done, unsigned long long* left, DevStatus* st);
 int solo_persistent_launch(cudaStream_t stream, int threads, int blocks, const void* desc_dev, SoloQueue* q_dev,
-                           uint32_t* head, int idle_limit);
+                           uint32_t* head, int idle_limit, int gen);
 int solo_blocks_per_sm(int threads, int* blocks);
 int nlist_build(mdg_system* sys, double kbuf, int half);
 int nlist_capacity(mdg_system* sys, int half);

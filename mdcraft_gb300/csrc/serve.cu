@@ -108,9 +108,10 @@ struct mdg_server {
     int block_threads = 0;
     std::vector<Slot> slots;
     mdg_ctx* alloc_ctx = nullptr;  // block-mode systems: allocations and releases
-    mdg_ctx* feed_ctx = nullptr;   // the persistent kernel
-    cudaEvent_t feed_ev = nullptr; // recorded after each persistent launch
-    int feed_launched = 0;
+    mdg_ctx* feed_ctx[2] = {nullptr, nullptr};  // the persistent kernel, two launch generations
+    cudaEvent_t feed_ev[2] = {nullptr, nullptr};  // recorded after each launch
+    int feed_launched[2] = {0, 0};
+    int feed_cur = 0;
     int threads = 512, blocks = 0; // persistent kernel shape
     SoloQueue* q = nullptr;        // host-mapped request queue
     SoloQueue* q_dev = nullptr;
@@ -486,23 +487,35 @@ int progress(mdg_server* sv) {
         MDG_CUDA(cudaEventRecord(group.ev, sv->alloc_ctx->stream));
         sv->alloc_groups.push_back(std::move(group));
     }
-    // the persistent kernel: (re)launched when requests are queued and none
-    // of its blocks is left
-    bool queued = false;
-    for (const Slot& sl : sv->slots) queued = queued || (sl.req && sl.state == BLOCK);
-    if (queued) {
-        bool running = false;
-        if (sv->feed_launched) {
-            cudaError_t e = cudaEventQuery(sv->feed_ev);
-            if (e == cudaErrorNotReady) running = true;
-            else if (e != cudaSuccess) return cuda_status(e, "persistent kernel");
-        }
-        if (!running) {
-            int rc = solo_persistent_launch(sv->feed_ctx->stream, sv->threads, sv->blocks, sv->desc_dev, sv->q_dev,
-                                            sv->head, kIdlePolls);
+    // the persistent kernel: launched when requests wait and it has fewer
+    // live blocks than it could have (its idle blocks exit after a bounded
+    // wait); the new launch is the other generation, whose previous launch
+    // must have ended, so at most two are in flight
+    size_t waiting = 0;
+    for (const Slot& sl : sv->slots) waiting += (sl.req && sl.state == BLOCK) ? 1 : 0;
+    if (waiting > 0) {
+        auto ended = [&](int gen) -> int {
+            if (!sv->feed_launched[gen]) return 1;
+            cudaError_t e = cudaEventQuery(sv->feed_ev[gen]);
+            if (e == cudaErrorNotReady) return 0;
+            return e == cudaSuccess ? 1 : -1;
+        };
+        const int cur = sv->feed_cur;
+        int live = 0;
+        int cur_end = ended(cur);
+        if (cur_end < 0) return cuda_status(cudaGetLastError(), "persistent kernel");
+        if (!cur_end)
+            for (int b = 0; b < sv->blocks; ++b) live += sv->q->live[cur][b] ? 1 : 0;
+        int gen = -1;
+        if (cur_end) gen = cur;
+        else if ((size_t)live < std::min<size_t>((size_t)sv->blocks, waiting) && ended(cur ^ 1) == 1) gen = cur ^ 1;
+        if (gen >= 0) {
+            int rc = solo_persistent_launch(sv->feed_ctx[gen]->stream, sv->threads, sv->blocks, sv->desc_dev,
+                                            sv->q_dev, sv->head, kIdlePolls, gen);
             if (rc) return rc;
-            MDG_CUDA(cudaEventRecord(sv->feed_ev, sv->feed_ctx->stream));
-            sv->feed_launched = 1;
+            MDG_CUDA(cudaEventRecord(sv->feed_ev[gen], sv->feed_ctx[gen]->stream));
+            sv->feed_launched[gen] = 1;
+            sv->feed_cur = gen;
             sv->kernel_launches++;
         }
     }
@@ -512,7 +525,8 @@ int progress(mdg_server* sv) {
 void server_free(mdg_server* sv) {
     cudaSetDevice(sv->device);
     if (sv->q) sv->q->stop = 1;
-    if (sv->feed_ctx) cudaStreamSynchronize(sv->feed_ctx->stream);
+    for (mdg_ctx* c : sv->feed_ctx)
+        if (c) cudaStreamSynchronize(c->stream);
     if (sv->alloc_ctx) cudaStreamSynchronize(sv->alloc_ctx->stream);
     for (Slot& sl : sv->slots) {
         if (sl.ctx) cudaStreamSynchronize(sl.ctx->stream);
@@ -527,9 +541,11 @@ void server_free(mdg_server* sv) {
     }
     for (AllocGroup& ag : sv->alloc_groups) sv->free_events.push_back(ag.ev);
     for (cudaEvent_t e : sv->free_events) cudaEventDestroy(e);
-    if (sv->feed_ev) cudaEventDestroy(sv->feed_ev);
+    for (int g = 0; g < 2; ++g) {
+        if (sv->feed_ev[g]) cudaEventDestroy(sv->feed_ev[g]);
+        if (sv->feed_ctx[g]) mdg_ctx_destroy(sv->feed_ctx[g]);
+    }
     if (sv->alloc_ctx) mdg_ctx_destroy(sv->alloc_ctx);
-    if (sv->feed_ctx) mdg_ctx_destroy(sv->feed_ctx);
     destroy_spent(sv);
     for (auto& kv : sv->reqs) delete kv.second;
     if (sv->desc) cudaFreeHost(sv->desc);
@@ -607,9 +623,10 @@ int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out
     }
     {
         int rc = mdg_ctx_create(device, &sv->alloc_ctx);
-        if (rc == MDG_OK) rc = mdg_ctx_create(device, &sv->feed_ctx);
+        for (int g = 0; g < 2 && rc == MDG_OK; ++g) rc = mdg_ctx_create(device, &sv->feed_ctx[g]);
         if (rc == MDG_OK) {
-            e = cudaEventCreateWithFlags(&sv->feed_ev, cudaEventDisableTiming);
+            e = cudaEventCreateWithFlags(&sv->feed_ev[0], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sv->feed_ev[1], cudaEventDisableTiming);
             if (e == cudaSuccess) e = cudaHostAlloc((void**)&sv->q, sizeof(SoloQueue), cudaHostAllocMapped);
             if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&sv->q_dev, sv->q, 0);
             if (e == cudaSuccess) memset((void*)sv->q, 0, sizeof(SoloQueue));
@@ -625,7 +642,7 @@ int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out
             server_free(sv);
             return rc;
         }
-        sv->blocks = std::max(1, per_sm) * std::max(1, sv->alloc_ctx->num_sms);
+        sv->blocks = std::min(kSoloMaxBlocks, std::max(1, per_sm) * std::max(1, sv->alloc_ctx->num_sms));
     }
     sv->slots.resize(nslots);
     for (Slot& sl : sv->slots) {
@@ -759,7 +776,7 @@ int mdg_server_stats_get(mdg_server* srv, mdg_server_stats* out) {
         if (sl.ctx) mdg_ctx_launch_count(sl.ctx, &l);
         total += l;
     }
-    for (mdg_ctx* c : {srv->alloc_ctx, srv->feed_ctx}) {
+    for (mdg_ctx* c : {srv->alloc_ctx, srv->feed_ctx[0], srv->feed_ctx[1]}) {
         uint64_t l = 0;
         if (c) mdg_ctx_launch_count(c, &l);
         total += l;

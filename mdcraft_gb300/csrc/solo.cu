@@ -374,12 +374,15 @@ __device__ __forceinline__ uint32_t ld_acquire_sys(const volatile uint32_t* p) {
 // `stop`, exits. Every wait is bounded.
 template <int NT>
 __global__ void __launch_bounds__(NT, 1) k_solo_persistent(const SoloArgs* __restrict__ desc, SoloQueue* q,
-                                                        uint32_t* head, int idle_limit) {
+                                                           uint32_t* head, int idle_limit, int gen) {
     __shared__ __align__(16) SoloArgs S;
     __shared__ GridParams g;
     __shared__ double red[7][NT / 32];
     __shared__ uint32_t scan_sh[32];
     __shared__ int s_rec;
+    // liveness for the host, which tops up the kernel's width with a second
+    // launch when blocks have gone idle and exited while requests wait
+    if (threadIdx.x == 0) q->live[gen][blockIdx.x] = 1u;
     for (;;) {
         if (threadIdx.x == 0) {
             int rec = -1;
@@ -409,6 +412,10 @@ __global__ void __launch_bounds__(NT, 1) k_solo_persistent(const SoloArgs* __res
         __syncthreads();
         if (S.any_eam) solo_run<true, NT>(S, g, red, scan_sh);
         else solo_run<false, NT>(S, g, red, scan_sh);
+    }
+    if (threadIdx.x == 0) {
+        __threadfence_system();
+        q->live[gen][blockIdx.x] = 0u;
     }
 }
 
@@ -479,12 +486,13 @@ int solo_out_read(const void* out_host, uint32_t* done, unsigned long long* left
 }
 
 int solo_persistent_launch(cudaStream_t stream, int threads, int blocks, const void* desc_dev, SoloQueue* q_dev,
-                           uint32_t* head, int idle_limit) {
+                           uint32_t* head, int idle_limit, int gen) {
     const SoloArgs* d = reinterpret_cast<const SoloArgs*>(desc_dev);
     if (blocks <= 0) return MDG_OK;
-    if (threads == 256) k_solo_persistent<256><<<blocks, 256, 0, stream>>>(d, q_dev, head, idle_limit);
-    else if (threads == 1024) k_solo_persistent<1024><<<blocks, 1024, 0, stream>>>(d, q_dev, head, idle_limit);
-    else k_solo_persistent<512><<<blocks, 512, 0, stream>>>(d, q_dev, head, idle_limit);
+    if (blocks > kSoloMaxBlocks || gen < 0 || gen > 1) return MDG_ERR_INVALID;
+    if (threads == 256) k_solo_persistent<256><<<blocks, 256, 0, stream>>>(d, q_dev, head, idle_limit, gen);
+    else if (threads == 1024) k_solo_persistent<1024><<<blocks, 1024, 0, stream>>>(d, q_dev, head, idle_limit, gen);
+    else k_solo_persistent<512><<<blocks, 512, 0, stream>>>(d, q_dev, head, idle_limit, gen);
     MDG_CUDA(cudaGetLastError());
     return MDG_OK;
 }
