@@ -54,6 +54,8 @@ def parse():
                     help="threads of the fused per-system block (256, 512, 1024; -1: a graph loop per request)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="only the serving stream (prints its summary)")
+    ap.add_argument("--config", default="", choices=["", "lj_argon", "nial", "lj_liquid", "nve_drift"],
+                    help="one of the other benchmark configurations (prints its own JSON line)")
     return ap.parse_args()
 
 
@@ -253,6 +255,16 @@ def run_mdg(args, rank, world, local):
 
     B.build()
     dist = Dist(world, local)
+    if args.config:
+        if rank == 0:
+            from mdcraft_gb300 import benchmarks as BM
+            clocks = Clocks(local)
+            clocks.start()
+            res = BM.CONFIGS[args.config](device=local)
+            res["clocks"] = clocks.stop()
+            print(json.dumps({"bench_config": args.config, **res}), flush=True)
+        dist.close()
+        return
     if args.serve_only:
         if rank == 0:
             print(json.dumps({"serving": run_serving(args, local)}), flush=True)

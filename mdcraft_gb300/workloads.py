@@ -15,8 +15,9 @@ identical inputs.
                      a = 2.88 A, per-pair analytic tables, rc = 6.0 A,
                      skin 0.5 A, 600 K, dt = 1 fs.
 - lj_liquid        : reduced LJ liquid (rho* = 0.8442, T* = 0.72) mapped to
-                     argon, fcc start with jitter, rc = 2.5 sigma,
-                     skin 0.3 sigma, dt* = 0.005.
+                     argon, fcc start with a bounded uniform jitter (at most
+                     0.05 a per component, so no pair starts closer than
+                     0.9 sigma), rc = 2.5 sigma, skin 0.3 sigma, dt* = 0.005.
 """
 from __future__ import annotations
 
@@ -197,7 +198,9 @@ def lj_liquid(nx=128, ny=128, nz=256, seed=4, rho_star=0.8442, T_star=0.72):
     Lx, Ly, Lz = nx * a, ny * a, nz * a
     rng = np.random.default_rng(seed)
     r = fcc_positions(nx, ny, nz, a) + 0.25 * a
-    r = r + rng.standard_normal(r.shape) * (0.05 * a)
+    # bounded displacements: a Gaussian tail would put a few pairs nearly on
+    # top of each other in a system of millions and blow it apart at step 1
+    r = r + rng.uniform(-0.05 * a, 0.05 * a, size=r.shape)
     atoms = new_atoms(len(r))
     atoms["r"] = np.stack([_wrap_inside(r[:, 0], 0, Lx), _wrap_inside(r[:, 1], 0, Ly),
                            _wrap_inside(r[:, 2], 0, Lz)], 1)
