@@ -257,20 +257,25 @@ __global__ void __launch_bounds__(kBlock) k_virials64(FArgs A, const PotSet* __r
 // ---------------------------------------------------------------------------
 // mixed precision (bodies in forces_dev.cuh)
 // ---------------------------------------------------------------------------
+// Blocks of 256 threads per SM the register budget must allow (measured on
+// EAM Cu 1M atoms: the force kernels are fastest at 4 (64 registers), the
+// density kernel at 5; more registers lose occupancy, fewer spill).
+constexpr int kForceMinBlocks = 4;
+constexpr int kDensityMinBlocks = 5;
 template <bool MULTI>
-__global__ void __launch_bounds__(kBlock) k_lj_mixed(FArgs A, const PotSet* __restrict__ ps) {
+__global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_lj_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < A.n) lj_mixed_one<MULTI>(A, ps, i);
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(kBlock) k_density_mixed(FArgs A, const PotSet* __restrict__ ps) {
+__global__ void __launch_bounds__(kBlock, kDensityMinBlocks) k_density_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < A.n) density_mixed_one<MULTI>(A, ps, i);
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(kBlock) k_eam_mixed(FArgs A, const PotSet* __restrict__ ps) {
+__global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_eam_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < A.n) eam_mixed_one<MULTI>(A, ps, i);
 }

@@ -120,8 +120,11 @@ __device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __res
     double R2c = P0.R2cut;
     Kahan3 acc;
     const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
+    uint4 e4n = ng > 0 ? __ldg(row) : make_uint4(0, 0, 0, 0);
     for (int g = 0; g < ng; ++g) {
-        const uint4 e4 = __ldg(row + (size_t)g * A.np);
+        // the next group's entries are requested before this group's work
+        const uint4 e4 = e4n;
+        if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
         const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
         float4 pj[4];
 #pragma unroll
@@ -182,8 +185,11 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
         int Nr1 = P->Nr1;
         const float4* tab = P->rho_c;
         const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
+        uint4 e4n = ng > 0 ? __ldg(row) : make_uint4(0, 0, 0, 0);
         for (int g = 0; g < ng; ++g) {
-            const uint4 e4 = __ldg(row + (size_t)g * A.np);
+            // the next group's entries are requested before this group's work
+            const uint4 e4 = e4n;
+            if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
             const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
             float4 pj[4];
 #pragma unroll
@@ -240,8 +246,11 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
     const float4* vt = P->v_c;
     Kahan3 acc;
     const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
+    uint4 e4n = ng > 0 ? __ldg(row) : make_uint4(0, 0, 0, 0);
     for (int g = 0; g < ng; ++g) {
-        const uint4 e4 = __ldg(row + (size_t)g * A.np);
+        // the next group's entries are requested before this group's work
+        const uint4 e4 = e4n;
+        if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
         const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
         float4 pj[4];
 #pragma unroll
