@@ -65,6 +65,14 @@ __device__ __forceinline__ void pair_vec32(uint32_t e, const float4& pi, const f
     dz = (pj.z - pi.z) + image_shift(e, 2, csf[2]);
 }
 
+// 1/sqrt(x) for x > 0: the hardware estimate refined by one Newton step, so
+// r = x * rinv and 1/r are nearly correctly rounded (pair forces near an
+// equilibrium lattice cancel, which magnifies their relative errors).
+__device__ __forceinline__ float rsqrt_nr(float x) {
+    const float y = rsqrtf(x);
+    return y * fmaf(-0.5f * x * y, y, 1.5f);
+}
+
 __device__ __forceinline__ float cubic(const float4 c, float u) {
     return fmaf(u, fmaf(u, fmaf(u, c.w, c.z), c.y), c.x);
 }
@@ -140,7 +148,7 @@ __device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __res
             pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             bool in = pair_in(A, i, e[q], r2, r2c, R2c, per);
-            float r2inv = __frcp_rn(fmaxf(r2, 1e-12f));
+            float r2inv = __fdividef(1.0f, fmaxf(r2, 1e-12f));
             float r6inv = r2inv * r2inv * r2inv;
             float pref = in ? mh * fmaf(l1, r6inv, -l2) * r6inv * r2inv : 0.f;
             fx = fmaf(dx, pref, fx);
@@ -207,7 +215,7 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
                 pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
                 float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                 bool in = eam && pair_in(A, i, e[q], r2, r2c, R2c, per);
-                float t = sqrtf(r2) * idr;
+                float t = r2 * rsqrt_nr(fmaxf(r2, 1e-12f)) * idr;
                 int nn = (int)t;
                 in = in && nn < Nr1;
                 nn = in ? nn : 0;
@@ -273,7 +281,9 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
             pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             bool in = eam && pair_in(A, i, e[q], r2, r2c, R2c, per);
-            float r = sqrtf(r2);
+            // one reciprocal square root gives both r and 1/r
+            float rinv = rsqrt_nr(fmaxf(r2, 1e-12f));
+            float r = r2 * rinv;
             float t = r * idr;
             int nn = (int)t;
             in = in && nn < Nr1;
@@ -284,7 +294,6 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
             float drho = dcubic(cr, u) * idr;
             float V = cubic(cv, u);
             float dV = dcubic(cv, u) * idr;
-            float rinv = __frcp_rn(fmaxf(r, 1e-6f));
             float FF = fmaf(Fpi + Fpj, drho, (dV * r - V) * (rinv * rinv)) * rinv;
             FF = in ? FF : 0.f;
             fx = fmaf(FF, dx, fx);

@@ -88,8 +88,8 @@ constexpr uint32_t kSelfCode = 0x15u << kJBits;  // image (0,0,0)
 
 // Image offset encoded in a list entry (2 bits per axis, value+1).
 __device__ inline float image_shift(uint32_t e, int axis, float cs) {
-    uint32_t b = (e >> (kJBits + 2 * axis)) & 3u;
-    return b == 0u ? -cs : (b == 2u ? cs : 0.0f);
+    int b = (int)((e >> (kJBits + 2 * axis)) & 3u);  // 0, 1, 2 for -1, 0, +1 cells
+    return __int2float_rn(b - 1) * cs;
 }
 
 // Per-kind-pair potential parameters handed to the force kernels by value.

@@ -233,10 +233,11 @@ __global__ void __launch_bounds__(kBlock) k_nbuild(NbArgs A, const GridParams* _
     __shared__ GridParams g;
     if (threadIdx.x == 0) g = *gp;
     __syncthreads();
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (g.empty || warp >= g.nbins) return;
-    nbuild_bin(A, g, warp, lane, A.st->nonuniform == 0);
+    // a half warp per bin
+    int bin = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+    int lane = threadIdx.x & 15;
+    if (g.empty || bin >= g.nbins) return;
+    nbuild_bin(A, g, bin, lane, A.st->nonuniform == 0, 16);
 }
 
 // VerletList::optimize_search_radius (verlet-list.cxx:72-92):
@@ -555,8 +556,8 @@ int nlist_enqueue(mdg_system* sys) {
                                         sys->u32[ORIG][c], sys->slot_of);
     MDG_LAUNCHED(ctx);
     NbArgs A = nb_args(sys);
-    size_t warps = sys->bin_cap;  // one warp per bin; the live bins come from the device grid
-    k_nbuild<<<nblk(warps * 32), kBlock, 0, st>>>(A, sys->dgrid);
+    // a half warp per bin of the capacity; the live bins come from the device grid
+    k_nbuild<<<nblk(sys->bin_cap * 16), kBlock, 0, st>>>(A, sys->dgrid);
     MDG_LAUNCHED(ctx);
     return MDG_OK;
 }

@@ -238,10 +238,12 @@ __device__ __forceinline__ bool are_neibs_exact(const GridParams& g, double xa, 
     return sq3_exact(drx, dry, drz) <= d2;
 }
 
-// The list of every atom of one bin (cell), one lane per atom: the 27 (or
-// fewer, on small periodic axes) neighbour cells in the reference's order.
+// The list of every atom of one bin (cell), one lane per atom, `width`
+// lanes per cell (a cell holds ~10-20 atoms, so two cells share a warp): the
+// 27 (or fewer, on small periodic axes) neighbour cells in the reference's
+// order.
 __device__ __forceinline__ void nbuild_bin(const NbArgs& A, const GridParams& g, int bin, int lane,
-                                           bool uniform_rns) {
+                                           bool uniform_rns, int width) {
     // prefilter band: rns^2 (1 -/+ 1e-5), valid when every atom has the same rns
     const float lo2 = (float)(g.max_rns * g.max_rns * (1.0 - 1e-5));
     const float hi2 = (float)(g.max_rns * g.max_rns * (1.0 + 1e-5));
@@ -256,7 +258,7 @@ __device__ __forceinline__ void nbuild_bin(const NbArgs& A, const GridParams& g,
     for (int a = 0; a < g.dim; ++a) edge[a] = gc[a] == 0 || gc[a] == g.num[a] - 1;
     const bool prefilter = uniform_rns && !g.small_box;
 
-    for (uint32_t base = s0; base < s1; base += 32) {
+    for (uint32_t base = s0; base < s1; base += width) {
         uint32_t i = base + lane;
         bool active = i < s1;
         double xi = 0, yi = 0, zi = 0, rni = 0;
