@@ -191,7 +191,11 @@ __device__ bool solo_rebuild(const SoloArgs& S, GridParams& g, double (*red)[NT 
     __syncthreads();
     {
         const bool uniform = S.st->nonuniform == 0;
-        for (int b = 2 * w + (lane >> 4); b < nb; b += NT / 16) nbuild_bin(S.N, g, b, lane & 15, uniform, 16);
+        if (n > 16 * g.ncells) {
+            for (int b = w; b < nb; b += NT / 32) nbuild_bin(S.N, g, b, lane, uniform, 32);
+        } else {
+            for (int b = 2 * w + (lane >> 4); b < nb; b += NT / 16) nbuild_bin(S.N, g, b, lane & 15, uniform, 16);
+        }
     }
     __syncthreads();
     for (int i = t; i < n; i += NT) trig_one(i, S.saved_rns, S.saved_rcut, S.trig);
