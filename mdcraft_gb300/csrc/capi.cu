@@ -784,7 +784,9 @@ int mdg_system_download_atoms(mdg_system* sys, mdg_atom* atoms, size_t n) {
     return MDG_OK;
 }
 
-static int vec_io(mdg_system* sys, double* host, int field, int in) {
+// Enqueues one xyz transfer (caller order <-> slot order through the
+// transfer buffer); `sync` waits for it (the host buffer is then free).
+static int vec_io(mdg_system* sys, double* host, int field, int in, int sync = 1) {
     if (!sys || !host) return MDG_ERR_INVALID;
     size_t n = sys->n;
     if (n == 0) return MDG_OK;
@@ -804,7 +806,7 @@ static int vec_io(mdg_system* sys, double* host, int field, int in) {
             rc = launch_offsets(sys);
             if (rc) return rc;
         }
-        MDG_CUDA(cudaStreamSynchronize(st));
+        if (sync) MDG_CUDA(cudaStreamSynchronize(st));
     } else {
         if (field == FX) {
             rc = sync_forces64(sys);
@@ -814,7 +816,7 @@ static int vec_io(mdg_system* sys, double* host, int field, int in) {
                                               sys->f64[field + 2][c], (double*)dbuf);
         MDG_LAUNCHED(sys->ctx);
         MDG_CUDA(cudaMemcpyAsync(host, dbuf, bytes, cudaMemcpyDeviceToHost, st));
-        MDG_CUDA(cudaStreamSynchronize(st));
+        if (sync) MDG_CUDA(cudaStreamSynchronize(st));
     }
     return MDG_OK;
 }
@@ -1338,6 +1340,13 @@ __global__ void k_loop_ctrl(cudaGraphConditionalHandle h, unsigned long long* co
     cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
+// Whether the step loop runs at all: steps to do and no overflowed rebuild
+// before it (the host then grows the capacities and relaunches).
+__global__ void k_loop_start(cudaGraphConditionalHandle h, const unsigned long long* counter, const DevStatus* st) {
+    if (threadIdx.x != 0) return;
+    cudaGraphSetConditional(h, (*counter > 0 && !(st->build_flags & FLAG_OVERFLOW)) ? 1u : 0u);
+}
+
 __global__ void k_set_counter(unsigned long long* counter, unsigned long long v, DevStatus* st) {
     if (threadIdx.x == 0) {
         *counter = v;
@@ -1367,19 +1376,81 @@ static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, dou
     cudaGraph_t g = nullptr;
     MDG_CUDA(cudaGraphCreate(&g, 0));
     sys->run_graph = g;
-    cudaGraphConditionalHandle hloop, hrb;
+    cudaGraphConditionalHandle hloop, hrb, hpre = 0;
     MDG_CUDA(cudaGraphConditionalHandleCreate(&hloop, g, 1, cudaGraphCondAssignDefault));
+    // a handle must belong to a conditional node: only the mixed form has the pre-rebuild
+    if (prec == MDG_PREC_MIXED) MDG_CUDA(cudaGraphConditionalHandleCreate(&hpre, g, 0, cudaGraphCondAssignDefault));
+
+    // Prefix: the mixed form prepares rcut and the boundary flags, rebuilds
+    // the list when an upload moved atoms past the half skin (the rebuild
+    // test on the prepared state), and refreshes the cell offsets — on the
+    // device, so a run starts without a host round trip. Then the WHILE
+    // node over steps, entered only when steps remain and no rebuild
+    // overflowed.
+    uint64_t l0 = ctx->launches;
+    int pre_kernels = 0;
+    cudaGraphNodeParams pp = {};
     cudaGraphNodeParams wp = {};
-    wp.type = cudaGraphNodeTypeConditional;
-    wp.conditional.handle = hloop;
-    wp.conditional.type = cudaGraphCondTypeWhile;
-    wp.conditional.size = 1;
-    cudaGraphNode_t wnode;
-    MDG_CUDA(cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp));
+    {
+        MDG_CUDA(cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        int rc0 = 0;
+        cudaError_t e = cudaSuccess;
+        auto add_cond = [&](cudaGraphNodeParams& np) {
+            cudaStreamCaptureStatus cs0;
+            cudaGraph_t cg0 = nullptr;
+            const cudaGraphNode_t* d0 = nullptr;
+            const cudaGraphEdgeData* ed0 = nullptr;
+            size_t nd0 = 0;
+            cudaGraphNode_t node = nullptr;
+            cudaError_t ee = cudaStreamGetCaptureInfo(st, &cs0, nullptr, &cg0, &d0, &ed0, &nd0);
+            if (ee == cudaSuccess) ee = cudaGraphAddNode(&node, cg0, d0, ed0, nd0, &np);
+            if (ee == cudaSuccess)
+                ee = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+            return ee;
+        };
+        if (prec == MDG_PREC_MIXED) {
+            rc0 = launch_drift(sys, 0.0, MDG_PREC_FP64, s->multi ? -1.0 : s->pot[0][0]->rcut, s->periodic, 0, 1);
+            if (rc0 == 0) {
+                k_rebuild_cond<<<1, 32, 0, st>>>(hpre, sys->dstat);
+                ctx->launches++;
+                pp.type = cudaGraphNodeTypeConditional;
+                pp.conditional.handle = hpre;
+                pp.conditional.type = cudaGraphCondTypeIf;
+                pp.conditional.size = 1;
+                e = add_cond(pp);
+            }
+            if (rc0 == 0 && e == cudaSuccess) rc0 = launch_offsets(sys);
+        }
+        if (rc0 == 0 && e == cudaSuccess) {
+            k_loop_start<<<1, 32, 0, st>>>(hloop, sys->dcounter, sys->dstat);
+            ctx->launches++;
+            wp.type = cudaGraphNodeTypeConditional;
+            wp.conditional.handle = hloop;
+            wp.conditional.type = cudaGraphCondTypeWhile;
+            wp.conditional.size = 1;
+            e = add_cond(wp);
+        }
+        cudaGraph_t outp = nullptr;
+        cudaError_t ec = cudaStreamEndCapture(st, &outp);
+        if (rc0) return rc0;
+        if (e != cudaSuccess) return cuda_status(e, "graph prefix node");
+        if (ec != cudaSuccess) return cuda_status(ec, "prefix capture");
+        pre_kernels = (int)(ctx->launches - l0);
+    }
+    if (pp.conditional.phGraph_out) {
+        MDG_CUDA(cudaStreamBeginCaptureToGraph(st, pp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal));
+        int rc1 = nlist_enqueue(sys);
+        if (rc1 == 0) rc1 = launch_trig(sys);
+        cudaGraph_t outr = nullptr;
+        cudaError_t ec = cudaStreamEndCapture(st, &outr);
+        if (rc1) return rc1;
+        if (ec != cudaSuccess) return cuda_status(ec, "pre-rebuild capture");
+    }
     cudaGraph_t body = wp.conditional.phGraph_out[0];
     MDG_CUDA(cudaGraphConditionalHandleCreate(&hrb, body, 0, cudaGraphCondAssignDefault));
 
-    uint64_t l0 = ctx->launches;
+    l0 = ctx->launches;
     MDG_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int rc = launch_drift(sys, dt, prec, s->multi ? -1.0 : s->pot[0][0]->rcut, s->periodic, 1, 1);
     for (int q = 0; rc == 0 && q < s->nstages; ++q) rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q]);
@@ -1426,7 +1497,9 @@ static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, dou
     if (rc) return rc;
     if (e2 != cudaSuccess) return cuda_status(e2, "rebuild capture");
     sys->run_rebuild_kernels = (int)(ctx->launches - l0);
-    ctx->launches -= (uint64_t)sys->run_step_kernels + (uint64_t)sys->run_rebuild_kernels;  // counted when run
+    sys->run_pre_kernels = pre_kernels;
+    // counted when run (the pre-rebuild's kernels are counted as one rebuild)
+    ctx->launches -= (uint64_t)sys->run_step_kernels + 2 * (uint64_t)sys->run_rebuild_kernels + pre_kernels;
     MDG_CUDA(cudaGraphInstantiate(&sys->run_exec, g, 0));
     return MDG_OK;
 }
@@ -1458,6 +1531,7 @@ int run_graph_launch(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt
     MDG_CUDA(cudaMemcpyAsync(sys->hcounter, sys->dcounter, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     MDG_CUDA(cudaMemcpyAsync(sys->hstat, sys->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, st));
     sys->run_launched = left;
+    sys->force_prec = s->precision;  // what later work in stream order will find
     return MDG_OK;
 }
 
@@ -1470,7 +1544,8 @@ int run_graph_finish(mdg_solver* s, mdg_system* sys, long* left) {
     long done = sys->run_launched - rem;
     uint32_t nreb = sys->hstat->pad[0];
     sys->rebuilds += nreb;
-    ctx->launches += (uint64_t)done * sys->run_step_kernels + (uint64_t)nreb * sys->run_rebuild_kernels;
+    ctx->launches += (uint64_t)sys->run_pre_kernels + (uint64_t)done * sys->run_step_kernels +
+                     (uint64_t)nreb * sys->run_rebuild_kernels;
     sys->force_prec = s->precision;
     *left = rem;
     if (sys->hstat->build_flags & FLAG_OVERFLOW) {
@@ -1505,24 +1580,11 @@ extern "C" {
 
 namespace mdg {
 
-// Before the graph loop: the mixed form prepares rcut and the boundary flags
-// once, rebuilds when that or an upload invalidated the list, and refreshes
-// the offsets; forces are brought into the solver's arithmetic.
+// Before the graph loop: forces are brought into the solver's arithmetic
+// (the graph's own prefix prepares, re-checks the list and refreshes the
+// offsets).
 static int graph_prologue(mdg_solver* s, mdg_system* sys) {
     int rc;
-    if (s->precision == MDG_PREC_MIXED) {
-        rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
-        if (rc) return rc;
-        int need = 0;
-        rc = mdg_nlist_decide(sys, &need);
-        if (rc) return rc;
-        if (need) {
-            rc = mdg_nlist_update(sys, -1.0, 0);
-            if (rc && rc != MDG_ERR_RANGE) return rc;
-        }
-        rc = launch_offsets(sys);
-        if (rc) return rc;
-    }
     if (sys->force_prec != s->precision) {
         rc = launch_force_copy(sys, s->precision == MDG_PREC_FP64);
         if (rc) return rc;
@@ -1724,6 +1786,35 @@ done:
 
 int mdg_run_host(mdg_solver* s, mdg_system* sys, double dt, long steps, double* pos, double* vel, double* force) {
     if (!s || !sys || !pos || !vel) return MDG_ERR_INVALID;
+    PotSet ps;
+    if (steps > 0 && !sys->ctx->timing && sys->n > 0 && !sys->half && check_ready(s, sys, &ps) == MDG_OK) {
+        // the whole call in stream order with one wait: uploads, the graph
+        // loop, its status read-back, the downloads (the transfer buffer is
+        // reused in order, so no transfer waits for another)
+        int rc = vec_io(sys, pos, RX, 1, 0);
+        if (!rc) rc = vec_io(sys, vel, VX, 1, 0);
+        if (!rc) rc = graph_prologue(s, sys);
+        if (!rc) rc = run_graph_launch(s, sys, ps, dt, steps);
+        if (!rc) rc = vec_io(sys, pos, RX, 0, 0);
+        if (!rc) rc = vec_io(sys, vel, VX, 0, 0);
+        if (!rc && force) rc = vec_io(sys, force, FX, 0, 0);
+        if (rc) return rc;
+        MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+        long left = 0;
+        rc = run_graph_finish(s, sys, &left);
+        if (rc) return rc;
+        if (left == 0) return MDG_OK;
+        // a rebuild outgrew its capacities (grown now): finish the steps and
+        // download again
+        rc = run_graph(s, sys, ps, dt, left);
+        if (rc) return rc;
+        rc = vec_io(sys, pos, RX, 0, 0);
+        if (!rc) rc = vec_io(sys, vel, VX, 0, 0);
+        if (!rc && force) rc = vec_io(sys, force, FX, 0, 0);
+        if (rc) return rc;
+        MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+        return MDG_OK;
+    }
     int rc = mdg_system_set_positions(sys, pos);
     if (rc) return rc;
     rc = mdg_system_set_velocities(sys, vel);

@@ -151,6 +151,7 @@ struct mdg_system {
     long run_launched = 0;                   // steps handed to the last graph launch
     int run_step_kernels = 0;                // kernels per step / per rebuild in the graph
     int run_rebuild_kernels = 0;
+    int run_pre_kernels = 0;                 // kernels of the graph's prefix
     double graph_build_s = 0.0;              // host seconds spent building run graphs
     int solo_threads = 0;                    // > 0: run loops as one block of this many threads (solo.cu)
 

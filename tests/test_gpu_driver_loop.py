@@ -1,0 +1,69 @@
+"""The driver loop's host-facing forms: mdg_run_host (uploads, the graph
+loop and downloads in stream order) equals upload + mdg_run + download, and
+the graph loop's device-side prologue (rebuild test after an upload) equals
+the host-side one of the stepwise loop."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import mdcraft_gb300 as mdg
+from mdcraft_gb300 import workloads as W
+from tests import gpu_helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(make, prec):
+    atoms, box, per, p = make()
+    _, g = H.make_pair(atoms, box, (1, 1, 1), p, precision=prec)
+    g["nl"].update(-1.0)
+    g["solver"].prepare(g["sys"])
+    g["solver"].stages(g["sys"])
+    return atoms, p, g
+
+
+CASES = [(lambda: W.eam_cu_fcc(ncell=8), "mixed"), (lambda: W.lj_argon_fcc(jitter=0.01), "fp64"),
+         (lambda: W.lj_argon_fcc(jitter=0.01), "mixed")]
+
+
+@pytest.mark.parametrize("make,prec", CASES, ids=["eam_mixed", "lj_fp64", "lj_mixed"])
+def test_run_host_equals_run_and_download(make, prec):
+    atoms, p, a = _pair(make, prec)
+    a["stepper"].run(a["sys"], p["dt"], 50)
+    ref = a["sys"].download()
+    _, _, b = _pair(make, prec)
+    pos = np.ascontiguousarray(atoms["r"].copy())
+    vel = np.ascontiguousarray(atoms["v"].copy())
+    frc = np.zeros_like(pos)
+    b["stepper"].run_host(b["sys"], p["dt"], 50, pos, vel, frc)
+    assert np.array_equal(pos, ref["r"])
+    assert np.array_equal(vel, ref["v"])
+    assert np.array_equal(frc, ref["f"])
+    assert a["nl"].rebuilds() == b["nl"].rebuilds()
+
+
+@pytest.mark.parametrize("make", [lambda: W.eam_cu_fcc(ncell=8), lambda: W.lj_argon_fcc(jitter=0.01)],
+                         ids=["eam", "lj"])
+def test_graph_prologue_rebuilds_after_upload(make):
+    """Positions moved past the half skin by an upload: the graph loop's
+    prologue rebuilds on the device, as the stepwise loop's host prologue
+    does; the two runs give the same bits."""
+    out = []
+    for timing in (False, True):
+        atoms, p, g = _pair(make, "mixed")
+        g["stepper"].run(g["sys"], p["dt"], 5)
+        r = g["sys"].positions()
+        rng = np.random.default_rng(9)
+        r = r + rng.uniform(-1, 1, r.shape) * 0.6 * p["skin"]
+        g["sys"].set_positions(np.ascontiguousarray(r))
+        rb0 = g["nl"].rebuilds()
+        ctx = g["sys"].ctx
+        ctx.set_timing(timing)
+        g["stepper"].run(g["sys"], p["dt"], 20)
+        ctx.set_timing(False)
+        out.append((g["sys"].download(), g["nl"].rebuilds() - rb0))
+    (a, ra), (b, rb) = out
+    assert ra == rb and ra >= 1
+    for k in ("r", "v", "f"):
+        assert np.array_equal(a[k], b[k]), k
