@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=4096)
     ap.add_argument("--serve-slots", type=int, default=320)
     ap.add_argument("--serve-steps", type=int, default=1000)
-    ap.add_argument("--serve-block-threads", type=int, default=512,
+    ap.add_argument("--serve-block-threads", type=int, default=1024,
                     help="threads of the fused per-system block (256, 512, 1024; -1: a graph loop per request)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="only the serving stream (prints its summary)")

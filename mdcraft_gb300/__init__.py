@@ -465,6 +465,8 @@ class Server:
 
     def __init__(self, device: int = 0, slots: int = 16, hbm_budget: int = 0, max_atoms: int = 1 << 16,
                  block_threads: int = 0):
+        """block_threads: threads of the fused per-request block (256, 512, 1024; 0 = 1024);
+        -1 runs every request as a graph loop on its slot's stream instead."""
         cfg = _ServerConfig(slots, hbm_budget, max_atoms, block_threads)
         h = C.c_void_p()
         _check(lib().mdg_server_create(device, C.byref(cfg), C.byref(h)))
