@@ -372,8 +372,12 @@ def run_mdg(args, rank, world, local):
     achieved = bytes_atom * n / (force_launch_ms / 1e3) / 1e9
     pk = peaks()
     peak = pk.get("hbm_gbs", 6800.0)
+    # DRAM bytes of one k_eam_mixed launch from ncu (read + write, 112.61 MB for 442,368 atoms of the
+    # same workload family, profiles/k_eam_mixed_eam_cu_442k.md), scaled to this launch by atoms
+    traffic = 112.61e6 / 442368 * n
     roof = {"bound": "hbm", "kernel": "k_eam_mixed (EAM force, mixed)", "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum on 442,368 atoms, scaled by atoms",
             "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
             "bytes_per_atom": bytes_atom, "launch_ms": force_launch_ms}
 
