@@ -50,8 +50,9 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=4096)
     ap.add_argument("--serve-slots", type=int, default=320)
     ap.add_argument("--serve-steps", type=int, default=1000)
-    ap.add_argument("--serve-block-threads", type=int, default=1024,
-                    help="threads of the fused per-system block (256, 512, 1024; -1: a graph loop per request)")
+    ap.add_argument("--serve-block-threads", type=int, default=0,
+                    help="threads of the fused per-system block (256, 512, 1024; 0: chosen by the autotuner "
+                         "on a sample of the stream; -1: a graph loop per request)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="only the serving stream (prints its summary)")
     ap.add_argument("--config", default="", choices=["", "lj_argon", "nial", "lj_liquid", "nve_drift"],
@@ -66,38 +67,9 @@ def dist_env():
     return rank, world, local
 
 
-class Dist:
-    def __init__(self, world, local):
-        self.world = world
-        self.pg = None
-        if world > 1:
-            import torch
-            import torch.distributed as td
-            torch.cuda.set_device(local)
-            td.init_process_group("nccl")
-            self.td, self.torch = td, torch
-
-    def barrier(self):
-        if self.world > 1:
-            self.td.barrier()
-
-    def max(self, x: float) -> float:
-        if self.world == 1:
-            return x
-        t = self.torch.tensor([x], device="cuda", dtype=self.torch.float64)
-        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum(self, x: float) -> float:
-        if self.world == 1:
-            return x
-        t = self.torch.tensor([x], device="cuda", dtype=self.torch.float64)
-        self.td.all_reduce(t)
-        return float(t.item())
-
-    def close(self):
-        if self.world > 1:
-            self.td.destroy_process_group()
+def Dist(world, local):
+    from mdcraft_gb300.replicas import Replicas
+    return Replicas(world, local, "nccl")
 
 
 class Clocks:
@@ -216,8 +188,12 @@ def run_serving(args, device):
     from mdcraft_gb300 import workloads as W
     specs = W.serving_stream(count=args.serve_requests, steps=args.serve_steps)
     solv = SV.solvers("mixed")
+    threads, tuning = args.serve_block_threads, None
+    if threads == 0:
+        from mdcraft_gb300 import tune
+        threads, tuning = tune.tune_serving(specs, solv, device=device, slots=args.serve_slots)
     reqs = SV.prepare(specs)
-    srv = mdg.Server(device=device, slots=args.serve_slots, max_atoms=32768, block_threads=args.serve_block_threads)
+    srv = mdg.Server(device=device, slots=args.serve_slots, max_atoms=32768, block_threads=threads)
     # warm-up: one request of each kind (pool pages, potential tables)
     for kind in ("lj", "eam"):
         s = next(x for x in specs if x["kind"] == kind)
@@ -233,7 +209,8 @@ def run_serving(args, device):
     st = srv.stats()
     srv.close()
     summary.update({"workload": SERVE_WORKLOAD, "slots": args.serve_slots, "steps_per_request": args.serve_steps,
-                    "block_threads": args.serve_block_threads,
+                    "block_threads": threads,
+                    "tuning": ({str(k): v for k, v in tuning.items()} if tuning else "given"),
                     "arrival_rate_per_s": 2000.0, "budget_bytes": st["budget"], "peak_bytes": st["peak"],
                     # the persistent kernel launched for the warm-up may still be the one that
                     # serves the stream: count every launch of the server

@@ -234,3 +234,15 @@ def test_fused_block_loop_matches_graph_loop(threads):
         srv.close()
     for k in range(len(specs)):
         assert _same(out[(-1, k)], out[(threads, k)]), f"request {k}"
+
+
+def test_autotuner_picks_a_measured_candidate():
+    _ensure_built()
+    from mdcraft_gb300 import tune
+    solv = SV.solvers("mixed")
+    specs = _specs(12, 50, seed=41, n_max=3000)
+    best, rates = tune.tune_serving(specs, solv, candidates=(256, 1024), sample=12, steps=50, slots=16,
+                                    use_cache=False)
+    assert best in (256, 1024)
+    assert set(rates) == {256, 1024} and all(r > 0 for r in rates.values())
+    assert rates[best] == max(rates.values())
