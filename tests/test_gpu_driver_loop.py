@@ -27,20 +27,38 @@ CASES = [(lambda: W.eam_cu_fcc(ncell=8), "mixed"), (lambda: W.lj_argon_fcc(jitte
          (lambda: W.lj_argon_fcc(jitter=0.01), "mixed")]
 
 
+def _host(x, pinned):
+    """A copy of x in page-locked memory (torch's pinned allocator) or in
+    ordinary memory."""
+    if not pinned:
+        return np.ascontiguousarray(np.array(x, dtype=np.float64))
+    import torch
+    t = torch.empty(np.shape(x), dtype=torch.float64, pin_memory=True)
+    a = t.numpy()
+    a[...] = x
+    return a, t
+
+
+@pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "pinned"])
 @pytest.mark.parametrize("make,prec", CASES, ids=["eam_mixed", "lj_fp64", "lj_mixed"])
-def test_run_host_equals_run_and_download(make, prec):
+def test_run_host_equals_run_and_download(make, prec, pinned):
     atoms, p, a = _pair(make, prec)
     a["stepper"].run(a["sys"], p["dt"], 50)
     ref = a["sys"].download()
     _, _, b = _pair(make, prec)
-    pos = np.ascontiguousarray(atoms["r"].copy())
-    vel = np.ascontiguousarray(atoms["v"].copy())
-    frc = np.zeros_like(pos)
+    keep = []
+    if pinned:
+        (pos, t1), (vel, t2), (frc, t3) = (_host(atoms["r"], True), _host(atoms["v"], True),
+                                            _host(np.zeros_like(atoms["r"]), True))
+        keep = [t1, t2, t3]
+    else:
+        pos, vel, frc = _host(atoms["r"], False), _host(atoms["v"], False), np.zeros((len(atoms), 3))
     b["stepper"].run_host(b["sys"], p["dt"], 50, pos, vel, frc)
     assert np.array_equal(pos, ref["r"])
     assert np.array_equal(vel, ref["v"])
     assert np.array_equal(frc, ref["f"])
     assert a["nl"].rebuilds() == b["nl"].rebuilds()
+    del keep
 
 
 @pytest.mark.parametrize("make", [lambda: W.eam_cu_fcc(ncell=8), lambda: W.lj_argon_fcc(jitter=0.01)],
