@@ -415,6 +415,13 @@ int pot_upload(mdg_potential* p, int device) {
     h32.insert(h32.end(), rc.begin(), rc.end());
     h32.insert(h32.end(), vc.begin(), vc.end());
     h32.insert(h32.end(), fc.begin(), fc.end());
+    // rho and V rows interleaved (32 bytes per interval) for the force pass,
+    // which reads both rows of one interval with one load
+    if (h32.size() & 1) h32.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int k = 0; k < p->Nr1; ++k) {
+        h32.push_back(rc[k]);
+        h32.push_back(vc[k]);
+    }
     MDG_CUDA(cudaSetDevice(device));
     MDG_CUDA(cudaMalloc(&p->d_tab64, h64.size() * sizeof(double)));
     MDG_CUDA(cudaMalloc(&p->d_tab32, h32.size() * sizeof(float4)));
@@ -455,6 +462,7 @@ static void fill_params(const mdg_potential* p, PotParams& P) {
         P.rho_c = p->d_tab32;
         P.v_c = p->d_tab32 + p->Nr1;
         P.f_c = p->d_tab32 + 2 * p->Nr1;
+        P.rv_c = p->d_tab32 + ((2 * (size_t)p->Nr1 + p->Nrh1 + 1) & ~size_t(1));
         P.inv_dr_f = (float)(1.0 / p->dr);
         P.inv_drh_f = (float)(1.0 / p->drh);
         P.dr1_f = (float)p->dr1;
