@@ -730,6 +730,7 @@ int upload_atoms_enqueue(mdg_system* sys, const mdg_atom* atoms, size_t n) {
     k_atoms_in<<<nblk(n), kBlock, 0, st>>>(xfer_args(sys), (const mdg_atom*)dbuf);
     MDG_LAUNCHED(sys->ctx);
     sys->force_prec = MDG_PREC_FP64;
+    sys->fp_ok = 0;  // nc replaced
     if (sys->have_list) {
         rc = launch_offsets(sys);
         if (rc) return rc;

@@ -140,6 +140,26 @@ __device__ __forceinline__ void visit64(const FArgs& A, int i, Fn&& fn) {
     }
 }
 
+// ---- F'(nc) of the current densities, FP64 -----------------------------------
+// The reference's force pass evaluates the embedding derivative from each
+// atom's nc as it is (EAM.cxx:465-497); the FP64 force kernel reads it from
+// Fp64, which the density pass writes. When nc changed since (prepare clears
+// it, an upload replaces it, a rebuild permutes the atoms), this pass brings
+// Fp64 back in line before a force pass.
+template <bool MULTI>
+__global__ void __launch_bounds__(kBlock) k_embed64(FArgs A, const PotSet* __restrict__ ps) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    const double nci = A.nc[i];
+    const int ki = MULTI ? (A.kind[i] & 3) : 0;
+    for (int b = 0; b < ps->nkinds; ++b) {
+        const PotParams& P = ps->p[ki][b];
+        double EF = 0, dF = 0;
+        if (P.type == 2) eam_embed64(P, nci, &EF, &dF, A.st);
+        A.Fp64[(size_t)b * A.np + i] = dF;
+    }
+}
+
 // ---- LJsCut / EAM forces, FP64 ------------------------------------------------
 template <bool MULTI>
 __global__ void __launch_bounds__(kBlock) k_forces64(FArgs A, const PotSet* __restrict__ ps) {
@@ -336,7 +356,14 @@ int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int preci
         if (stage == 0) {
             if (multi) k_density64<true><<<nb, kBlock, 0, st>>>(A, dps);
             else k_density64<false><<<nb, kBlock, 0, st>>>(A, dps);
+            sys->fp_ok = 1;
         } else {
+            if (ps.any_eam && !sys->fp_ok) {
+                if (multi) k_embed64<true><<<nb, kBlock, 0, st>>>(A, dps);
+                else k_embed64<false><<<nb, kBlock, 0, st>>>(A, dps);
+                MDG_LAUNCHED(ctx);
+                sys->fp_ok = 1;
+            }
             if (multi) k_forces64<true><<<nb, kBlock, 0, st>>>(A, dps);
             else k_forces64<false><<<nb, kBlock, 0, st>>>(A, dps);
         }

@@ -288,6 +288,7 @@ int launch_force_copy(mdg_system* sys, int to64) {
 
 int launch_zero(mdg_system* sys, int eam) {
     if (sys->n == 0) return MDG_OK;
+    if (eam) sys->fp_ok = 0;  // nc cleared
     int c = sys->cur;
     ZeroArgs Z;
     Z.fx = sys->f64[FX][c];

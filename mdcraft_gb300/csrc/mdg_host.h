@@ -118,6 +118,7 @@ struct mdg_system {
     float* Fp32 = nullptr;        // F'(rho) per kind column [nk][np] (mixed Multi)
     float* trig32 = nullptr;      // (skin/2)^2 per atom for the mixed half-skin test
     int force_prec = MDG_PREC_FP64;  // arithmetic of the forces last computed
+    int fp_ok = 0;                   // Fp64 = F'(nc) of the current nc (set by the FP64 density pass)
 
     // rebuild scratch
     uint32_t* key = nullptr;

@@ -504,6 +504,7 @@ static int nb_width(const mdg_system* sys) {
 
 int nlist_enqueue(mdg_system* sys) {
     mdg_ctx* ctx = sys->ctx;
+    sys->fp_ok = 0;  // the atoms are permuted; Fp64 is per slot
     cudaStream_t st = ctx->stream;
     const int n = (int)sys->n;
     if (n == 0) return MDG_OK;

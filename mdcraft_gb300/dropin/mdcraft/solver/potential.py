@@ -1,0 +1,41 @@
+"""mdcraft.solver.potential (python/mdcraft/solver/potential/_potential.cxx):
+EAM (arrays or a setfl file) and LJsCut on the GPU engine."""
+from __future__ import annotations
+
+import numpy as np
+
+import mdcraft_gb300 as _mdg
+
+
+class EAM:
+    def __init__(self, *args, **kw):
+        if (len(args) == 1 and isinstance(args[0], str)) or "filename" in kw:
+            self._p = _mdg.EAM.from_file(args[0] if args else kw["filename"])
+            return
+        names = ["Rcutoff", "pairPotential", "chargeDensity", "embeddingEnergy", "NrPot", "drPot", "NrEmb", "drEmb"]
+        a = dict(zip(names, args))
+        a.update(kw)
+        self._p = _mdg.EAM(a["Rcutoff"], np.asarray(a["embeddingEnergy"], dtype=np.float64),
+                           np.asarray(a["chargeDensity"], dtype=np.float64),
+                           np.asarray(a["pairPotential"], dtype=np.float64), int(a["NrPot"]), float(a["drPot"]),
+                           int(a["NrEmb"]), float(a["drEmb"]))
+
+    @property
+    def rcut(self) -> float:
+        return self._p.rcut()
+
+
+class LJsCut:
+    def __init__(self, a: float, s: float, rcut: float):
+        self._p = _mdg.LJsCut(a, s, rcut)
+
+    @property
+    def rcut(self) -> float:
+        return self._p.rcut()
+
+
+class Pair:
+    """Tabulated pair potential: not built on the GPU path."""
+
+    def __init__(self, *args, **kw):
+        raise NotImplementedError("the tabulated Pair potential is not built on the GPU path")
