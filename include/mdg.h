@@ -48,6 +48,7 @@ extern "C" {
 typedef struct mdg_ctx mdg_ctx;
 typedef struct mdg_system mdg_system;
 typedef struct mdg_potential mdg_potential;
+typedef struct mdg_thermostat mdg_thermostat;
 typedef struct mdg_solver mdg_solver;
 
 /* mdcraft::data::Atom, 208 bytes, V column-major (Eigen 3x3). */
@@ -163,6 +164,15 @@ int mdg_pot_eam_create(double rcut, const double* Femb, const double* Rho,
 /* EAM(std::string filename) (EAM.cxx:55-87): single-element setfl file;
  * unlike the reference, a missing or short file fails with MDG_ERR_IO. */
 int mdg_pot_eam_create_from_file(const char* path, mdg_potential** out);
+/* Pair(Rcutoff, Vpar, Nr1, dr) (mdcraft/solver/potential/pair.h:13-18,
+ * pair.cxx:15-33): tabulated r*phi(r) with the reference's spline; pair
+ * energy phi(r)/2 per side, force from d(r*phi)/dr. */
+int mdg_pot_pair_create(double rcut, const double* Vpar, int Nr1, double dr,
+                        mdg_potential** out);
+/* Pair(std::string filename) (pair.cxx:36-56): skips 4 lines, reads
+ * `Nr1 dr rcut` and Nr1 values of r*phi in eV*A; a missing or short file
+ * fails with MDG_ERR_IO. */
+int mdg_pot_pair_create_from_file(const char* path, mdg_potential** out);
 int mdg_pot_destroy(mdg_potential* pot);
 /* Base::rcut() (mdcraft/solver/potential/base.h:37). */
 int mdg_pot_rcut(mdg_potential* pot, double* rcut);
@@ -188,6 +198,43 @@ int mdg_solver_forces(mdg_solver* s, mdg_system* sys);
 int mdg_solver_virials(mdg_solver* s, mdg_system* sys);
 /* All of solver.stages in order (single.cxx:23-35). */
 int mdg_solver_stages(mdg_solver* s, mdg_system* sys);
+
+/* ---- thermostats ------------------------------------------------------------ */
+/* thermostat::Langevin(beta, temperature, time_step, heat_x, heat_y, heat_z,
+ * Ux, Uy, Uz, xmin, xmax) (mdcraft/solver/thermostat/langevin.h:17-29):
+ * during the force stage each atom with xmin <= x <= xmax gets
+ * f += heat * (sqrt(m) * N(0, sigma) - (v - U) * beta * m),
+ * sigma = sqrt(2 beta Kb T / time_step) (langevin.cxx:21-42). The normals
+ * come from Philox4x32-10 keyed by `seed` with the counter {caller index of
+ * the atom, call number of the system, term index, 0} (the reference seeds
+ * std::default_random_engine from std::random_device, so its runs do not
+ * repeat; these do). */
+typedef struct mdg_langevin {
+    double beta, temperature, time_step;
+    int32_t heat[3];
+    int32_t _pad;
+    double U[3];
+    double xmin, xmax;
+    uint64_t seed;
+} mdg_langevin;
+int mdg_thermo_langevin_create(const mdg_langevin* params, mdg_thermostat** out);
+/* Langevin::set_friction / set_temperature / set_average_velocity /
+ * set_heating_axes / set_dimensions (langevin.cxx:44-76) in one call, and
+ * the getters friction() ... xmax() (langevin.cxx:78-82). */
+int mdg_thermo_langevin_set(mdg_thermostat* t, const mdg_langevin* params);
+int mdg_thermo_langevin_get(mdg_thermostat* t, mdg_langevin* params);
+/* thermostat::Compound (mdcraft/solver/thermostat/compound.h:12-24): its
+ * parts apply in the order they were added. */
+int mdg_thermo_compound_create(mdg_thermostat** out);
+int mdg_thermo_compound_add(mdg_thermostat* compound, mdg_thermostat* part);
+int mdg_thermo_destroy(mdg_thermostat* t);
+/* The thermostat argument of Single / Multi (single.h:37-42, multi.h:42-47);
+ * NULL restores the no-op thermostat. The solver keeps the pointer. */
+int mdg_solver_set_thermostat(mdg_solver* s, mdg_thermostat* t);
+/* Thermostat applications on this system so far (the Philox call number
+ * of the next one), and a way to set it (to resume a run). */
+int mdg_system_thermo_calls(mdg_system* sys, uint32_t* calls);
+int mdg_system_set_thermo_calls(mdg_system* sys, uint32_t calls);
 
 /* ---- stepper ----------------------------------------------------------------------- */
 /* stepper::Verlet::make_step(atoms, nlist, dt) (verlet.cxx:36-48). */

@@ -18,7 +18,8 @@ import numpy as np
 
 __all__ = [
     "ATOM_DTYPE", "Context", "Domain", "System", "VerletList", "LJsCut", "EAM", "Single", "Multi", "Verlet",
-    "MDGError", "new_atoms", "lib", "lib_path", "PREC_FP64", "PREC_MIXED", "Server",
+    "MDGError", "new_atoms", "lib", "lib_path", "PREC_FP64", "PREC_MIXED", "Server", "Pair", "Langevin",
+    "Compound",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -99,6 +100,14 @@ def lib():
         "mdg_server_result": ([vp, C.c_uint64, vp, sz, vp], ip),
         "mdg_server_stats_get": ([vp, vp], ip), "mdg_server_clock": ([vp, C.POINTER(C.c_double)], ip),
         "mdg_server_footprint": ([sz, ip], sz),
+        "mdg_pot_pair_create": ([dp, vp, ip, dp, pp], ip),
+        "mdg_pot_pair_create_from_file": ([C.c_char_p, pp], ip),
+        "mdg_thermo_langevin_create": ([vp, pp], ip), "mdg_thermo_langevin_set": ([vp, vp], ip),
+        "mdg_thermo_langevin_get": ([vp, vp], ip), "mdg_thermo_compound_create": ([pp], ip),
+        "mdg_thermo_compound_add": ([vp, vp], ip), "mdg_thermo_destroy": ([vp], ip),
+        "mdg_solver_set_thermostat": ([vp, vp], ip),
+        "mdg_system_thermo_calls": ([vp, C.POINTER(C.c_uint32)], ip),
+        "mdg_system_set_thermo_calls": ([vp, C.c_uint32], ip),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -234,6 +243,14 @@ class System:
     def set_velocities(self, xyz):
         self._vec(lib().mdg_system_set_velocities, xyz)
 
+    def thermo_calls(self) -> int:
+        v = C.c_uint32()
+        _check(lib().mdg_system_thermo_calls(self.h, C.byref(v)))
+        return v.value
+
+    def set_thermo_calls(self, calls: int):
+        _check(lib().mdg_system_set_thermo_calls(self.h, int(calls)))
+
     def measure(self) -> dict:
         """FP64 totals of measure_state (test/cxx/support/md_test_utils.h:214-239)."""
         buf = (C.c_double * 8)()
@@ -353,9 +370,130 @@ class EAM(_Pot):
         return obj
 
 
+class Pair(_Pot):
+    """Pair(Rcutoff, pairPotential, NrPot, drPot) (pair.h:13-18): tabulated
+    r*phi(r) on a uniform grid."""
+
+    def __init__(self, rcut, Vpar, Nr1, dr):
+        V = np.ascontiguousarray(Vpar, dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib().mdg_pot_pair_create(rcut, _ptr(V), int(Nr1), dr, C.byref(h)))
+        self.h = h
+
+    @classmethod
+    def from_file(cls, path: str) -> "Pair":
+        """Pair(std::string filename) (pair.cxx:36-56)."""
+        obj = cls.__new__(cls)
+        h = C.c_void_p()
+        _check(lib().mdg_pot_pair_create_from_file(path.encode(), C.byref(h)))
+        obj.h = h
+        return obj
+
+
+class _LangevinParams(C.Structure):
+    _fields_ = [("beta", C.c_double), ("temperature", C.c_double), ("time_step", C.c_double),
+                ("heat", C.c_int32 * 3), ("_pad", C.c_int32), ("U", C.c_double * 3), ("xmin", C.c_double),
+                ("xmax", C.c_double), ("seed", C.c_uint64)]
+
+
+class _Thermo:
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().mdg_thermo_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+class Langevin(_Thermo):
+    """thermostat::Langevin(beta, temperature, time_step, heat_x, heat_y,
+    heat_z, Ux, Uy, Uz, xmin, xmax) (langevin.h:17-29); `seed` keys the
+    Philox stream of the random force."""
+
+    def __init__(self, beta, temperature, time_step, heat_x=1, heat_y=1, heat_z=1, Ux=0.0, Uy=0.0, Uz=0.0,
+                 xmin=-1e15, xmax=1e15, seed=0):
+        p = _LangevinParams(beta, temperature, time_step, (C.c_int32 * 3)(heat_x, heat_y, heat_z), 0,
+                            (C.c_double * 3)(Ux, Uy, Uz), xmin, xmax, seed)
+        h = C.c_void_p()
+        _check(lib().mdg_thermo_langevin_create(C.byref(p), C.byref(h)))
+        self.h = h
+
+    def _get(self) -> _LangevinParams:
+        p = _LangevinParams()
+        _check(lib().mdg_thermo_langevin_get(self.h, C.byref(p)))
+        return p
+
+    def _set(self, p: _LangevinParams):
+        _check(lib().mdg_thermo_langevin_set(self.h, C.byref(p)))
+
+    def set_friction(self, beta):
+        p = self._get()
+        p.beta = beta
+        self._set(p)
+
+    def set_temperature(self, T):
+        p = self._get()
+        p.temperature = T
+        self._set(p)
+
+    def set_average_velocity(self, U):
+        p = self._get()
+        p.U = (C.c_double * 3)(*U)
+        self._set(p)
+
+    def set_heating_axes(self, heat_x=1, heat_y=1, heat_z=1):
+        p = self._get()
+        p.heat = (C.c_int32 * 3)(heat_x, heat_y, heat_z)
+        self._set(p)
+
+    def set_dimensions(self, xmin, xmax):
+        p = self._get()
+        p.xmin, p.xmax = xmin, xmax
+        self._set(p)
+
+    def friction(self):
+        return self._get().beta
+
+    def temperature(self):
+        return self._get().temperature
+
+    def average_velocity(self):
+        return np.array(self._get().U[:])
+
+    def xmin(self):
+        return self._get().xmin
+
+    def xmax(self):
+        return self._get().xmax
+
+
+class Compound(_Thermo):
+    """thermostat::Compound (compound.h:12-24): parts apply in order."""
+
+    def __init__(self, *parts):
+        h = C.c_void_p()
+        _check(lib().mdg_thermo_compound_create(C.byref(h)))
+        self.h = h
+        self._parts = []
+        for q in parts:
+            self.add(q)
+
+    def add(self, part: _Thermo):
+        self._parts.append(part)
+        _check(lib().mdg_thermo_compound_add(self.h, part.h))
+
+
 class _Solver:
     def __init__(self):
         self._pots = []
+        self._thermo = None
+
+    def set_thermostat(self, thermo: "_Thermo | None"):
+        """The thermostat argument of Single / Multi (None: no thermostat)."""
+        self._thermo = thermo
+        _check(lib().mdg_solver_set_thermostat(self.h, thermo.h if thermo is not None else None))
+        return self
 
     def num_stages(self) -> int:
         v = C.c_int()

@@ -32,7 +32,8 @@ int cuda_status(cudaError_t e, const char* what) {
     return MDG_ERR_CUDA;
 }
 
-int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int precision, int stage);
+int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int precision, int stage,
+                 const ThermoDev* th);
 int launch_virials(mdg_system* sys, const PotSet* dps, const PotSet& ps);
 int launch_drift(mdg_system* sys, double dt, int precision, double pot_rcut, int periodic_boundary, int drift,
                  int check);
@@ -398,7 +399,7 @@ static void cubic_coeffs(const std::vector<double>& y, const std::vector<double>
 }
 
 int pot_upload(mdg_potential* p, int device) {
-    if (p->type != 2 || p->device == device) return MDG_OK;
+    if (p->type < POT_EAM || p->device == device) return MDG_OK;
     if (p->d_tab64) cudaFree(p->d_tab64);
     if (p->d_tab32) cudaFree(p->d_tab32);
     p->d_tab64 = nullptr;
@@ -431,8 +432,17 @@ int pot_upload(mdg_potential* p, int device) {
     return MDG_OK;
 }
 
-static void fill_params(const mdg_potential* p, PotParams& P) {
+// Table-less slots (no potential, LJsCut) point every table at `z64` /
+// `z32`, kZeroRows rows of zeros, so that no kernel load sees a null pointer.
+static void zero_tables(PotParams& P, const double* z64, const float4* z32) {
+    P.Rho = P.dRho = P.Vpar = P.dVpar = P.Femb = P.dFemb = z64;
+    P.rho_c = P.v_c = P.f_c = P.rv_c = z32;
+}
+
+static void fill_params(const mdg_potential* p, PotParams& P, const double* z64, const float4* z32) {
     memset(&P, 0, sizeof(P));
+    zero_tables(P, z64, z32);
+    if (!p) return;
     P.type = p->type;
     P.R2cut = p->rcut * p->rcut;
     P.r2cut_f = (float)P.R2cut;
@@ -445,7 +455,7 @@ static void fill_params(const mdg_potential* p, PotParams& P) {
         P.lj1_f = (float)p->lj1;
         P.lj2_f = (float)p->lj2;
         P.mhf_f = (float)(-0.5 * p->factor);
-    } else if (p->type == 2) {
+    } else if (p->type >= POT_EAM) {
         size_t nr = (size_t)p->Nr1 + 1, nh = (size_t)p->Nrh1 + 1;
         P.Nr1 = p->Nr1;
         P.Nrh1 = p->Nrh1;
@@ -474,13 +484,24 @@ static void fill_params(const mdg_potential* p, PotParams& P) {
 
 using namespace mdg;
 
-// solver + system binding: the PotSet lives in device memory, one per
-// (solver, device); rebuilt when potentials change.
+// solver + system binding: the PotSet, the thermostat's terms and the zero
+// table live in one device block per (solver, device); the PotSet is
+// rebuilt when potentials change, the terms whenever they differ from the
+// last copy (before any capture, so a graph reads the current values).
+struct SolverBlob {
+    PotSet ps;
+    ThermoDev th;
+    alignas(32) float4 z32[2 * kZeroRows];
+    double z64[2 * kZeroRows];
+};
+
 struct SolverDev {
     PotSet host;
-    PotSet* dev = nullptr;
+    PotSet* dev = nullptr;  // start of the SolverBlob
     int device = -1;
     int version = -1;
+    ThermoDev th_host{};
+    int th_valid = 0;
 };
 
 struct mdg_solver_ext {
@@ -488,6 +509,8 @@ struct mdg_solver_ext {
     SolverDev d;
     int version = 0;
 };
+
+static SolverBlob* blob_of(SolverDev& d) { return reinterpret_cast<SolverBlob*>(d.dev); }
 
 static mdg_solver_ext* ext(mdg_solver* s) { return reinterpret_cast<mdg_solver_ext*>(s); }
 
@@ -500,31 +523,46 @@ int potset_build(mdg_solver* s, mdg_system* sys, PotSet* out) {
         if (out) *out = e->d.host;
         return MDG_OK;
     }
+    if (!e->d.dev || e->d.device != dev) {
+        if (e->d.dev) cudaFree(e->d.dev);
+        e->d.dev = nullptr;
+        e->d.th_valid = 0;
+        MDG_CUDA(cudaMalloc(&e->d.dev, sizeof(SolverBlob)));
+        MDG_CUDA(cudaMemset(e->d.dev, 0, sizeof(SolverBlob)));
+    }
+    SolverBlob* b = blob_of(e->d);
     PotSet ps;
     memset(&ps, 0, sizeof(ps));
     ps.nkinds = s->multi ? s->nkinds : 1;
     ps.multi = s->multi;
     ps.periodic = s->periodic;
-    for (int i = 0; i < ps.nkinds; ++i)
-        for (int j = 0; j < ps.nkinds; ++j) {
-            mdg_potential* p = s->pot[i][j];
-            if (!p) continue;
-            int rc = pot_upload(p, dev);
-            if (rc) return rc;
-            fill_params(p, ps.p[i][j]);
-            if (p->type == 2) ps.any_eam = 1;
+    for (int i = 0; i < kMaxKinds; ++i)
+        for (int j = 0; j < kMaxKinds; ++j) {
+            mdg_potential* p = i < ps.nkinds && j < ps.nkinds ? s->pot[i][j] : nullptr;
+            if (p) {
+                int rc = pot_upload(p, dev);
+                if (rc) return rc;
+                if (p->type == POT_EAM) ps.any_eam = 1;
+                if (p->type == POT_LJCUT) ps.any_lj = 1;
+                if (p->type == POT_TAB) ps.any_tab = 1;
+            }
+            fill_params(p, ps.p[i][j], b->z64, b->z32);
         }
-    if (!e->d.dev || e->d.device != dev) {
-        if (e->d.dev) cudaFree(e->d.dev);
-        e->d.dev = nullptr;
-        MDG_CUDA(cudaMalloc(&e->d.dev, sizeof(PotSet)));
-    }
     MDG_CUDA(cudaMemcpy(e->d.dev, &ps, sizeof(PotSet), cudaMemcpyHostToDevice));
     e->d.host = ps;
     e->d.device = dev;
     e->d.version = e->version;
     if (out) *out = ps;
     return MDG_OK;
+}
+}  // namespace mdg
+
+namespace mdg {
+// Device terms of the solver's thermostat (null without one); refreshed in
+// check_ready, read by the launches.
+const ThermoDev* thermo_of(mdg_solver* s) {
+    if (!s->thermo) return nullptr;
+    return &blob_of(ext(s)->d)->th;
 }
 }  // namespace mdg
 
@@ -1096,6 +1134,71 @@ int mdg_pot_eam_create_from_file(const char* path, mdg_potential** out) {
     return mdg_pot_eam_create(rcut, F.data(), R.data(), V.data(), Nr1, dr, Nrh1, drh, out);
 }
 
+int mdg_pot_pair_create(double rcut, const double* Vpar, int Nr1, double dr, mdg_potential** out) {
+    // Pair::Pair(arrays) (pair.cxx:15-33). The table rides the EAM table
+    // layout with zero rho and embedding rows, so the force kernels of a
+    // Multi solver that mixes it with EAM pairs use one code path.
+    if (!out || !Vpar || Nr1 < 3 || !(dr > 0)) {
+        set_error("invalid Pair table");
+        return MDG_ERR_INVALID;
+    }
+    mdg_potential* p = new mdg_potential();
+    p->type = POT_TAB;
+    p->rcut = rcut;
+    p->Nr1 = Nr1;
+    p->Nrh1 = 3;
+    p->dr = dr;
+    p->drh = 1.0;
+    p->dr1 = 1.0 / dr;
+    p->drh1 = 1.0;
+    p->Vpar.assign(Vpar, Vpar + Nr1);
+    p->dVpar.assign(Nr1 + 1, 0.0);
+    init_spline(p->Vpar.data(), p->dVpar.data(), p->dr1, Nr1, 1);
+    // one padding element: the reference reads Vpar[N1 + 1] for N1 = Nr1 - 1
+    p->Vpar.push_back(p->Vpar.back());
+    p->dVpar[Nr1] = p->dVpar[Nr1 - 1];
+    p->Rho.assign(Nr1 + 1, 0.0);
+    p->dRho.assign(Nr1 + 1, 0.0);
+    p->Femb.assign(4, 0.0);
+    p->dFemb.assign(4, 0.0);
+    *out = p;
+    return MDG_OK;
+}
+
+int mdg_pot_pair_create_from_file(const char* path, mdg_potential** out) {
+    // Pair::Pair(std::string) (pair.cxx:36-56)
+    if (!path || !out) return MDG_ERR_INVALID;
+    std::ifstream file(path);
+    if (!file.is_open()) {
+        set_error(std::string("cannot open Pair file: ") + path);
+        return MDG_ERR_IO;
+    }
+    const double N_a = 6.02214076e+23, Qelectron = 1.602176634e-19;
+    const double UnMass = 1e-3 / N_a, UnLeng = 1e-9, UnTime = 1e-12;
+    const double UnEnrg = UnMass * (UnLeng / UnTime) * (UnLeng / UnTime);
+    std::string line;
+    for (int k = 0; k < 4; ++k) std::getline(file, line);
+    int Nr1 = 0;
+    double dr = 0, rcut = 0;
+    file >> Nr1 >> dr >> rcut;
+    if (!file || Nr1 < 3) {
+        set_error("malformed Pair file header");
+        return MDG_ERR_IO;
+    }
+    dr /= 10;
+    rcut /= 10;
+    std::vector<double> V(Nr1);
+    for (int i = 0; i < Nr1; ++i) {
+        file >> V[i];
+        V[i] *= Qelectron / (10 * UnEnrg);
+    }
+    if (!file) {
+        set_error("Pair file ended before the table was read");
+        return MDG_ERR_IO;
+    }
+    return mdg_pot_pair_create(rcut, V.data(), Nr1, dr, out);
+}
+
 int mdg_pot_destroy(mdg_potential* p) {
     if (!p) return MDG_ERR_INVALID;
     if (p->d_tab64) cudaFree(p->d_tab64);
@@ -1112,6 +1215,7 @@ int mdg_pot_rcut(mdg_potential* p, double* rcut) {
 
 // ---- solvers ----------------------------------------------------------------
 static void set_stages(mdg_solver* s, int type, bool first) {
+    if (type == POT_TAB) type = POT_LJCUT;  // both potential::type::pair
     if (first) {
         if (type == 1) {
             s->nstages = 1;
@@ -1163,6 +1267,126 @@ int mdg_solver_add_potential(mdg_solver* s, int i, int j, mdg_potential* pot) {
     return MDG_OK;
 }
 
+// ---- thermostats ----------------------------------------------------------
+static bool langevin_ok(const mdg_langevin* p) {
+    return p && p->beta >= 0 && p->temperature >= 0 && p->time_step > 0;
+}
+
+int mdg_thermo_langevin_create(const mdg_langevin* params, mdg_thermostat** out) {
+    if (!out || !langevin_ok(params)) {
+        set_error("Langevin: need beta >= 0, temperature >= 0, time_step > 0");
+        return MDG_ERR_INVALID;
+    }
+    mdg_thermostat* t = new mdg_thermostat();
+    t->p = *params;
+    *out = t;
+    return MDG_OK;
+}
+
+int mdg_thermo_langevin_set(mdg_thermostat* t, const mdg_langevin* params) {
+    if (!t || t->compound || !langevin_ok(params)) return MDG_ERR_INVALID;
+    t->p = *params;
+    return MDG_OK;
+}
+
+int mdg_thermo_langevin_get(mdg_thermostat* t, mdg_langevin* params) {
+    if (!t || t->compound || !params) return MDG_ERR_INVALID;
+    *params = t->p;
+    return MDG_OK;
+}
+
+int mdg_thermo_compound_create(mdg_thermostat** out) {
+    if (!out) return MDG_ERR_INVALID;
+    mdg_thermostat* t = new mdg_thermostat();
+    t->compound = 1;
+    *out = t;
+    return MDG_OK;
+}
+
+int mdg_thermo_compound_add(mdg_thermostat* c, mdg_thermostat* part) {
+    if (!c || !part || !c->compound || part == c) return MDG_ERR_INVALID;
+    c->parts.push_back(part);
+    return MDG_OK;
+}
+
+int mdg_thermo_destroy(mdg_thermostat* t) {
+    if (!t) return MDG_ERR_INVALID;
+    delete t;
+    return MDG_OK;
+}
+
+// Langevin terms of a thermostat tree in application order.
+static int thermo_flatten(const mdg_thermostat* t, ThermoDev& out, int depth) {
+    if (depth > 16) {
+        set_error("thermostat compound nests too deep");
+        return MDG_ERR_INVALID;
+    }
+    if (!t->compound) {
+        if (out.n >= kMaxThermo) {
+            set_error("more than 8 Langevin terms in one thermostat");
+            return MDG_ERR_INVALID;
+        }
+        const mdg_langevin& p = t->p;
+        LangevinTerm& L = out.t[out.n++];
+        L.beta = p.beta;
+        // sigma = sqrt(2 beta Kb T / dt) (langevin.cxx:24), Kb of thermostat/base.h:10
+        L.sigma = std::sqrt(2.0 * p.beta * 0.008314462175 * p.temperature / p.time_step);
+        for (int k = 0; k < 3; ++k) {
+            L.heat[k] = (double)p.heat[k];
+            L.U[k] = p.U[k];
+        }
+        L.xmin = p.xmin;
+        L.xmax = p.xmax;
+        L.seed = p.seed;
+        return MDG_OK;
+    }
+    for (const mdg_thermostat* q : t->parts) {
+        int rc = thermo_flatten(q, out, depth + 1);
+        if (rc) return rc;
+    }
+    return MDG_OK;
+}
+
+int mdg_solver_set_thermostat(mdg_solver* s, mdg_thermostat* t) {
+    if (!s) return MDG_ERR_INVALID;
+    s->thermo = t;
+    ext(s)->version++;  // captured graphs gain or lose the thermostat pass
+    return MDG_OK;
+}
+
+static int thermo_sync(mdg_solver* s) {
+    if (!s->thermo) return MDG_OK;
+    mdg_solver_ext* e = ext(s);
+    ThermoDev h;
+    memset(&h, 0, sizeof(h));
+    int rc = thermo_flatten(s->thermo, h, 0);
+    if (rc) return rc;
+    if (e->d.th_valid && memcmp(&h, &e->d.th_host, sizeof(h)) == 0) return MDG_OK;
+    MDG_CUDA(cudaMemcpy(&blob_of(e->d)->th, &h, sizeof(h), cudaMemcpyHostToDevice));
+    e->d.th_host = h;
+    e->d.th_valid = 1;
+    return MDG_OK;
+}
+
+int mdg_system_thermo_calls(mdg_system* sys, uint32_t* calls) {
+    if (!sys || !calls) return MDG_ERR_INVALID;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    MDG_CUDA(cudaMemcpyAsync(calls, &sys->dstat->therm_calls, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                             sys->ctx->stream));
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    return MDG_OK;
+}
+
+int mdg_system_set_thermo_calls(mdg_system* sys, uint32_t calls) {
+    if (!sys) return MDG_ERR_INVALID;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    sys->hstat->therm_calls = calls;
+    MDG_CUDA(cudaMemcpyAsync(&sys->dstat->therm_calls, &sys->hstat->therm_calls, sizeof(uint32_t),
+                             cudaMemcpyHostToDevice, sys->ctx->stream));
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
+    return MDG_OK;
+}
+
 int mdg_solver_destroy(mdg_solver* s) {
     if (!s) return MDG_ERR_INVALID;
     mdg_solver_ext* e = ext(s);
@@ -1206,7 +1430,9 @@ static int check_ready(mdg_solver* s, mdg_system* sys, PotSet* ps) {
                     return MDG_ERR_STATE;
                 }
     }
-    return potset_build(s, sys, ps);
+    int rc = potset_build(s, sys, ps);
+    if (rc) return rc;
+    return thermo_sync(s);
 }
 
 static double pot_rcut_of(mdg_solver* s) { return s->multi ? -1.0 : s->pot[0][0]->rcut; }
@@ -1225,7 +1451,7 @@ int mdg_solver_prepare(mdg_solver* s, mdg_system* sys) {
 
 static int stage_impl(mdg_solver* s, mdg_system* sys, const PotSet& ps, int stage, int prec) {
     mdg_solver_ext* e = ext(s);
-    int rc = launch_stage(sys, e->d.dev, ps, prec, stage);
+    int rc = launch_stage(sys, e->d.dev, ps, prec, stage, thermo_of(s));
     if (rc) return rc;
     if (stage == 1) sys->force_prec = prec;
     return MDG_OK;
@@ -1271,11 +1497,11 @@ int mdg_solver_virials(mdg_solver* s, mdg_system* sys) {
     if (rc) return rc;
     mdg_solver_ext* e = ext(s);
     if (ps.any_eam && s->precision == MDG_PREC_MIXED) {
-        rc = launch_stage(sys, e->d.dev, ps, MDG_PREC_FP64, 0);
+        rc = launch_stage(sys, e->d.dev, ps, MDG_PREC_FP64, 0, nullptr);
         if (rc) return rc;
     } else if (ps.any_eam) {
         // F'(nc) of the current densities (the reference recomputes them)
-        rc = launch_stage(sys, e->d.dev, ps, MDG_PREC_FP64, 0);
+        rc = launch_stage(sys, e->d.dev, ps, MDG_PREC_FP64, 0, nullptr);
         if (rc) return rc;
     }
     rc = launch_virials(sys, e->d.dev, ps);
@@ -1297,7 +1523,7 @@ static int step_impl(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt
     rc = launch_drift(sys, dt, prec, pot_rcut_of(s), s->periodic, 1, 1);
     if (rc) return rc;
     for (int k = 0; k < s->nstages; ++k) {
-        rc = launch_stage(sys, e->d.dev, ps, prec, s->stages[k]);
+        rc = launch_stage(sys, e->d.dev, ps, prec, s->stages[k], thermo_of(s));
         if (rc) return rc;
     }
     sys->force_prec = prec;
@@ -1462,7 +1688,8 @@ static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, dou
     l0 = ctx->launches;
     MDG_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int rc = launch_drift(sys, dt, prec, s->multi ? -1.0 : s->pot[0][0]->rcut, s->periodic, 1, 1);
-    for (int q = 0; rc == 0 && q < s->nstages; ++q) rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q]);
+    for (int q = 0; rc == 0 && q < s->nstages; ++q)
+        rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q], thermo_of(s));
     if (rc == 0) rc = launch_kick(sys, dt, prec);
     if (rc == 0) {
         k_rebuild_cond<<<1, 32, 0, st>>>(hrb, sys->dstat);
@@ -1754,7 +1981,7 @@ int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
         }
         for (int q = 0; q < s->nstages; ++q) {
             cudaEvent_t t0 = timer_begin(sys->ctx);
-            rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q]);
+            rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q], thermo_of(s));
             timer_end(sys->ctx, s->stages[q] == 0 ? MDG_TIME_DENSITY : MDG_TIME_FORCES, t0);
             if (rc) goto done;
         }

@@ -98,6 +98,28 @@ __device__ __forceinline__ double eam_ff64(const PotParams& P, double R2, double
     return (AdF * FF + (DV * R1 - VR) / R2) / R1;
 }
 
+// Force(r)/r of a tabulated Pair and its energy term V(r)/(2r)
+// (pair.cxx:316-346, 228-314).
+__device__ __forceinline__ double tab_ff64(const PotParams& P, double R2, double* Vr) {
+    double R1 = sqrt(R2);
+    double RN = R1 * P.dr1;
+    int N1 = (int)trunc(RN);
+    double VR = 0.0, DV = 0.0;
+    if (N1 < P.Nr1) {
+        VR = N1;
+        DV = RN - VR;
+        RN = R1 - VR * P.dr;
+        VR = (P.Vpar[N1 + 1] - P.Vpar[N1]) * P.dr1;
+        double aa = (P.dVpar[N1 + 1] - VR) - (VR - P.dVpar[N1]);
+        double bb = aa - (VR - P.dVpar[N1]);
+        aa = aa * DV;
+        VR = P.Vpar[N1] + RN * (P.dVpar[N1] + DV * (aa - bb));
+        DV = P.dVpar[N1] + 2.0 * DV * (1.5 * aa - bb);
+    }
+    if (Vr) *Vr = 0.5 * VR / R1;
+    return ((DV * R1 - VR) / R2) / R1;
+}
+
 __device__ __forceinline__ double lj_pref64(const PotParams& P, double r2) {
     double r2inv = 1.0 / r2;
     double r6inv = r2inv * r2inv * r2inv;
@@ -177,6 +199,8 @@ __global__ void __launch_bounds__(kBlock) k_forces64(FArgs A, const PotSet* __re
         } else if (P.type == 2) {
             double AdF = A.Fp64[(size_t)ki * A.np + j] + A.Fp64[(size_t)kj * A.np + i];
             pref = eam_ff64(P, r2, AdF, nullptr);
+        } else if (P.type == POT_TAB) {
+            pref = tab_ff64(P, r2, nullptr);
         } else {
             return;
         }
@@ -259,6 +283,12 @@ __global__ void __launch_bounds__(kBlock) k_virials64(FArgs A, const PotSet* __r
             for (int c = 0; c < 3; ++c)
                 for (int r = 0; r < 3; ++r) M[r + 3 * c] += h * d[r] * d[c];
             Ep += Vr;
+        } else if (P.type == POT_TAB) {
+            double Vr;
+            double h = 0.5 * tab_ff64(P, r2, &Vr);
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 3; ++r) M[r + 3 * c] += h * d[r] * d[c];
+            Ep += Vr;
         }
     });
     A.Ep[i] = Ep;
@@ -300,6 +330,93 @@ __global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_eam_mixed(FArgs A, 
     if (i < A.n) eam_mixed_one<MULTI>(A, ps, i);
 }
 
+
+template <bool MULTI, int FORM>
+__global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_tab_mixed(FArgs A, const PotSet* __restrict__ ps) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < A.n) tab_mixed_one<MULTI, FORM>(A, ps, i);
+}
+
+// ---- Langevin thermostat (langevin.cxx:29-42) ----------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): ten rounds of two
+// 32x32->64 multiplications, key bumped by the Weyl constants.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k.x += 0x9E3779B9u;
+            k.y += 0xBB67AE85u;
+        }
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    }
+    return c;
+}
+
+struct ThermoArgs {
+    int n;
+    const double *rx, *vx, *vy, *vz, *m;
+    const uint32_t* orig;
+    double *fx, *fy, *fz;  // FP64 form
+    float *gx, *gy, *gz;   // mixed form
+    const DevStatus* st;
+};
+
+// f += heat * (sqrt(m) * sigma * z - (v - U) * beta * m) for every term whose
+// x range holds the atom; z = three Box-Muller normals of one Philox block
+// with counter {caller index, call number, term, 0}.
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_langevin(ThermoArgs A, const ThermoDev* __restrict__ th) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    const int nt = th->n;
+    if (nt == 0) return;
+    const uint32_t call = A.st->therm_calls;
+    const double x = A.rx[i], m = A.m[i];
+    const double v[3] = {A.vx[i], A.vy[i], A.vz[i]};
+    const double sqrt_mass = sqrt(m);
+    double f[3] = {0.0, 0.0, 0.0};
+    if (!MIXED) {
+        f[0] = A.fx[i];
+        f[1] = A.fy[i];
+        f[2] = A.fz[i];
+    }
+    const uint32_t atom = A.orig[i];
+    for (int q = 0; q < nt && q < kMaxThermo; ++q) {
+        const LangevinTerm& L = th->t[q];
+        if (x < L.xmin || x > L.xmax) continue;
+        const uint4 b = philox4x32_10(make_uint4(atom, call, (uint32_t)q, 0u),
+                                      make_uint2((uint32_t)L.seed, (uint32_t)(L.seed >> 32)));
+        const double k32 = 2.3283064365386962890625e-10;  // 2^-32
+        const double two_pi = 6.283185307179586476925;
+        const double ra = sqrt(-2.0 * log(((double)b.x + 0.5) * k32));
+        const double rb = sqrt(-2.0 * log(((double)b.z + 0.5) * k32));
+        const double a1 = two_pi * (((double)b.y + 0.5) * k32);
+        const double a3 = two_pi * (((double)b.w + 0.5) * k32);
+        const double z[3] = {ra * cos(a1), ra * sin(a1), rb * cos(a3)};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double tf = __dmul_rn(__dadd_rn(__dmul_rn(z[k], L.sigma), 0.0), sqrt_mass);
+            tf = __dsub_rn(tf, __dmul_rn(__dmul_rn(__dsub_rn(v[k], L.U[k]), L.beta), m));
+            tf = __dmul_rn(tf, L.heat[k]);
+            f[k] = __dadd_rn(f[k], tf);
+        }
+    }
+    if (MIXED) {
+        A.gx[i] += (float)f[0];
+        A.gy[i] += (float)f[1];
+        A.gz[i] += (float)f[2];
+    } else {
+        A.fx[i] = f[0];
+        A.fy[i] = f[1];
+        A.fz[i] = f[2];
+    }
+}
+
+__global__ void k_thermo_tick(DevStatus* st) {
+    if (threadIdx.x == 0) st->therm_calls += 1u;
+}
 
 // ---------------------------------------------------------------------------
 // host side
@@ -344,8 +461,39 @@ FArgs force_args(mdg_system* sys) {
     return A;
 }
 
-// stage: 0 = charge (density), 1 = forces
-int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int precision, int stage) {
+// Thermostat pass after the force stage (pair.cxx:81), then the call
+// counter's increment.
+static int launch_thermostat(mdg_system* sys, const ThermoDev* th, int precision) {
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    int c = sys->cur;
+    ThermoArgs T;
+    T.n = (int)sys->n;
+    T.rx = sys->f64[RX][c];
+    T.vx = sys->f64[VX][c];
+    T.vy = sys->f64[VY][c];
+    T.vz = sys->f64[VZ][c];
+    T.m = sys->f64[MASS][c];
+    T.orig = sys->u32[ORIG][c];
+    T.fx = sys->f64[FX][c];
+    T.fy = sys->f64[FY][c];
+    T.fz = sys->f64[FZ][c];
+    T.gx = sys->f32[0][c];
+    T.gy = sys->f32[1][c];
+    T.gz = sys->f32[2][c];
+    T.st = sys->dstat;
+    int nb = nblk(sys->n);
+    if (precision == MDG_PREC_FP64) k_langevin<false><<<nb, kBlock, 0, st>>>(T, th);
+    else k_langevin<true><<<nb, kBlock, 0, st>>>(T, th);
+    MDG_LAUNCHED(ctx);
+    k_thermo_tick<<<1, 32, 0, st>>>(sys->dstat);
+    MDG_LAUNCHED(ctx);
+    return MDG_OK;
+}
+
+// stage: 0 = charge (density), 1 = forces (then the thermostat, if any)
+int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int precision, int stage,
+                 const ThermoDev* th) {
     mdg_ctx* ctx = sys->ctx;
     cudaStream_t st = ctx->stream;
     FArgs A = force_args(sys);
@@ -374,12 +522,17 @@ int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int preci
         } else if (ps.any_eam) {
             if (multi) k_eam_mixed<true><<<nb, kBlock, 0, st>>>(A, dps);
             else k_eam_mixed<false><<<nb, kBlock, 0, st>>>(A, dps);
+        } else if (ps.any_tab) {
+            if (!multi) k_tab_mixed<false, 3><<<nb, kBlock, 0, st>>>(A, dps);
+            else if (ps.any_lj) k_tab_mixed<true, 0><<<nb, kBlock, 0, st>>>(A, dps);
+            else k_tab_mixed<true, 3><<<nb, kBlock, 0, st>>>(A, dps);
         } else {
             if (multi) k_lj_mixed<true><<<nb, kBlock, 0, st>>>(A, dps);
             else k_lj_mixed<false><<<nb, kBlock, 0, st>>>(A, dps);
         }
     }
     MDG_LAUNCHED(ctx);
+    if (stage == 1 && th) return launch_thermostat(sys, th, precision);
     return MDG_OK;
 }
 

@@ -174,6 +174,77 @@ __device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __res
     A.gz[i] = acc.s[2];
 }
 
+// Force / r of a tabulated Pair term (pair.cxx:316-346) in FP32 from the
+// cubic coefficients of its r*phi table: d(r phi)/dr * r - r phi, over r^3.
+__device__ __forceinline__ float tab_ff32(const PotParams& P, float r2, bool& in) {
+    const float rinv = rsqrt_nr(fmaxf(r2, 1e-12f));
+    const float r = r2 * rinv;
+    const float t = r * P.inv_dr_f;
+    int nn = (int)t;
+    in = in && nn < P.Nr1;
+    nn = in ? nn : 0;
+    const float u = t - (float)nn;
+    const float4 cv = __ldg(P.v_c + nn);
+    const float V = cubic(cv, u);
+    const float dV = dcubic(cv, u) * P.inv_dr_f;
+    return (dV * r - V) * (rinv * rinv) * rinv;
+}
+
+__device__ __forceinline__ float lj_ff32(const PotParams& P, float r2) {
+    const float r2inv = __fdividef(1.0f, fmaxf(r2, 1e-12f));
+    const float r6inv = r2inv * r2inv * r2inv;
+    return P.mhf_f * fmaf(P.lj1_f, r6inv, -P.lj2_f) * r6inv * r2inv;
+}
+
+// Pair-type forces (no EAM term) where some kind pair uses the tabulated
+// Pair: FORM 3 = every pair tabulated, 0 = LJsCut or tabulated by kind pair.
+template <bool MULTI, int FORM>
+__device__ __forceinline__ void tab_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
+    if (A.tag[i] == 0) return;
+    const float4 pi = A.pos32[i];
+    const int ng = A.ncnt[i] >> 2;
+    const int ki = MULTI ? (A.kind[i] & 3) : 0;
+    const bool per = ps->periodic;
+    const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
+    Kahan3 acc;
+    const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
+    uint4 e4n = ng > 0 ? __ldg(row) : make_uint4(0, 0, 0, 0);
+    for (int g = 0; g < ng; ++g) {
+        const uint4 e4 = e4n;
+        if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
+        const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
+        float4 pj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32 + (e[q] & kJMask));
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const PotParams& P = ps->p[ki][MULTI ? (A.kind[e[q] & kJMask] & 3) : 0];
+            float dx, dy, dz;
+            pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            bool in = pair_in(A, i, e[q], r2, P.r2cut_f, P.R2cut, per);
+            float FF;
+            if (FORM == 3 || P.type == POT_TAB) {
+                FF = tab_ff32(P, r2, in);
+            } else {
+                in = in && P.type == POT_LJCUT;
+                FF = lj_ff32(P, r2);
+            }
+            FF = in ? FF : 0.f;
+            fx = fmaf(dx, FF, fx);
+            fy = fmaf(dy, FF, fy);
+            fz = fmaf(dz, FF, fz);
+        }
+        acc.add(0, fx);
+        acc.add(1, fy);
+        acc.add(2, fz);
+    }
+    A.gx[i] = acc.s[0];
+    A.gy[i] = acc.s[1];
+    A.gz[i] = acc.s[2];
+}
+
 __device__ __forceinline__ void embed32(const PotParams& P, float rho, float* F, float* dF,
                                         DevStatus* st) {
     float t = rho * P.inv_drh_f;
@@ -276,12 +347,15 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             float Fpi = pi.w, Fpj = pj[q].w;
-            bool eam = true;
+            bool eam = true, lj = false;
             if (MULTI) {
                 uint32_t j = e[q] & kJMask;
                 int kj = A.kind[j] & 3;
                 P = &ps->p[ki][kj];
-                eam = P->type == 2;
+                // a tabulated Pair has zero rho rows: the EAM arithmetic
+                // below reduces to its pair term exactly
+                eam = P->type >= POT_EAM;
+                lj = P->type == POT_LJCUT;
                 r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; rv = P->rv_c; R2c = P->R2cut;
                 Fpj = A.Fp32[(size_t)ki * A.np + j];
                 Fpi = A.Fp32[(size_t)kj * A.np + i];
@@ -289,14 +363,14 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
             float dx, dy, dz;
             pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            bool in = eam && pair_in(A, i, e[q], r2, r2c, R2c, per);
+            bool in = (eam || lj) && pair_in(A, i, e[q], r2, r2c, R2c, per);
             // one reciprocal square root gives both r and 1/r
             float rinv = rsqrt_nr(fmaxf(r2, 1e-12f));
             float r = r2 * rinv;
             float t = r * idr;
             int nn = (int)t;
-            in = in && nn < Nr1;
-            nn = in ? nn : 0;
+            in = in && (lj || nn < Nr1);
+            nn = in && !lj ? nn : 0;
             float u = t - (float)nn;
             float4 cr, cv;
             load_rv(rv, nn, cr, cv);
@@ -304,6 +378,7 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
             float V = cubic(cv, u);
             float dV = dcubic(cv, u) * idr;
             float FF = fmaf(Fpi + Fpj, drho, (dV * r - V) * (rinv * rinv)) * rinv;
+            if (MULTI && lj) FF = lj_ff32(*P, r2);
             FF = in ? FF : 0.f;
             fx = fmaf(FF, dx, fx);
             fy = fmaf(FF, dy, fy);

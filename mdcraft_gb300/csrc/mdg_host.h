@@ -65,8 +65,15 @@ cudaEvent_t timer_begin(mdg_ctx* ctx);
 void timer_end(mdg_ctx* ctx, int which, cudaEvent_t start);
 }  // namespace mdg
 
+// thermostat::Langevin (one term) or thermostat::Compound (parts in order).
+struct mdg_thermostat {
+    int compound = 0;
+    mdg_langevin p{};
+    std::vector<mdg_thermostat*> parts;
+};
+
 struct mdg_potential {
-    int type = 0;  // 1 pair (LJsCut), 2 EAM
+    int type = 0;  // mdg::POT_LJCUT, POT_EAM or POT_TAB (tabulated Pair: EAM layout, zero rho/F rows)
     double rcut = 0.0;
     // LJsCut
     double a = 0, s = 0, s6 = 0, lj1 = 0, lj2 = 0, factor = 0;
@@ -87,6 +94,7 @@ struct mdg_solver {
     int nstages = 0;
     int stages[2] = {0, 0};  // 0 charge, 1 forces
     mdg_potential* pot[mdg::kMaxKinds][mdg::kMaxKinds] = {};
+    mdg_thermostat* thermo = nullptr;  // applied after the force stage
 };
 
 struct mdg_system {
@@ -221,6 +229,7 @@ int download_atoms_enqueue(mdg_system* sys, size_t n);
 // A solver's potential parameters on the device (valid after a check on a
 // system of that device) and, optionally, their host copy.
 const PotSet* solver_potsets(mdg_solver* s, PotSet* host);
+const ThermoDev* thermo_of(mdg_solver* s);
 int nlist_capacity_host(mdg_system* sys, const mdg_atom* atoms, size_t n, int half);
 // The fused one-block driver loop (solo.cu): small mixed-precision systems,
 // one request per block of a persistent kernel fed through a queue.

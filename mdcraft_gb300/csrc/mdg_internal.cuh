@@ -92,9 +92,16 @@ __device__ inline float image_shift(uint32_t e, int axis, float cs) {
     return __int2float_rn(b - 1) * cs;
 }
 
+// Potential types: LJsCut and the tabulated Pair are the reference's
+// potential::type::pair (one force stage), EAM its potential::type::eam.
+enum : int { POT_NONE = 0, POT_LJCUT = 1, POT_EAM = 2, POT_TAB = 3 };
+
 // Per-kind-pair potential parameters handed to the force kernels by value.
+// Every table pointer is valid (a zero table stands in where a potential
+// has none), so a load the compiler issues ahead of its condition stays
+// in bounds.
 struct PotParams {
-    int type;          // 1 = LJsCut (pair), 2 = EAM
+    int type;          // POT_*
     double R2cut;
     float r2cut_f;
     // LJsCut (LJs-cut.cxx:8-20)
@@ -122,7 +129,28 @@ struct PotSet {
     int multi;
     int any_eam;
     int periodic;     // boundary::Periodic
+    int any_lj, any_tab;
     PotParams p[kMaxKinds][kMaxKinds];
+};
+
+// Rows of the zero table every table-less PotParams points at: enough for
+// the widest unconditional read (an interleaved rho/V row at interval 0,
+// FP64 knots 0 and 1).
+constexpr int kZeroRows = 8;
+
+// thermostat::Langevin terms (mdcraft/solver/thermostat/langevin.cxx),
+// applied in order after the force stage; sigma = sqrt(2 beta Kb T / dt).
+constexpr int kMaxThermo = 8;
+struct LangevinTerm {
+    double beta, sigma;
+    double heat[3], U[3];
+    double xmin, xmax;
+    unsigned long long seed;
+};
+struct ThermoDev {
+    int n;
+    int pad;
+    LangevinTerm t[kMaxThermo];
 };
 
 // Exact FP64 arithmetic without contraction, for bit-for-bit parity with
@@ -150,7 +178,8 @@ struct DevStatus {
     uint32_t max_count;     // longest list of the last build
     uint32_t nonuniform;    // some atom's rns differs from atom 0's
     uint32_t build_flags;   // FLAG_* raised by the current rebuild
-    uint32_t pad[3];
+    uint32_t pad[2];
+    uint32_t therm_calls;   // thermostat applications so far (Philox counter word)
 };
 
 }  // namespace mdg

@@ -424,7 +424,9 @@ __global__ void __launch_bounds__(NT, 1) k_solo_persistent(const SoloArgs* __res
 }
 
 int solo_eligible(const mdg_solver* s, const mdg_system* sys) {
-    if (s->precision != MDG_PREC_MIXED || s->multi || s->nstages < 1) return 0;
+    if (s->precision != MDG_PREC_MIXED || s->multi || s->nstages < 1 || s->thermo) return 0;
+    // the fused loop carries the LJsCut and EAM bodies only
+    if (!s->pot[0][0] || (s->pot[0][0]->type != POT_LJCUT && s->pot[0][0]->type != POT_EAM)) return 0;
     if (sys->n == 0 || sys->n > (size_t)kSoloMaxAtoms || sys->half || !sys->cap_ready || sys->ctx->timing) return 0;
     return 1;
 }

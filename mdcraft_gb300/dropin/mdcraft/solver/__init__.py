@@ -34,23 +34,26 @@ class Pair:
         self._run(atoms, neibs, nlist, "stages")
 
 
-def _check_thermostat(thermostat):
-    if thermostat is not None:
-        raise NotImplementedError("thermostats are not built on the GPU path (NVE only)")
+def _attach(solver, thermostat):
+    """The thermostat argument of Single / Multi: applied after each atom's
+    forces in the force stage (pair.cxx:72-86)."""
+    solver._thermostat = thermostat
+    if thermostat is not None and thermostat._t is not None:
+        solver._s.set_thermostat(thermostat._t)
 
 
 class Single(Pair):
     def __init__(self, potential, boundary=None, thermostat=None, threads=None, precision="fp64"):
-        _check_thermostat(thermostat)
         self.potential = potential
         self._s = _mdg.Single(potential._p, periodic=boundary is not None, precision=precision)
+        _attach(self, thermostat)
 
 
 class Multi(Pair):
     def __init__(self, boundary=None, thermostat=None, nkinds: int = 1, threads=None, precision="fp64"):
-        _check_thermostat(thermostat)
         self._keep = []
         self._s = _mdg.Multi(nkinds, periodic=boundary is not None, precision=precision)
+        _attach(self, thermostat)
 
     def add_potential(self, i: int, j: int, potential):
         self._keep.append(potential)

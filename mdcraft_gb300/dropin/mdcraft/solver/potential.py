@@ -1,5 +1,6 @@
 """mdcraft.solver.potential (python/mdcraft/solver/potential/_potential.cxx):
-EAM (arrays or a setfl file) and LJsCut on the GPU engine."""
+EAM (arrays or a setfl file), Pair (arrays or a file) and LJsCut on the GPU
+engine."""
 from __future__ import annotations
 
 import numpy as np
@@ -35,7 +36,19 @@ class LJsCut:
 
 
 class Pair:
-    """Tabulated pair potential: not built on the GPU path."""
+    """Pair(Rcutoff, pairPotential, NrPot, drPot) or Pair(filename)
+    (_potential.cxx:170-201): tabulated r*phi(r)."""
 
     def __init__(self, *args, **kw):
-        raise NotImplementedError("the tabulated Pair potential is not built on the GPU path")
+        if (len(args) == 1 and isinstance(args[0], str)) or "filename" in kw:
+            self._p = _mdg.Pair.from_file(args[0] if args else kw["filename"])
+            return
+        names = ["Rcutoff", "pairPotential", "NrPot", "drPot"]
+        a = dict(zip(names, args))
+        a.update(kw)
+        self._p = _mdg.Pair(a["Rcutoff"], np.asarray(a["pairPotential"], dtype=np.float64), int(a["NrPot"]),
+                            float(a["drPot"]))
+
+    @property
+    def rcut(self) -> float:
+        return self._p.rcut()

@@ -703,6 +703,27 @@ md_pot* md_pot_eam_create(double rcut, const double* Femb, const double* Rho,
     return p;
 }
 
+md_pot* md_pot_pair_create(double rcut, const double* Vpar, int Nr1,
+                           double dr) {
+    /* Pair::Pair(arrays) (pair.cxx:15-33). The reference's table has Nr1
+     * entries and its spline reads entry N1+1 for N1 < Nr1 (one past the
+     * end at the last interval); the copy here carries the last value as
+     * padding, as for the EAM tables. */
+    if (Nr1 < 3) return NULL;
+    md_pot* p = (md_pot*)calloc(1, sizeof(md_pot));
+    p->type = MD_POT_TAB;
+    p->R1cut = rcut;
+    p->R2cut = rcut * rcut;
+    p->Nr1 = Nr1;
+    p->dr = dr;
+    p->dr1 = 1.0 / dr;
+    p->Vpar = padded_copy(Vpar, Nr1);
+    p->dVpar = (double*)calloc((size_t)Nr1 + 1, sizeof(double));
+    md_eam_init_spline(p->Vpar, p->dVpar, p->dr1, (size_t)Nr1, 1);
+    p->dVpar[Nr1] = p->dVpar[Nr1 - 1];
+    return p;
+}
+
 void md_pot_destroy(md_pot* p) {
     if (!p) return;
     free(p->Femb); free(p->Rho); free(p->Vpar);
@@ -1022,6 +1043,178 @@ static void eam_virial(const md_pot* p, md_atom* a, const nview* v, scratch* s) 
     a->Ep += eam_value(p, s->r2, natoms);
 }
 
+/* Pair spline of one cut pair (pair.cxx:316-346): force/r, and V(r) */
+static inline double tab_pair_ff(const md_pot* p, double R2, double* VRout) {
+    double R1 = sqrt(R2);
+    double RN = R1 * p->dr1;
+    int N1 = (int)trunc(RN);
+    double VR = 0.0, DV = 0.0;
+    if (N1 < p->Nr1) {
+        VR = N1;
+        DV = RN - VR;
+        RN = R1 - VR * p->dr;
+        VR = (p->Vpar[N1 + 1] - p->Vpar[N1]) * p->dr1;
+        double aa = (p->dVpar[N1 + 1] - VR) - (VR - p->dVpar[N1]);
+        double bb = aa - (VR - p->dVpar[N1]);
+        aa = aa * DV;
+        VR = p->Vpar[N1] + RN * (p->dVpar[N1] + DV * (aa - bb));
+        DV = p->dVpar[N1] + 2.0 * DV * (1.5 * aa - bb);
+    }
+    if (VRout) *VRout = VR;
+    return ((DV * R1 - VR) / R2) / R1;
+}
+
+/* Pair::force(self, ...) (pair.cxx:387-462): half lists push the pair
+ * force onto both atoms; full lists sum the cut pairs from zero, then add. */
+static void tab_force(const md_pot* p, md_atom* a, const nview* v) {
+    double F[3] = {0.0, 0.0, 0.0};
+    for (size_t i = 0; i < v->nn; i++) {
+        double rx = v->rj[i][0] - a->r[0];
+        double ry = v->rj[i][1] - a->r[1];
+        double rz = v->rj[i][2] - a->r[2];
+        double r2 = rx * rx + ry * ry + rz * rz;
+        if (r2 > p->R2cut || r2 < 1e-15) continue;
+        double FF = tab_pair_ff(p, r2, NULL);
+        if (v->nbp) {
+            double G[3] = {FF * rx, FF * ry, FF * rz};
+            for (int k = 0; k < 3; ++k) {
+                a->f[k] += G[k];
+                v->nbp[i]->f[k] -= G[k];
+            }
+        } else {
+            F[0] += FF * rx;
+            F[1] += FF * ry;
+            F[2] += FF * rz;
+        }
+    }
+    if (!v->nbp) {
+        a->f[0] += F[0];
+        a->f[1] += F[1];
+        a->f[2] += F[2];
+    }
+}
+
+/* Pair::virial(self, ...) (pair.cxx:228-314): V += 1/2 FF d d^T and
+ * Ep += V(r)/(2r) per cut pair (both atoms for half lists). */
+static void tab_virial(const md_pot* p, md_atom* a, const nview* v) {
+    double Vt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double Ut = 0.0;
+    for (size_t i = 0; i < v->nn; i++) {
+        double d[3] = {v->rj[i][0] - a->r[0], v->rj[i][1] - a->r[1],
+                       v->rj[i][2] - a->r[2]};
+        double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (r2 > p->R2cut || r2 < 1e-15) continue;
+        double VR;
+        double FF = tab_pair_ff(p, r2, &VR);
+        double E = 0.5 * VR / sqrt(r2);
+        if (v->nbp) {
+            double M[9];
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 3; ++r) M[r + 3 * c] = 0.5 * (FF * d[r]) * d[c];
+            for (int k = 0; k < 9; ++k) {
+                a->V[k] += M[k];
+                v->nbp[i]->V[k] += M[k];
+            }
+            a->Ep += E;
+            v->nbp[i]->Ep += E;
+        } else {
+            double h = 0.5 * FF;
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 3; ++r) Vt[r + 3 * c] += h * d[r] * d[c];
+            Ut += E;
+        }
+    }
+    if (!v->nbp) {
+        for (int k = 0; k < 9; ++k) a->V[k] += Vt[k];
+        a->Ep += Ut;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Langevin thermostat — mdcraft/solver/thermostat/langevin.cxx:8-42        */
+/* ------------------------------------------------------------------------ */
+
+#define MD_MAXTHERMO 8
+
+struct md_thermo {
+    int n;
+    md_langevin term[MD_MAXTHERMO];
+};
+
+md_thermo* md_thermo_create(void) { return (md_thermo*)calloc(1, sizeof(md_thermo)); }
+
+int md_thermo_add(md_thermo* t, const md_langevin* term) {
+    if (!t || !term || t->n >= MD_MAXTHERMO) return MDREF_ERR_INVALID;
+    t->term[t->n++] = *term;
+    return MDREF_OK;
+}
+
+void md_thermo_destroy(md_thermo* t) { free(t); }
+
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+ * easy as 1, 2, 3", SC'11): ten rounds of two 32x32->64 multiplications
+ * with a Weyl-sequence key schedule. */
+void md_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
+                      uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c1 = (uint32_t)p1;
+        c3 = (uint32_t)p0;
+        c0 = n0;
+        c2 = n2;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+/* Two Box-Muller pairs from one Philox block; the first three normals. */
+void md_langevin_normals(uint64_t seed, uint32_t atom, uint32_t call,
+                         uint32_t term, double z[3]) {
+    const uint32_t ctr[4] = {atom, call, term, 0u};
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint32_t x[4];
+    md_philox4x32_10(ctr, key, x);
+    const double k32 = 2.3283064365386962890625e-10; /* 2^-32 */
+    const double two_pi = 6.283185307179586476925;
+    double u0 = ((double)x[0] + 0.5) * k32, u1 = ((double)x[1] + 0.5) * k32;
+    double u2 = ((double)x[2] + 0.5) * k32, u3 = ((double)x[3] + 0.5) * k32;
+    double ra = sqrt(-2.0 * log(u0)), rb = sqrt(-2.0 * log(u2));
+    z[0] = ra * cos(two_pi * u1);
+    z[1] = ra * sin(two_pi * u1);
+    z[2] = rb * cos(two_pi * u3);
+}
+
+/* Langevin::apply_one (langevin.cxx:29-42) for every term, in order. */
+static void thermo_apply(const md_thermo* t, md_atom* a, uint32_t atom,
+                         uint32_t call) {
+    for (int q = 0; q < t->n; ++q) {
+        const md_langevin* L = &t->term[q];
+        if (a->r[0] < L->xmin || a->r[0] > L->xmax) continue;
+        /* sigma = sqrt(2 beta Kb T / dt) (langevin.cxx:24), Kb of base.h:10 */
+        double sigma = sqrt(2.0 * L->beta * 0.008314462175 * L->temperature / L->time_step);
+        double z[3];
+        md_langevin_normals(L->seed, atom, call, (uint32_t)q, z);
+        double sqrt_mass = sqrt(a->m);
+        for (int k = 0; k < 3; ++k) {
+            double tf = (z[k] * sigma + 0.0) * sqrt_mass;
+            tf -= (a->v[k] - L->U[k]) * L->beta * a->m;
+            tf = tf * L->heat[k];
+            a->f[k] += tf;
+        }
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Solvers — mdcraft/solver/{pair,single,multi}.cxx + boundary/periodic.cxx */
 /* ------------------------------------------------------------------------ */
@@ -1037,7 +1230,20 @@ struct md_solver {
     md_domain dom;
     scratch* scr;
     int nscr;
+    const md_thermo* thermo;
+    uint32_t thermo_calls;
 };
+
+void md_solver_set_thermostat(md_solver* s, md_thermo* t, uint32_t calls) {
+    s->thermo = t;
+    s->thermo_calls = calls;
+}
+
+uint32_t md_solver_thermo_calls(const md_solver* s) { return s->thermo_calls; }
+
+static int pair_type(const md_pot* p) {
+    return p->type == MD_POT_PAIR || p->type == MD_POT_TAB;
+}
 
 static md_solver* solver_new(const md_domain* pd, int nthreads) {
     md_solver* s = (md_solver*)calloc(1, sizeof(md_solver));
@@ -1056,7 +1262,7 @@ md_solver* md_solver_single(md_pot* p, const md_domain* pd, int nthreads) {
     md_solver* s = solver_new(pd, nthreads);
     s->nkinds = 1;
     s->pot[0][0] = p;
-    if (p->type == MD_POT_PAIR) {
+    if (pair_type(p)) {
         s->nstages = 1;
         s->stages[0] = STAGE_FORCES;
     } else if (p->type == MD_POT_EAM) {
@@ -1082,7 +1288,7 @@ int md_solver_add_potential(md_solver* s, int i, int j, md_pot* p) {
     s->pot[i][j] = p;
     s->pot[j][i] = p;
     if (s->nstages == 0) {
-        if (p->type == MD_POT_PAIR) {
+        if (pair_type(p)) {
             s->nstages = 1;
             s->stages[0] = STAGE_FORCES;
         } else if (p->type == MD_POT_EAM) {
@@ -1122,6 +1328,9 @@ static void pot_apply(md_pot* p, int op, md_atom* a, const nview* v, scratch* s)
         if (op == 1) ljcut_force(p, a, v);
         else if (op == 2) ljcut_virial(p, a, v);
         /* Base::density is a no-op for pair potentials */
+    } else if (p->type == MD_POT_TAB) {
+        if (op == 1) tab_force(p, a, v);
+        else if (op == 2) tab_virial(p, a, v);
     } else if (p->type == MD_POT_EAM) {
         if (op == 0) eam_density(p, a, v, s);
         else if (op == 1) eam_force(p, a, v, s);
@@ -1182,7 +1391,8 @@ static void stage_range(void* pctx, size_t b, size_t e, int tid) {
         nview v = {nn, (const double(*)[3])rj, sc->gnc, nl->half ? sc->gnb : NULL};
         /* The potentials reuse rall/r2; they do not touch gr/gnc/gkind. */
         solver_one(s, c->op, a, &v, sc->gkind, sc);
-        /* thermostat.apply_one: the default thermostat is a no-op */
+        /* thermostat.apply_one, for every atom (pair.cxx:81) */
+        if (c->op == 1 && s->thermo) thermo_apply(s->thermo, a, (uint32_t)i, s->thermo_calls);
         if (!a->bc) continue;
         /* Periodic::prepare_ghosts (periodic.cxx:36-60) */
         size_t g = 0;
@@ -1211,6 +1421,7 @@ static void run_stage(md_solver* s, md_atom* atoms, size_t n,
                       const md_nlist* nl, int op) {
     st_ctx c = {s, atoms, n, nl, op};
     parallel_for(nl->half ? 1 : s->nthreads, n, stage_range, &c);
+    if (op == 1 && s->thermo) s->thermo_calls += 1;
 }
 
 typedef struct {

@@ -103,9 +103,12 @@ size_t md_nlist_list_for(const md_nlist* nl, const md_domain* d,
                          uint64_t* out, size_t cap);
 void md_nlist_grid(const md_nlist* nl, md_grid* out);
 
-/* Potentials (mdcraft/solver/potential). */
+/* Potentials (mdcraft/solver/potential). MD_POT_PAIR is LJsCut and
+ * MD_POT_TAB the tabulated Pair; both are potential::type::pair in the
+ * reference (one force stage, no density). */
 #define MD_POT_PAIR 1
 #define MD_POT_EAM 2
+#define MD_POT_TAB 3
 
 typedef struct md_pot md_pot;
 
@@ -113,6 +116,10 @@ md_pot* md_pot_ljcut_create(double a, double s, double rcut);
 md_pot* md_pot_eam_create(double rcut, const double* Femb, const double* Rho,
                           const double* Vpar, int Nr1, double dr, int Nrh1,
                           double drh);
+/* Pair(Rcutoff, Vpar, Nr1, dr) (mdcraft/solver/potential/pair.cxx:15-33):
+ * Vpar = r*phi(r) on a uniform grid of step dr. */
+md_pot* md_pot_pair_create(double rcut, const double* Vpar, int Nr1,
+                           double dr);
 void md_pot_destroy(md_pot* p);
 double md_pot_rcut(const md_pot* p);
 int md_pot_type(const md_pot* p);
@@ -146,6 +153,37 @@ void md_solver_virials(md_solver* s, md_atom* atoms, size_t n,
 /* Runs solver.stages in order (Single: [forces] or [charge, forces]). */
 void md_solver_stages(md_solver* s, md_atom* atoms, size_t n,
                       const md_nlist* nl);
+
+/* thermostat::Langevin (mdcraft/solver/thermostat/langevin.cxx:8-42) and
+ * thermostat::Compound (compound.h): a list of Langevin terms applied in
+ * order after each atom's own forces and before its ghost pass
+ * (mdcraft/solver/pair.cxx:72-86). The reference draws from an unseeded
+ * std::default_random_engine; here the normals come from Philox4x32-10
+ * (Salmon et al., SC'11) keyed by `seed`, counter = {atom index, call
+ * number, term index, 0}, through the Box-Muller transform, so that a run
+ * is reproducible and the product can be checked draw for draw. */
+typedef struct md_langevin {
+    double beta, temperature, time_step;
+    double heat[3], U[3];
+    double xmin, xmax;
+    uint64_t seed;
+} md_langevin;
+
+typedef struct md_thermo md_thermo;
+md_thermo* md_thermo_create(void);
+int md_thermo_add(md_thermo* t, const md_langevin* term);
+void md_thermo_destroy(md_thermo* t);
+/* Attaches (or with NULL detaches) the thermostat; the solver's call
+ * counter restarts at `calls`. */
+void md_solver_set_thermostat(md_solver* s, md_thermo* t, uint32_t calls);
+uint32_t md_solver_thermo_calls(const md_solver* s);
+
+/* Philox4x32-10 block and the three normals of one draw (exposed for the
+ * known-answer test and the statistics tests). */
+void md_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
+                      uint32_t out[4]);
+void md_langevin_normals(uint64_t seed, uint32_t atom, uint32_t call,
+                         uint32_t term, double z[3]);
 
 /* stepper::Verlet::make_step (mdcraft/solver/stepper/verlet.cxx:36-85). */
 void md_verlet_make_step(md_solver* s, md_atom* atoms, size_t n,

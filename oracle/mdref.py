@@ -92,6 +92,8 @@ def lib():
         L.md_pot_ljcut_create.restype = vp
         L.md_pot_eam_create.argtypes = [dp, vp, vp, vp, ip, dp, ip, dp]
         L.md_pot_eam_create.restype = vp
+        L.md_pot_pair_create.argtypes = [dp, vp, ip, dp]
+        L.md_pot_pair_create.restype = vp
         L.md_pot_destroy.argtypes = [vp]
         L.md_pot_rcut.argtypes = [vp]
         L.md_pot_rcut.restype = dp
@@ -113,6 +115,14 @@ def lib():
         L.md_run.argtypes = [vp, vp, sz, vp, vp, dp, C.c_long]
         L.md_run.restype = C.c_long
         L.md_measure_state.argtypes = [vp, sz, vp]
+        L.md_thermo_create.restype = vp
+        L.md_thermo_add.argtypes = [vp, vp]
+        L.md_thermo_destroy.argtypes = [vp]
+        L.md_solver_set_thermostat.argtypes = [vp, vp, C.c_uint32]
+        L.md_solver_thermo_calls.argtypes = [vp]
+        L.md_solver_thermo_calls.restype = C.c_uint32
+        L.md_philox4x32_10.argtypes = [vp, vp, vp]
+        L.md_langevin_normals.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, vp]
         L.md_hardware_threads.restype = ip
         _lib = L
     return _lib
@@ -337,6 +347,70 @@ class EAM:
             self.h = None
 
 
+class Pair:
+    """mdcraft::solver::potential::Pair (pair.h:13-18), array constructor:
+    Vpar = r*phi(r) on a uniform grid of step dr."""
+
+    type = 3
+
+    def __init__(self, rcut, Vpar, Nr1, dr):
+        self._keep = np.ascontiguousarray(Vpar, dtype=np.float64)
+        self.h = lib().md_pot_pair_create(rcut, _ptr(self._keep), int(Nr1), dr)
+        if not self.h:
+            raise ValueError("bad Pair table")
+
+    def rcut(self) -> float:
+        return lib().md_pot_rcut(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().md_pot_destroy(self.h)
+            self.h = None
+
+
+class _Langevin(C.Structure):
+    _fields_ = [("beta", C.c_double), ("temperature", C.c_double), ("time_step", C.c_double),
+                ("heat", C.c_double * 3), ("U", C.c_double * 3), ("xmin", C.c_double), ("xmax", C.c_double),
+                ("seed", C.c_uint64)]
+
+
+class Thermostat:
+    """thermostat::Langevin terms applied in order (langevin.cxx:29-42,
+    compound.h); each term is a dict of Langevin's constructor arguments
+    plus `seed`."""
+
+    def __init__(self, *terms):
+        self.h = lib().md_thermo_create()
+        for t in terms:
+            self.add(**t)
+
+    def add(self, beta, temperature, time_step, heat_x=1, heat_y=1, heat_z=1, Ux=0.0, Uy=0.0, Uz=0.0,
+            xmin=-1e15, xmax=1e15, seed=0):
+        L = _Langevin(beta, temperature, time_step, (C.c_double * 3)(heat_x, heat_y, heat_z),
+                      (C.c_double * 3)(Ux, Uy, Uz), xmin, xmax, seed)
+        if lib().md_thermo_add(self.h, C.byref(L)) != 0:
+            raise ValueError("too many thermostat terms")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().md_thermo_destroy(self.h)
+            self.h = None
+
+
+def philox4x32_10(ctr, key):
+    c = np.asarray(ctr, dtype=np.uint32)
+    k = np.asarray(key, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib().md_philox4x32_10(_ptr(c), _ptr(k), _ptr(out))
+    return out
+
+
+def langevin_normals(seed, atom, call, term):
+    z = np.zeros(3)
+    lib().md_langevin_normals(seed, atom, call, term, _ptr(z))
+    return z
+
+
 class Solver:
     """Single (single.h:22-166) or Multi (multi.h:27-174) with an optional
     Periodic boundary (periodic.h:29)."""
@@ -353,6 +427,13 @@ class Solver:
     def add_potential(self, i, j, pot):
         self._pots.append(pot)
         return lib().md_solver_add_potential(self.h, i, j, pot.h)
+
+    def set_thermostat(self, thermo: "Thermostat | None", calls: int = 0):
+        self._thermo = thermo
+        lib().md_solver_set_thermostat(self.h, thermo.h if thermo is not None else None, calls)
+
+    def thermo_calls(self) -> int:
+        return lib().md_solver_thermo_calls(self.h)
 
     def num_stages(self) -> int:
         return lib().md_solver_num_stages(self.h)

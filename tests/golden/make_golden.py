@@ -5,6 +5,8 @@ own test fixtures (run in a container where the reference is checked out).
   atoms) used by test/cxx/solver/test_argon_ball_md.cxx
 - al2009_eam_alloy.xz   <- test/python/solver/Al2009.eam.alloy (setfl EAM Al)
   used by test/cxx/solver/test_aluminum_bulk_eam.cxx
+- nialpair_eam_alloy.xz <- problems/NiAl/NiAlpair.eam.alloy (tabulated Ni-Al
+  pair term read by Pair(filename)) used by problems/NiAl/test-NiAl.py
 
 The files are byte-identical copies, xz-compressed, so the tests parse them
 exactly as the reference's loaders do. The golden VALUES the tests check are
@@ -23,6 +25,7 @@ def main(ref: str) -> None:
     pairs = [
         (os.path.join(ref, "test", "cxx", "LMP_BALL_130k_Ar"), "lmp_ball_130k_ar.xz"),
         (os.path.join(ref, "test", "python", "solver", "Al2009.eam.alloy"), "al2009_eam_alloy.xz"),
+        (os.path.join(ref, "problems", "NiAl", "NiAlpair.eam.alloy"), "nialpair_eam_alloy.xz"),
     ]
     for src, dst in pairs:
         raw = open(src, "rb").read()

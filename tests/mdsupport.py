@@ -105,6 +105,31 @@ def al2009():
         return read_setfl(f.read())
 
 
+def read_pair_file(text: str) -> dict:
+    """Pair::Pair(std::string) reader (mdcraft/solver/potential/pair.cxx:36-56):
+    skips 4 lines, reads Nr1 dr rcut, then Nr1 values of r*phi(r) in eV*A;
+    converts A->nm and eV*A->kJ*nm/mol."""
+    lines = text.splitlines(True)
+    toks = "".join(lines[4:]).split()
+    Nr1, dr, rcut = int(toks[0]), float(toks[1]), float(toks[2])
+    Vpar = np.array([float(t) for t in toks[3: 3 + Nr1]], dtype=np.float64) * (Qelectron / (10 * UnEnrg))
+    return dict(rcut=rcut / 10, Vpar=Vpar, Nr1=Nr1, dr=dr / 10)
+
+
+def nialpair_text() -> str:
+    with lzma.open(os.path.join(GOLDEN, "nialpair_eam_alloy.xz"), "rt") as f:
+        return f.read()
+
+
+def nialpair():
+    return read_pair_file(nialpair_text())
+
+
+def al2009_text() -> str:
+    with lzma.open(os.path.join(GOLDEN, "al2009_eam_alloy.xz"), "rt") as f:
+        return f.read()
+
+
 def set_common_atom_properties(atoms, mass, rcut, skin_factor):
     """set_common_atom_properties (md_test_utils.h:171-184)."""
     n = len(atoms)
