@@ -164,6 +164,10 @@ int mdg_pot_eam_create(double rcut, const double* Femb, const double* Rho,
 /* EAM(std::string filename) (EAM.cxx:55-87): single-element setfl file;
  * unlike the reference, a missing or short file fails with MDG_ERR_IO. */
 int mdg_pot_eam_create_from_file(const char* path, mdg_potential** out);
+/* LJs(aVr, rVr, Rcutoff) (mdcraft/solver/potential/LJs.h:14-18): Lennard-
+ * Jones 4 aVr [(rVr/r)^12 - (rVr/r)^6] with a cubic in X = (r/rVr)^2 - 2^(1/3)
+ * that brings force and energy to zero at the cutoff (LJs.cxx:7-29). */
+int mdg_pot_ljs_create(double aVr, double rVr, double rcut, mdg_potential** out);
 /* Pair(Rcutoff, Vpar, Nr1, dr) (mdcraft/solver/potential/pair.h:13-18,
  * pair.cxx:15-33): tabulated r*phi(r) with the reference's spline; pair
  * energy phi(r)/2 per side, force from d(r*phi)/dr. */

@@ -18,8 +18,8 @@ import numpy as np
 
 __all__ = [
     "ATOM_DTYPE", "Context", "Domain", "System", "VerletList", "LJsCut", "EAM", "Single", "Multi", "Verlet",
-    "MDGError", "new_atoms", "lib", "lib_path", "PREC_FP64", "PREC_MIXED", "Server", "Pair", "Langevin",
-    "Compound",
+    "MDGError", "new_atoms", "lib", "lib_path", "PREC_FP64", "PREC_MIXED", "Server", "Pair", "LJs",
+    "Langevin", "Compound",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -100,7 +100,7 @@ def lib():
         "mdg_server_result": ([vp, C.c_uint64, vp, sz, vp], ip),
         "mdg_server_stats_get": ([vp, vp], ip), "mdg_server_clock": ([vp, C.POINTER(C.c_double)], ip),
         "mdg_server_footprint": ([sz, ip], sz),
-        "mdg_pot_pair_create": ([dp, vp, ip, dp, pp], ip),
+        "mdg_pot_pair_create": ([dp, vp, ip, dp, pp], ip), "mdg_pot_ljs_create": ([dp, dp, dp, pp], ip),
         "mdg_pot_pair_create_from_file": ([C.c_char_p, pp], ip),
         "mdg_thermo_langevin_create": ([vp, pp], ip), "mdg_thermo_langevin_set": ([vp, vp], ip),
         "mdg_thermo_langevin_get": ([vp, vp], ip), "mdg_thermo_compound_create": ([pp], ip),
@@ -368,6 +368,15 @@ class EAM(_Pot):
         _check(lib().mdg_pot_eam_create_from_file(path.encode(), C.byref(h)))
         obj.h = h
         return obj
+
+
+class LJs(_Pot):
+    """LJs(aVr, rVr, Rcutoff) (LJs.h:14-18): smoothed Lennard-Jones."""
+
+    def __init__(self, aVr: float, rVr: float, rcut: float):
+        h = C.c_void_p()
+        _check(lib().mdg_pot_ljs_create(aVr, rVr, rcut, C.byref(h)))
+        self.h = h
 
 
 class Pair(_Pot):

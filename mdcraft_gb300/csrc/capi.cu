@@ -399,7 +399,7 @@ static void cubic_coeffs(const std::vector<double>& y, const std::vector<double>
 }
 
 int pot_upload(mdg_potential* p, int device) {
-    if (p->type < POT_EAM || p->device == device) return MDG_OK;
+    if ((p->type != POT_EAM && p->type != POT_TAB) || p->device == device) return MDG_OK;
     if (p->d_tab64) cudaFree(p->d_tab64);
     if (p->d_tab32) cudaFree(p->d_tab32);
     p->d_tab64 = nullptr;
@@ -455,7 +455,21 @@ static void fill_params(const mdg_potential* p, PotParams& P, const double* z64,
         P.lj1_f = (float)p->lj1;
         P.lj2_f = (float)p->lj2;
         P.mhf_f = (float)(-0.5 * p->factor);
-    } else if (p->type >= POT_EAM) {
+    } else if (p->type == POT_LJS) {
+        P.ljs_rVr1 = p->ljs_rVr1;
+        P.ljs_rVr2 = p->ljs_rVr2;
+        P.ljs_aLJ = p->ljs_aLJ;
+        P.ljs_bLJ = p->ljs_bLJ;
+        P.ljs_aLJ3 = p->ljs_aLJ3;
+        P.ljs_bLJ2 = p->ljs_bLJ2;
+        P.ljs_aVr = p->ljs_aVr;
+        P.ljs_aVr2 = p->ljs_aVr2;
+        P.ljs_rVr1_f = (float)p->ljs_rVr1;
+        P.ljs_rVr2_f = (float)p->ljs_rVr2;
+        P.ljs_aLJ_f = (float)p->ljs_aLJ;
+        P.ljs_bLJ_f = (float)p->ljs_bLJ;
+        P.ljs_aVr2_f = (float)p->ljs_aVr2;
+    } else if (p->type == POT_EAM || p->type == POT_TAB) {
         size_t nr = (size_t)p->Nr1 + 1, nh = (size_t)p->Nrh1 + 1;
         P.Nr1 = p->Nr1;
         P.Nrh1 = p->Nrh1;
@@ -544,6 +558,7 @@ int potset_build(mdg_solver* s, mdg_system* sys, PotSet* out) {
                 if (rc) return rc;
                 if (p->type == POT_EAM) ps.any_eam = 1;
                 if (p->type == POT_LJCUT) ps.any_lj = 1;
+                if (p->type == POT_LJS) ps.any_ljs = 1;
                 if (p->type == POT_TAB) ps.any_tab = 1;
             }
             fill_params(p, ps.p[i][j], b->z64, b->z32);
@@ -1134,6 +1149,32 @@ int mdg_pot_eam_create_from_file(const char* path, mdg_potential** out) {
     return mdg_pot_eam_create(rcut, F.data(), R.data(), V.data(), Nr1, dr, Nrh1, drh, out);
 }
 
+int mdg_pot_ljs_create(double aVr, double rVr, double rcut, mdg_potential** out) {
+    // LJs::LJs (LJs.cxx:7-29), same operation order
+    if (!out || !(rcut > 0.0) || !(rVr > 0.0)) return MDG_ERR_INVALID;
+    const double X2min = 1.2599210498948732;
+    mdg_potential* p = new mdg_potential();
+    p->type = POT_LJS;
+    p->rcut = rcut;
+    const double R2cut = rcut * rcut;
+    double rVr2 = rVr * rVr;
+    double aVr2 = R2cut / rVr2 - X2min;
+    double aLJ3 = (rVr2 / R2cut) * (rVr2 / R2cut) * (rVr2 / R2cut);
+    double bLJ2 = (aLJ3 - 0.5) * aVr2 * rVr2 / R2cut;
+    double aLJ = (aLJ3 - 1.0 + 2.0 * bLJ2) * aLJ3 / (aVr2 * aVr2);
+    double bLJ = -(aLJ3 - 1.0 + 3.0 * bLJ2) * aLJ3 / (aVr2 * aVr2 * aVr2);
+    p->ljs_rVr2 = rVr2;
+    p->ljs_rVr1 = 1.0 / rVr2;
+    p->ljs_aLJ = aLJ;
+    p->ljs_bLJ = bLJ;
+    p->ljs_aLJ3 = 3.0 * aLJ;
+    p->ljs_bLJ2 = 2.0 * bLJ;
+    p->ljs_aVr2 = -48.0 * aVr / rVr2;
+    p->ljs_aVr = 2.0 * aVr;
+    *out = p;
+    return MDG_OK;
+}
+
 int mdg_pot_pair_create(double rcut, const double* Vpar, int Nr1, double dr, mdg_potential** out) {
     // Pair::Pair(arrays) (pair.cxx:15-33). The table rides the EAM table
     // layout with zero rho and embedding rows, so the force kernels of a
@@ -1215,7 +1256,7 @@ int mdg_pot_rcut(mdg_potential* p, double* rcut) {
 
 // ---- solvers ----------------------------------------------------------------
 static void set_stages(mdg_solver* s, int type, bool first) {
-    if (type == POT_TAB) type = POT_LJCUT;  // both potential::type::pair
+    if (type == POT_TAB || type == POT_LJS) type = POT_LJCUT;  // all potential::type::pair
     if (first) {
         if (type == 1) {
             s->nstages = 1;

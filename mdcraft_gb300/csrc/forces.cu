@@ -120,6 +120,16 @@ __device__ __forceinline__ double tab_ff64(const PotParams& P, double R2, double
     return ((DV * R1 - VR) / R2) / R1;
 }
 
+// LJs force / r (LJs.cxx:153-166) and energy term (LJs.cxx:90-101).
+__device__ __forceinline__ double ljs_ff64(const PotParams& P, double r2, double* E) {
+    const double X2min = 1.2599210498948732;
+    double XX = P.ljs_rVr1 * r2 - X2min;
+    double FV = P.ljs_rVr2 / r2;
+    double Ur = FV * FV * FV;
+    if (E) *E = P.ljs_aVr * (Ur * (Ur - 1.0) - (P.ljs_aLJ3 + P.ljs_bLJ2 * XX) * XX * XX);
+    return P.ljs_aVr2 * (Ur * (Ur - 0.5) * FV + (P.ljs_aLJ + P.ljs_bLJ * XX) * XX);
+}
+
 __device__ __forceinline__ double lj_pref64(const PotParams& P, double r2) {
     double r2inv = 1.0 / r2;
     double r6inv = r2inv * r2inv * r2inv;
@@ -201,6 +211,8 @@ __global__ void __launch_bounds__(kBlock) k_forces64(FArgs A, const PotSet* __re
             pref = eam_ff64(P, r2, AdF, nullptr);
         } else if (P.type == POT_TAB) {
             pref = tab_ff64(P, r2, nullptr);
+        } else if (P.type == POT_LJS) {
+            pref = ljs_ff64(P, r2, nullptr);
         } else {
             return;
         }
@@ -289,6 +301,12 @@ __global__ void __launch_bounds__(kBlock) k_virials64(FArgs A, const PotSet* __r
             for (int c = 0; c < 3; ++c)
                 for (int r = 0; r < 3; ++r) M[r + 3 * c] += h * d[r] * d[c];
             Ep += Vr;
+        } else if (P.type == POT_LJS) {
+            double E;
+            double FF = ljs_ff64(P, r2, &E);
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 3; ++r) M[r + 3 * c] += 0.5 * (FF * d[r]) * d[c];
+            Ep += E;
         }
     });
     A.Ep[i] = Ep;
@@ -332,9 +350,9 @@ __global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_eam_mixed(FArgs A, 
 
 
 template <bool MULTI, int FORM>
-__global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_tab_mixed(FArgs A, const PotSet* __restrict__ ps) {
+__global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_pair_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < A.n) tab_mixed_one<MULTI, FORM>(A, ps, i);
+    if (i < A.n) pair_mixed_one<MULTI, FORM>(A, ps, i);
 }
 
 // ---- Langevin thermostat (langevin.cxx:29-42) ----------------------------------
@@ -522,10 +540,13 @@ int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int preci
         } else if (ps.any_eam) {
             if (multi) k_eam_mixed<true><<<nb, kBlock, 0, st>>>(A, dps);
             else k_eam_mixed<false><<<nb, kBlock, 0, st>>>(A, dps);
-        } else if (ps.any_tab) {
-            if (!multi) k_tab_mixed<false, 3><<<nb, kBlock, 0, st>>>(A, dps);
-            else if (ps.any_lj) k_tab_mixed<true, 0><<<nb, kBlock, 0, st>>>(A, dps);
-            else k_tab_mixed<true, 3><<<nb, kBlock, 0, st>>>(A, dps);
+        } else if (ps.any_tab || ps.any_ljs) {
+            const int kinds = ps.any_lj + ps.any_tab + ps.any_ljs;
+            if (!multi && ps.any_tab) k_pair_mixed<false, 3><<<nb, kBlock, 0, st>>>(A, dps);
+            else if (!multi) k_pair_mixed<false, 4><<<nb, kBlock, 0, st>>>(A, dps);
+            else if (kinds > 1) k_pair_mixed<true, 0><<<nb, kBlock, 0, st>>>(A, dps);
+            else if (ps.any_tab) k_pair_mixed<true, 3><<<nb, kBlock, 0, st>>>(A, dps);
+            else k_pair_mixed<true, 4><<<nb, kBlock, 0, st>>>(A, dps);
         } else {
             if (multi) k_lj_mixed<true><<<nb, kBlock, 0, st>>>(A, dps);
             else k_lj_mixed<false><<<nb, kBlock, 0, st>>>(A, dps);

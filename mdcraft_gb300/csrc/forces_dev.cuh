@@ -196,10 +196,24 @@ __device__ __forceinline__ float lj_ff32(const PotParams& P, float r2) {
     return P.mhf_f * fmaf(P.lj1_f, r6inv, -P.lj2_f) * r6inv * r2inv;
 }
 
-// Pair-type forces (no EAM term) where some kind pair uses the tabulated
-// Pair: FORM 3 = every pair tabulated, 0 = LJsCut or tabulated by kind pair.
+// Force / r of an LJs pair (LJs.cxx:153-166) in FP32.
+__device__ __forceinline__ float ljs_ff32(const PotParams& P, float r2) {
+    const float XX = fmaf(P.ljs_rVr1_f, r2, -1.2599210498948732f);
+    const float FV = P.ljs_rVr2_f * __fdividef(1.0f, fmaxf(r2, 1e-12f));
+    const float Ur = FV * FV * FV;
+    return P.ljs_aVr2_f * fmaf(Ur * (Ur - 0.5f), FV, fmaf(P.ljs_bLJ_f, XX, P.ljs_aLJ_f) * XX);
+}
+
+// Force / r of an analytic pair potential by type (LJsCut or LJs).
+__device__ __forceinline__ float analytic_ff32(const PotParams& P, float r2) {
+    return P.type == POT_LJS ? ljs_ff32(P, r2) : lj_ff32(P, r2);
+}
+
+// Pair-type forces (no EAM term) beyond the plain LJsCut kernel: FORM 3 =
+// every pair a tabulated Pair, 4 = every pair LJs, 0 = chosen per kind pair
+// among LJsCut, Pair and LJs.
 template <bool MULTI, int FORM>
-__device__ __forceinline__ void tab_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
+__device__ __forceinline__ void pair_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
     if (A.tag[i] == 0) return;
     const float4 pi = A.pos32[i];
     const int ng = A.ncnt[i] >> 2;
@@ -225,11 +239,13 @@ __device__ __forceinline__ void tab_mixed_one(const FArgs& A, const PotSet* __re
             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             bool in = pair_in(A, i, e[q], r2, P.r2cut_f, P.R2cut, per);
             float FF;
-            if (FORM == 3 || P.type == POT_TAB) {
+            if (FORM == 3 || (FORM == 0 && P.type == POT_TAB)) {
                 FF = tab_ff32(P, r2, in);
+            } else if (FORM == 4) {
+                FF = ljs_ff32(P, r2);
             } else {
-                in = in && P.type == POT_LJCUT;
-                FF = lj_ff32(P, r2);
+                in = in && (P.type == POT_LJCUT || P.type == POT_LJS);
+                FF = analytic_ff32(P, r2);
             }
             FF = in ? FF : 0.f;
             fx = fmaf(dx, FF, fx);
@@ -354,8 +370,8 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
                 P = &ps->p[ki][kj];
                 // a tabulated Pair has zero rho rows: the EAM arithmetic
                 // below reduces to its pair term exactly
-                eam = P->type >= POT_EAM;
-                lj = P->type == POT_LJCUT;
+                eam = P->type == POT_EAM || P->type == POT_TAB;
+                lj = P->type == POT_LJCUT || P->type == POT_LJS;
                 r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; rv = P->rv_c; R2c = P->R2cut;
                 Fpj = A.Fp32[(size_t)ki * A.np + j];
                 Fpi = A.Fp32[(size_t)kj * A.np + i];
@@ -378,7 +394,7 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
             float V = cubic(cv, u);
             float dV = dcubic(cv, u) * idr;
             float FF = fmaf(Fpi + Fpj, drho, (dV * r - V) * (rinv * rinv)) * rinv;
-            if (MULTI && lj) FF = lj_ff32(*P, r2);
+            if (MULTI && lj) FF = analytic_ff32(*P, r2);
             FF = in ? FF : 0.f;
             fx = fmaf(FF, dx, fx);
             fy = fmaf(FF, dy, fy);

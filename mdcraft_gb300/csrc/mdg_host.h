@@ -77,6 +77,9 @@ struct mdg_potential {
     double rcut = 0.0;
     // LJsCut
     double a = 0, s = 0, s6 = 0, lj1 = 0, lj2 = 0, factor = 0;
+    // LJs (LJs.cxx:7-29)
+    double ljs_rVr1 = 0, ljs_rVr2 = 0, ljs_aLJ = 0, ljs_bLJ = 0, ljs_aLJ3 = 0, ljs_bLJ2 = 0, ljs_aVr = 0,
+           ljs_aVr2 = 0;
     // EAM host tables (padded by one element) and device copies
     int Nr1 = 0, Nrh1 = 0;
     double dr = 0, drh = 0, dr1 = 0, drh1 = 0;

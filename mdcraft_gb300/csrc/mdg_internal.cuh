@@ -94,7 +94,7 @@ __device__ inline float image_shift(uint32_t e, int axis, float cs) {
 
 // Potential types: LJsCut and the tabulated Pair are the reference's
 // potential::type::pair (one force stage), EAM its potential::type::eam.
-enum : int { POT_NONE = 0, POT_LJCUT = 1, POT_EAM = 2, POT_TAB = 3 };
+enum : int { POT_NONE = 0, POT_LJCUT = 1, POT_EAM = 2, POT_TAB = 3, POT_LJS = 4 };
 
 // Per-kind-pair potential parameters handed to the force kernels by value.
 // Every table pointer is valid (a zero table stands in where a potential
@@ -107,6 +107,9 @@ struct PotParams {
     // LJsCut (LJs-cut.cxx:8-20)
     double a, s6, lj1, lj2, factor;
     float lj1_f, lj2_f, mhf_f;  // mhf = -0.5 * factor
+    // LJs (LJs.cxx:7-29), after its constructor's rescaling
+    double ljs_rVr1, ljs_rVr2, ljs_aLJ, ljs_bLJ, ljs_aLJ3, ljs_bLJ2, ljs_aVr, ljs_aVr2;
+    float ljs_rVr1_f, ljs_rVr2_f, ljs_aLJ_f, ljs_bLJ_f, ljs_aVr2_f;
     // EAM tables, FP64 values + knot slopes with one padding element
     int Nr1, Nrh1;
     double dr, drh, dr1, drh1;
@@ -129,7 +132,7 @@ struct PotSet {
     int multi;
     int any_eam;
     int periodic;     // boundary::Periodic
-    int any_lj, any_tab;
+    int any_lj, any_tab, any_ljs;
     PotParams p[kMaxKinds][kMaxKinds];
 };
 

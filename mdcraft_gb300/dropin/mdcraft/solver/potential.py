@@ -1,6 +1,6 @@
 """mdcraft.solver.potential (python/mdcraft/solver/potential/_potential.cxx):
-EAM (arrays or a setfl file), Pair (arrays or a file) and LJsCut on the GPU
-engine."""
+EAM (arrays or a setfl file), Pair (arrays or a file), LJs and LJsCut on the
+GPU engine."""
 from __future__ import annotations
 
 import numpy as np
@@ -35,6 +35,17 @@ class LJsCut:
         return self._p.rcut()
 
 
+class LJs:
+    """LJs(aVr, rVr, Rcutoff) (_potential.cxx:82-100)."""
+
+    def __init__(self, aVr: float, rVr: float, Rcutoff: float):
+        self._p = _mdg.LJs(aVr, rVr, Rcutoff)
+
+    @property
+    def rcut(self) -> float:
+        return self._p.rcut()
+
+
 class Pair:
     """Pair(Rcutoff, pairPotential, NrPot, drPot) or Pair(filename)
     (_potential.cxx:170-201): tabulated r*phi(r)."""
@@ -52,3 +63,7 @@ class Pair:
     @property
     def rcut(self) -> float:
         return self._p.rcut()
+
+
+# the reference's module also exports LJsCut under this name (_potential.cxx:110)
+LJsTEST = LJsCut

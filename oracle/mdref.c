@@ -595,6 +595,8 @@ struct md_pot {
     int Nr1, Nrh1;
     double dr, drh, dr1, drh1;
     double *Femb, *Rho, *Vpar, *dFemb, *dRho, *dVpar;
+    /* LJs (LJs.cxx:7-29, LJs.h:41) */
+    double aVr, aVr2, rVr, rVr1, rVr2, aLJ, aLJ3, bLJ, bLJ2;
 };
 
 md_pot* md_pot_ljcut_create(double a, double s, double rcut) {
@@ -721,6 +723,29 @@ md_pot* md_pot_pair_create(double rcut, const double* Vpar, int Nr1,
     p->dVpar = (double*)calloc((size_t)Nr1 + 1, sizeof(double));
     md_eam_init_spline(p->Vpar, p->dVpar, p->dr1, (size_t)Nr1, 1);
     p->dVpar[Nr1] = p->dVpar[Nr1 - 1];
+    return p;
+}
+
+md_pot* md_pot_ljs_create(double aVr, double rVr, double rcut) {
+    /* LJs::LJs (LJs.cxx:7-29), same operation order */
+    const double X2min = 1.2599210498948732;
+    md_pot* p = (md_pot*)calloc(1, sizeof(md_pot));
+    p->type = MD_POT_LJS;
+    p->R1cut = rcut;
+    p->R2cut = rcut * rcut;
+    double R2cut = p->R2cut;
+    p->rVr = rVr;
+    p->rVr2 = rVr * rVr;
+    p->rVr1 = 1.0 / p->rVr2;
+    p->aVr2 = R2cut / p->rVr2 - X2min;
+    p->aLJ3 = (p->rVr2 / R2cut) * (p->rVr2 / R2cut) * (p->rVr2 / R2cut);
+    p->bLJ2 = (p->aLJ3 - 0.5) * p->aVr2 * p->rVr2 / R2cut;
+    p->aLJ = (p->aLJ3 - 1.0 + 2.0 * p->bLJ2) * p->aLJ3 / (p->aVr2 * p->aVr2);
+    p->bLJ = -(p->aLJ3 - 1.0 + 3.0 * p->bLJ2) * p->aLJ3 / (p->aVr2 * p->aVr2 * p->aVr2);
+    p->aLJ3 = 3.0 * p->aLJ;
+    p->bLJ2 = 2.0 * p->bLJ;
+    p->aVr2 = -48.0 * aVr / p->rVr2;
+    p->aVr = 2.0 * aVr;
     return p;
 }
 
@@ -1130,6 +1155,75 @@ static void tab_virial(const md_pot* p, md_atom* a, const nview* v) {
     }
 }
 
+/* LJs pair terms (LJs.cxx:153-166 force/r, 90-101 energy V(r)/2) */
+static inline double ljs_ff(const md_pot* p, double r2, double* E) {
+    const double X2min = 1.2599210498948732;
+    double XX = p->rVr1 * r2 - X2min;
+    double FV = p->rVr2 / r2;
+    double Ur = FV * FV * FV;
+    if (E) *E = p->aVr * (Ur * (Ur - 1.0) - (p->aLJ3 + p->bLJ2 * XX) * XX * XX);
+    return p->aVr2 * (Ur * (Ur - 0.5) * FV + (p->aLJ + p->bLJ * XX) * XX);
+}
+
+/* LJs::force(self, ...) (LJs.cxx:196-256) */
+static void ljs_force(const md_pot* p, md_atom* a, const nview* v) {
+    double F[3] = {0.0, 0.0, 0.0};
+    for (size_t i = 0; i < v->nn; i++) {
+        double d[3] = {v->rj[i][0] - a->r[0], v->rj[i][1] - a->r[1], v->rj[i][2] - a->r[2]};
+        double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (r2 > p->R2cut || r2 < 1e-15) continue;
+        double FF = ljs_ff(p, r2, NULL);
+        if (v->nbp) {
+            for (int k = 0; k < 3; ++k) {
+                double G = FF * d[k];
+                a->f[k] += G;
+                v->nbp[i]->f[k] -= G;
+            }
+        } else {
+            F[0] += FF * d[0];
+            F[1] += FF * d[1];
+            F[2] += FF * d[2];
+        }
+    }
+    if (!v->nbp) {
+        a->f[0] += F[0];
+        a->f[1] += F[1];
+        a->f[2] += F[2];
+    }
+}
+
+/* LJs::virial(self, ...) (LJs.cxx:103-151) */
+static void ljs_virial(const md_pot* p, md_atom* a, const nview* v) {
+    double Vt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double Ut = 0.0;
+    for (size_t i = 0; i < v->nn; i++) {
+        double d[3] = {v->rj[i][0] - a->r[0], v->rj[i][1] - a->r[1], v->rj[i][2] - a->r[2]};
+        double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (r2 > p->R2cut || r2 < 1e-15) continue;
+        double E;
+        double FF = ljs_ff(p, r2, &E);
+        double G[3] = {FF * d[0], FF * d[1], FF * d[2]};
+        if (v->nbp) {
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 3; ++r) {
+                    double m = 0.5 * G[r] * d[c];
+                    a->V[r + 3 * c] += m;
+                    v->nbp[i]->V[r + 3 * c] += m;
+                }
+            a->Ep += E;
+            v->nbp[i]->Ep += E;
+        } else {
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 3; ++r) Vt[r + 3 * c] += 0.5 * G[r] * d[c];
+            Ut += E;
+        }
+    }
+    if (!v->nbp) {
+        for (int k = 0; k < 9; ++k) a->V[k] += Vt[k];
+        a->Ep += Ut;
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Langevin thermostat — mdcraft/solver/thermostat/langevin.cxx:8-42        */
 /* ------------------------------------------------------------------------ */
@@ -1242,7 +1336,7 @@ void md_solver_set_thermostat(md_solver* s, md_thermo* t, uint32_t calls) {
 uint32_t md_solver_thermo_calls(const md_solver* s) { return s->thermo_calls; }
 
 static int pair_type(const md_pot* p) {
-    return p->type == MD_POT_PAIR || p->type == MD_POT_TAB;
+    return p->type == MD_POT_PAIR || p->type == MD_POT_TAB || p->type == MD_POT_LJS;
 }
 
 static md_solver* solver_new(const md_domain* pd, int nthreads) {
@@ -1331,6 +1425,9 @@ static void pot_apply(md_pot* p, int op, md_atom* a, const nview* v, scratch* s)
     } else if (p->type == MD_POT_TAB) {
         if (op == 1) tab_force(p, a, v);
         else if (op == 2) tab_virial(p, a, v);
+    } else if (p->type == MD_POT_LJS) {
+        if (op == 1) ljs_force(p, a, v);
+        else if (op == 2) ljs_virial(p, a, v);
     } else if (p->type == MD_POT_EAM) {
         if (op == 0) eam_density(p, a, v, s);
         else if (op == 1) eam_force(p, a, v, s);

@@ -109,6 +109,7 @@ void md_nlist_grid(const md_nlist* nl, md_grid* out);
 #define MD_POT_PAIR 1
 #define MD_POT_EAM 2
 #define MD_POT_TAB 3
+#define MD_POT_LJS 4
 
 typedef struct md_pot md_pot;
 
@@ -120,6 +121,10 @@ md_pot* md_pot_eam_create(double rcut, const double* Femb, const double* Rho,
  * Vpar = r*phi(r) on a uniform grid of step dr. */
 md_pot* md_pot_pair_create(double rcut, const double* Vpar, int Nr1,
                            double dr);
+/* LJs(aVr, rVr, Rcutoff) (mdcraft/solver/potential/LJs.cxx:7-29): 4 aVr
+ * [(rVr/r)^12 - (rVr/r)^6] with a cubic in X = (r/rVr)^2 - 2^(1/3) that
+ * takes force and energy to zero at the cutoff. */
+md_pot* md_pot_ljs_create(double aVr, double rVr, double rcut);
 void md_pot_destroy(md_pot* p);
 double md_pot_rcut(const md_pot* p);
 int md_pot_type(const md_pot* p);

@@ -94,6 +94,8 @@ def lib():
         L.md_pot_eam_create.restype = vp
         L.md_pot_pair_create.argtypes = [dp, vp, ip, dp]
         L.md_pot_pair_create.restype = vp
+        L.md_pot_ljs_create.argtypes = [dp, dp, dp]
+        L.md_pot_ljs_create.restype = vp
         L.md_pot_destroy.argtypes = [vp]
         L.md_pot_rcut.argtypes = [vp]
         L.md_pot_rcut.restype = dp
@@ -340,6 +342,23 @@ class EAM:
         dF = C.c_double(0)
         lib().md_eam_embedding(self.h, rho, C.byref(F), C.byref(dF))
         return F.value, dF.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().md_pot_destroy(self.h)
+            self.h = None
+
+
+class LJs:
+    """mdcraft::solver::potential::LJs (LJs.h:14-18)."""
+
+    type = 4
+
+    def __init__(self, aVr: float, rVr: float, rcut: float):
+        self.h = lib().md_pot_ljs_create(aVr, rVr, rcut)
+
+    def rcut(self) -> float:
+        return lib().md_pot_rcut(self.h)
 
     def __del__(self):
         if getattr(self, "h", None):

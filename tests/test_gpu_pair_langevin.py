@@ -1,5 +1,5 @@
-"""GPU parity of the tabulated Pair potential (mdcraft/solver/potential/
-pair.cxx), of Multi solvers that mix potential types (multi.cxx:28-151), and
+"""GPU parity of the tabulated Pair and LJs potentials (mdcraft/solver/
+potential/pair.cxx, LJs.cxx), of Multi solvers that mix potential types (multi.cxx:28-151), and
 of the Langevin thermostat (mdcraft/solver/thermostat/langevin.cxx:29-42)
 against the CPU oracle.
 
@@ -37,6 +37,8 @@ def _spec_pots(spec):
     if kind == "eam":
         args = (t["rcut"], t["Femb"], t["Rho"], t["Vpar"], t["Nr1"], t["dr"], t["Nrh1"], t["drh"])
         return R.EAM(*args), mdg.EAM(*args)
+    if kind == "ljs":
+        return R.LJs(*t), mdg.LJs(*t)
     return R.LJsCut(*t), mdg.LJsCut(*t)
 
 
@@ -152,6 +154,51 @@ def test_multi_ljcut_with_pair(precision):
     pots = {(0, 0): ("lj", lj), (1, 1): ("pair", t), (0, 1): ("pair", t)}
     atoms, box = _fcc(5, 0.405, 5)
     atoms["kind"] = (np.arange(len(atoms)) % 3 == 0).astype(np.uint16)
+    o, g = _build(atoms, box, pots, t["rcut"], precision=precision)
+    ao, ag = _forces_both(o, g)
+    if precision == "fp64":
+        assert _rel(ag["f"], ao["f"]) < FP64_REL
+    else:
+        _, l2 = H.force_error(g["sys"].forces(), ao["f"])
+        assert l2 < MIXED_L2
+
+
+LJS = (0.9, 0.26, 0.62)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ljs_single(precision):
+    atoms, box = _fcc(6, 0.405, 10)
+    o, g = _build(atoms, box, ("ljs", LJS), LJS[2], precision=precision)
+    ao, ag = _forces_both(o, g)
+    assert np.abs(ao["f"]).max() > 1.0
+    if precision == "fp64":
+        assert _rel(ag["f"], ao["f"]) < FP64_REL
+        assert _rel(ag["Ep"], ao["Ep"]) < FP64_REL
+        assert _rel(ag["V"], ao["V"]) < FP64_REL
+    else:
+        _, l2 = H.force_error(g["sys"].forces(), ao["f"])
+        assert l2 < MIXED_L2
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_multi_all_four_potential_types(precision):
+    """EAM, LJs, Pair and (with three kinds) LJsCut in one Multi solver."""
+    al = S.al2009()
+    t = S.nialpair()
+    pots = {(0, 0): ("eam", al), (1, 1): ("ljs", LJS), (0, 1): ("pair", t)}
+    atoms, box = _fcc(5, 0.405, 11)
+    atoms["kind"] = (np.arange(len(atoms)) % 3 == 1).astype(np.uint16)
+    rc = max(al["rcut"], t["rcut"], LJS[2])
+    o, g = _build(atoms, box, pots, rc, precision=precision)
+    ao, ag = _forces_both(o, g)
+    if precision == "fp64":
+        assert _rel(ag["f"], ao["f"]) < FP64_REL
+        assert _rel(ag["Ep"], ao["Ep"]) < FP64_REL
+    else:
+        _, l2 = H.force_error(g["sys"].forces(), ao["f"])
+        assert l2 < MIXED_L2
+    pots = {(0, 0): ("lj", (0.5, 0.26, 0.55)), (1, 1): ("ljs", LJS), (0, 1): ("pair", t)}
     o, g = _build(atoms, box, pots, t["rcut"], precision=precision)
     ao, ag = _forces_both(o, g)
     if precision == "fp64":

@@ -1,11 +1,15 @@
-"""CPU checks of the oracle's tabulated Pair potential and Langevin
-thermostat, and of the product's Pair file reader (host code, no GPU).
+"""CPU checks of the oracle's tabulated Pair and LJs potentials and the
+Langevin thermostat, and of the product's Pair file reader (host code, no
+GPU).
 
 The reference's tests hold no golden values for these two, so the oracle is
 pinned by identities with pinned parts:
 - Pair::force/virial (mdcraft/solver/potential/pair.cxx:228-462) is the pair
   term of EAM::force/virial (EAM.cxx:306-497) with zero density tables, and
   the EAM arithmetic is pinned by the Al EAM golden test;
+- LJs (mdcraft/solver/potential/LJs.cxx) forces are minus the gradient of
+  its energies, and both vanish at the cutoff, which is what its cubic in
+  X = (r/rVr)^2 - 2^(1/3) is built for;
 - Philox4x32-10 reproduces the published known-answer vectors of Salmon et
   al. (SC'11, Random123 kat_vectors);
 - Langevin::apply_one (mdcraft/solver/thermostat/langevin.cxx:29-42) at zero
@@ -232,3 +236,38 @@ def test_product_pair_reader(tmp_path):
     short.write_text("\n".join(S.nialpair_text().splitlines()[:100]))
     with pytest.raises(mdg.MDGError):
         mdg.Pair.from_file(str(short))
+
+
+def _two_atoms(r, pot, rc):
+    atoms = R.new_atoms(2)
+    atoms["r"][1, 0] = r
+    atoms["m"] = 1.0
+    atoms["rcut"] = rc
+    atoms["rns"] = rc + 0.05
+    nl = R.VerletList(atoms, R.Domain(-2.0, 2.0, -2.0, 2.0, -2.0, 2.0), threads=1)
+    nl.update(-1.0)
+    s = R.Solver(pot, periodic=None, threads=1)
+    s.prepare(atoms)
+    s.forces(atoms, nl)
+    s.virials(atoms, nl)
+    return atoms
+
+
+def test_ljs_force_is_energy_gradient_and_vanishes_at_cutoff():
+    aVr, rVr, rc = 1.0, 0.34, 0.85
+    pot = R.LJs(aVr, rVr, rc)
+    for r in (0.33, 0.38, 0.5, 0.7):
+        h = 1e-6
+        up = _two_atoms(r + h, pot, rc)["Ep"].sum()
+        dn = _two_atoms(r - h, pot, rc)["Ep"].sum()
+        a = _two_atoms(r, pot, rc)
+        # atom 1 sits at +r on x: its force is -dU/dr
+        assert a["f"][1, 0] == pytest.approx(-(up - dn) / (2 * h), rel=1e-6)
+        assert a["f"][0, 0] == -a["f"][1, 0]
+        # the short-range limit is Lennard-Jones 4 aVr [(rVr/r)^12 - (rVr/r)^6] plus the smooth tail
+    near = _two_atoms(rc * (1 - 1e-7), pot, rc)
+    assert abs(near["Ep"].sum()) < 1e-9 and abs(near["f"][0, 0]) < 1e-5
+    assert _two_atoms(rc * (1 + 1e-7), pot, rc)["Ep"].sum() == 0.0
+    # V = 1/2 sum f_i (r_j - r_i): both sides give f_1 . (r_0 - r_1) / 2
+    a = _two_atoms(0.4, pot, rc)
+    assert (a["V"][:, 0]).sum() == pytest.approx(a["f"][1, 0] * -0.4, rel=1e-12)
