@@ -6,9 +6,11 @@
 //   tools::Threads             mdcraft/tools/threads.h:28-60   (no-op pool)
 //   neibs::ListOne / List      mdcraft/neibs/verlet-list.h:9-123
 //   neibs::VerletList          mdcraft/neibs/verlet-list.h:134-470
-//   solver::potential::Base, LJsCut, EAM   potential/{base,LJs-cut,EAM}.h
+//   solver::potential::Base, LJsCut, LJs, EAM, Pair
+//                                          potential/{base,LJs-cut,LJs,EAM,pair}.h
 //   solver::boundary::Base, Periodic       boundary/{base,periodic}.h
-//   solver::thermostat::Base               thermostat/base.h (no-op)
+//   solver::thermostat::Base, Langevin, Compound
+//                                          thermostat/{base,langevin,compound}.h
 //   solver::ISolver, Single, Multi         solver/{isolver,single,multi}.h
 //   solver::stepper::Verlet                solver/stepper/verlet.h
 //
@@ -27,6 +29,7 @@
 #include <functional>
 #include <limits>
 #include <memory>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -349,6 +352,26 @@ public:
     }
 };
 
+// LJs(aVr, rVr, Rcutoff) (LJs.h:14-18)
+class LJs : public Base {
+public:
+    LJs(double aVr, double rVr, double Rcutoff) : Base(Rcutoff, type::pair) {
+        gpu::check(mdg_pot_ljs_create(aVr, rVr, Rcutoff, &m_pot), "LJs");
+    }
+};
+
+// Pair(Rcutoff, Vpar, Nr1, dr) / Pair(filename) (pair.h:13-18)
+class Pair : public Base {
+public:
+    Pair(double Rcutoff, const double* Vpar, int Nr1, const double dr) : Base(Rcutoff, type::pair) {
+        gpu::check(mdg_pot_pair_create(Rcutoff, Vpar, Nr1, dr, &m_pot), "Pair");
+    }
+    explicit Pair(std::string filename) : Base(0.0, type::pair) {
+        gpu::check(mdg_pot_pair_create_from_file(filename.c_str(), &m_pot), "Pair(file)");
+        gpu::check(mdg_pot_rcut(m_pot, &m_rcut), "Pair rcut");
+    }
+};
+
 }  // namespace potential
 
 namespace boundary {
@@ -375,11 +398,88 @@ public:
 
 namespace thermostat {
 const double Kb = 0.008314462175;
+// thermostat::Base (thermostat/base.h): applies nothing.
 class Base {
 public:
-    virtual ~Base() = default;
+    virtual ~Base() {
+        if (m_t) mdg_thermo_destroy(m_t);
+    }
+    mdg_thermostat* handle() const { return m_t; }
+
+protected:
+    mdg_thermostat* m_t = nullptr;
 };
 inline Base dummy_thermostat;
+
+// Langevin(beta, temperature, time_step, heat_x, heat_y, heat_z, Ux, Uy, Uz,
+// xmin, xmax) (langevin.h:17-29). Like the reference it seeds its random
+// stream from std::random_device; set_seed makes a run repeatable.
+class Langevin : public Base {
+public:
+    Langevin(double beta, double temperature, double time_step, int heat_x = 1, int heat_y = 1, int heat_z = 1,
+             double Ux = 0.0, double Uy = 0.0, double Uz = 0.0, double xmin = -1e+15, double xmax = 1e+15) {
+        m_p.beta = beta;
+        m_p.temperature = temperature;
+        m_p.time_step = time_step;
+        m_p.heat[0] = heat_x;
+        m_p.heat[1] = heat_y;
+        m_p.heat[2] = heat_z;
+        m_p.U[0] = Ux;
+        m_p.U[1] = Uy;
+        m_p.U[2] = Uz;
+        m_p.xmin = xmin;
+        m_p.xmax = xmax;
+        std::random_device rd;
+        m_p.seed = ((uint64_t)rd() << 32) ^ (uint64_t)rd();
+        gpu::check(mdg_thermo_langevin_create(&m_p, &m_t), "Langevin");
+    }
+    void set_friction(double beta) {
+        m_p.beta = beta;
+        push();
+    }
+    void set_temperature(double T) {
+        m_p.temperature = T;
+        push();
+    }
+    void set_average_velocity(data::vector U) {
+        for (int k = 0; k < 3; ++k) m_p.U[k] = U[k];
+        push();
+    }
+    void set_heating_axes(int heat_x = 1, int heat_y = 1, int heat_z = 1) {
+        m_p.heat[0] = heat_x;
+        m_p.heat[1] = heat_y;
+        m_p.heat[2] = heat_z;
+        push();
+    }
+    void set_dimensions(double xmin, double xmax) {
+        m_p.xmin = xmin;
+        m_p.xmax = xmax;
+        push();
+    }
+    // GPU-specific: the Philox key of the random force
+    void set_seed(uint64_t seed) {
+        m_p.seed = seed;
+        push();
+    }
+    double friction() { return m_p.beta; }
+    double temperature() { return m_p.temperature; }
+    data::vector average_velocity() { return data::vector(m_p.U[0], m_p.U[1], m_p.U[2]); }
+    double xmin() { return m_p.xmin; }
+    double xmax() { return m_p.xmax; }
+
+private:
+    void push() { gpu::check(mdg_thermo_langevin_set(m_t, &m_p), "Langevin set"); }
+    mdg_langevin m_p{};
+};
+
+// Compound (thermostat/compound.h:12-24): its parts in the order added.
+class Compound : public Base {
+public:
+    Compound() { gpu::check(mdg_thermo_compound_create(&m_t), "Compound"); }
+    void add(Base& thermostat) {
+        if (thermostat.handle()) gpu::check(mdg_thermo_compound_add(m_t, thermostat.handle()), "Compound add");
+    }
+};
 }  // namespace thermostat
 
 using Potential = potential::Base;
@@ -432,9 +532,9 @@ class Single : public ISolver {
 public:
     Single(Potential& potential, Boundary& boundary = boundary::dummy_boundary,
            Thermostat& thermostat = thermostat::dummy_thermostat, tools::Threads& threads = tools::dummy_pool) {
-        (void)thermostat;
         (void)threads;
         gpu::check(mdg_solver_single(potential.handle(), boundary.periodic() ? 1 : 0, &m_s), "Single");
+        if (thermostat.handle()) gpu::check(mdg_solver_set_thermostat(m_s, thermostat.handle()), "thermostat");
         make_stages();
     }
 };
@@ -444,9 +544,9 @@ class Multi : public ISolver {
 public:
     Multi(Boundary& boundary = boundary::dummy_boundary, Thermostat& thermostat = thermostat::dummy_thermostat,
           std::size_t nkinds = 1, tools::Threads& threads = tools::dummy_pool) {
-        (void)thermostat;
         (void)threads;
         gpu::check(mdg_solver_multi((int)nkinds, boundary.periodic() ? 1 : 0, &m_s), "Multi");
+        if (thermostat.handle()) gpu::check(mdg_solver_set_thermostat(m_s, thermostat.handle()), "thermostat");
     }
     void add_potential(std::size_t i, std::size_t j, Potential& pot) {
         gpu::check(mdg_solver_add_potential(m_s, (int)i, (int)j, pot.handle()), "add_potential");

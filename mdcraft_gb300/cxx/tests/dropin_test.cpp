@@ -1,9 +1,12 @@
-// C++ drop-in test: MDcraft-style host code (VerletList / Single / EAM /
-// LJsCut / Periodic / stepper::Verlet, as test/cxx/solver/*.cxx and
-// test/cxx/neibs/test_verlet_list.cxx use them) compiled against the drop-in
-// headers and linked with libmdg. Asserts the reference tests' golden values.
+// C++ drop-in test: MDcraft-style host code (VerletList / Single / Multi /
+// EAM / LJsCut / LJs / Pair / Periodic / Langevin / stepper::Verlet, as
+// test/cxx/solver/*.cxx, test/cxx/neibs/test_verlet_list.cxx and
+// problems/NiAl/test-NiAl.py use them) compiled against the drop-in headers
+// and linked with libmdg. Asserts the reference tests' golden values, and
+// for the potentials those tests do not cover, energy conservation and the
+// Langevin thermostat's temperature.
 //
-// usage: dropin_test <LAMMPS Ar ball file> <Al setfl EAM file>
+// usage: dropin_test <LAMMPS Ar ball file> <Al setfl EAM file> [NiAl pair file]
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -16,8 +19,13 @@
 #include <mdcraft/neibs/verlet-list.h>
 #include <mdcraft/solver/boundary/periodic.h>
 #include <mdcraft/solver/potential/EAM.h>
+#include <mdcraft/solver/multi.h>
 #include <mdcraft/solver/potential/LJs-cut.h>
+#include <mdcraft/solver/potential/LJs.h>
+#include <mdcraft/solver/potential/pair.h>
 #include <mdcraft/solver/single.h>
+#include <mdcraft/solver/thermostat/compound.h>
+#include <mdcraft/solver/thermostat/langevin.h>
 #include <mdcraft/solver/stepper/verlet.h>
 #include <mdcraft/tools/threads.h>
 
@@ -286,6 +294,130 @@ static void test_aluminum(const std::string& path) {
     CHECK(nlist[0].size() > 12U);
 }
 
+static Atoms fcc_lattice(int n, double a0, double mass, unsigned seed_kinds) {
+    Atoms atoms;
+    const vector basis[4] = {vector(0, 0, 0), vector(0.5, 0.5, 0), vector(0.5, 0, 0.5), vector(0, 0.5, 0.5)};
+    const double L = n * a0;
+    unsigned uid = 1, h = seed_kinds;
+    for (int iz = 0; iz < n; ++iz)
+        for (int iy = 0; iy < n; ++iy)
+            for (int ix = 0; ix < n; ++ix) {
+                vector co(-0.5 * L + ix * a0, -0.5 * L + iy * a0, -0.5 * L + iz * a0);
+                for (const auto& b : basis) {
+                    Atom at{};
+                    at.uid = uid++;
+                    h = h * 1664525u + 1013904223u;
+                    at.kind = seed_kinds ? (unsigned short)((h >> 16) % 5 == 0) : 0;
+                    at.m = mass;
+                    at.r = co + a0 * b;
+                    // a small deterministic displacement so that forces are nonzero
+                    at.r += vector(1e-3 * std::sin(1.0 * uid), 1e-3 * std::cos(2.0 * uid), 1e-3 * std::sin(3.0 * uid));
+                    atoms.push_back(at);
+                }
+            }
+    return atoms;
+}
+
+template <class Solver>
+static double total_energy(Solver& solver, Atoms& atoms, neibs::VerletList& nlist) {
+    solver.virials(atoms, atoms, nlist.get());
+    return measure(atoms).Etot;
+}
+
+// problems/NiAl/test-NiAl.py: two EAM kinds, the Ni-Al Pair from its file as
+// cross term, Multi with Periodic; then LJs in a Single solver. NVE energy
+// must hold, the total force must vanish.
+static void test_pair_and_ljs(const std::string& al_path, const std::string& pair_path) {
+    const double a0 = 0.405, mass = 26.9815384, dt = 1e-3;
+    tools::Threads threads{1};
+    solver::potential::EAM al{al_path};
+    solver::potential::Pair cross{pair_path};
+    CHECK_NEAR(cross.rcut(), 0.6724883999724820, 1e-15);
+    for (int form = 0; form < 2; ++form) {
+        Atoms atoms = fcc_lattice(5, a0, mass, form == 0 ? 7u : 0u);
+        const double L = 5 * a0;
+        lattice::Domain domain(-0.5 * L, 0.5 * L, -0.5 * L, 0.5 * L, -0.5 * L, 0.5 * L);
+        for (int k = 0; k < 3; ++k) domain.set_periodic(k, true);
+        solver::boundary::Periodic periodic(domain);
+        solver::potential::LJs ljs(0.9, 0.26, 0.62);
+        std::unique_ptr<solver::ISolver> solver;
+        double rc;
+        if (form == 0) {
+            auto m = std::make_unique<solver::Multi>(periodic, solver::thermostat::dummy_thermostat, 2, threads);
+            m->add_potential(0, 0, al);
+            m->add_potential(1, 1, al);
+            m->add_potential(0, 1, cross);
+            CHECK(m->stages.size() == 2U);
+            rc = std::max(al.rcut(), cross.rcut());
+            solver = std::move(m);
+        } else {
+            solver = std::make_unique<solver::Single>(ljs, periodic, solver::thermostat::dummy_thermostat, threads);
+            CHECK(solver->stages.size() == 1U);
+            rc = ljs.rcut();
+        }
+        for (auto& at : atoms) {
+            at.rcut = rc;
+            at.rns = 1.2 * rc;
+        }
+        solver::stepper::Verlet stepper(*solver, threads);
+        neibs::VerletList nlist(atoms, atoms, domain, threads);
+        nlist.update(-1.0);
+        solver->prepare(atoms, atoms, nlist.get());
+        for (auto& st : solver->stages) st(atoms, atoms, nlist.get());
+        vector ftot = vector::Zero();
+        double fmax = 0.0;
+        for (const auto& at : atoms) {
+            ftot += at.f;
+            fmax = std::max(fmax, at.f.norm());
+        }
+        CHECK(fmax > 1.0);
+        CHECK(ftot.norm() < 1e-9 * fmax * atoms.size());
+        const double e0 = total_energy(*solver, atoms, nlist);
+        for (int s = 1; s <= 300; ++s) {
+            stepper.make_step(atoms, nlist.get(), dt);
+            if (nlist.decide()) nlist.update(-1.0);
+        }
+        const double e1 = total_energy(*solver, atoms, nlist);
+        CHECK_NEAR((e1 - e0) / std::fabs(e0), 0.0, 2e-5);
+    }
+}
+
+// A Langevin thermostat (langevin.cxx:29-42) brings a cold lattice to its
+// temperature: <KE> -> 3/2 N kB T over the last steps of the run.
+static void test_langevin(const std::string& al_path) {
+    const double a0 = 0.4032, mass = 26.9815384, dt = 2e-3, T = 300.0;
+    tools::Threads threads{1};
+    solver::potential::EAM al{al_path};
+    Atoms atoms = fcc_lattice(5, a0, mass, 0u);
+    const double L = 5 * a0;
+    lattice::Domain domain(-0.5 * L, 0.5 * L, -0.5 * L, 0.5 * L, -0.5 * L, 0.5 * L);
+    for (int k = 0; k < 3; ++k) domain.set_periodic(k, true);
+    solver::boundary::Periodic periodic(domain);
+    solver::thermostat::Langevin langevin(5.0, T, dt);
+    langevin.set_seed(42);
+    solver::thermostat::Compound compound;
+    compound.add(langevin);
+    solver::Single solver(al, periodic, compound, threads);
+    set_common(atoms, mass, al.rcut(), 1.25);
+    solver::stepper::Verlet stepper(solver, threads);
+    neibs::VerletList nlist(atoms, atoms, domain, threads);
+    nlist.update(-1.0);
+    double ke = 0.0;
+    int samples = 0;
+    for (int s = 1; s <= 3000; ++s) {
+        stepper.make_step(atoms, nlist.get(), dt);
+        if (nlist.decide()) nlist.update(-1.0);
+        if (s > 1500 && s % 10 == 0) {
+            ke += measure(atoms).KE;
+            ++samples;
+        }
+    }
+    const double t_kin = (ke / samples) / (1.5 * atoms.size() * solver::thermostat::Kb);
+    std::printf("Langevin: <T_kin> = %.1f K (target %.1f K)\n", t_kin, T);
+    CHECK(std::fabs(t_kin - T) < 0.1 * T);
+    CHECK_NEAR(langevin.temperature(), T, 0.0);
+}
+
 int main(int argc, char** argv) {
     if (argc < 3) {
         std::printf("usage: %s <LAMMPS Ar ball> <Al setfl>\n", argv[0]);
@@ -294,6 +426,8 @@ int main(int argc, char** argv) {
     test_verlet_lists();
     test_argon_ball(argv[1]);
     test_aluminum(argv[2]);
+    if (argc > 3) test_pair_and_ljs(argv[2], argv[3]);
+    test_langevin(argv[2]);
     std::printf("%d checks, %d failures\n", g_checks, g_fail);
     return g_fail == 0 ? 0 : 1;
 }

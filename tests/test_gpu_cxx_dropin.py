@@ -38,9 +38,11 @@ def test_cxx_dropin_reference_tests_on_gpu(tmp_path):
     _compile(exe)
     ball = tmp_path / "LMP_BALL_130k_Ar"
     al = tmp_path / "Al2009.eam.alloy"
+    pair = tmp_path / "NiAlpair.eam.alloy"
     ball.write_bytes(lzma.decompress(open(os.path.join(GOLDEN, "lmp_ball_130k_ar.xz"), "rb").read()))
     al.write_bytes(lzma.decompress(open(os.path.join(GOLDEN, "al2009_eam_alloy.xz"), "rb").read()))
-    r = subprocess.run([exe, str(ball), str(al)], capture_output=True, text=True, timeout=600)
+    pair.write_bytes(lzma.decompress(open(os.path.join(GOLDEN, "nialpair_eam_alloy.xz"), "rb").read()))
+    r = subprocess.run([exe, str(ball), str(al), str(pair)], capture_output=True, text=True, timeout=600)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "0 failures" in r.stdout
