@@ -225,23 +225,181 @@ __global__ void k_cells(int n, const double* __restrict__ rx, const double* __re
 }
 
 // ---------------------------------------------------------------------------
-// Verlet list: one warp per cell, lanes over the cell's atoms
+// Verlet list
 // ---------------------------------------------------------------------------
 
+// ---- list build, a warp per cell with lanes over candidates -------------------
+// The cell's candidates are the atoms of its neighbour cells in the
+// reference's cell order (x outer, z inner), each cell's atoms in slot order.
+// Lanes take 32 consecutive candidates; the warp then walks the cell's atoms
+// and appends, for each, the accepted lanes in lane order (ballot + popc).
+// Entry order per atom is therefore the order of the per-atom loop in
+// nbuild_bin, and the lists are the same, entry for entry. Used when no
+// periodic axis has 3 cells or fewer (no minimum-image adjustment of the
+// image code); otherwise nbuild_bin runs.
+struct NbWarpSmem {
+    uint32_t cj0[27];        // first slot of each non-empty neighbour cell
+    uint32_t cpre[28];       // candidate prefix over those cells
+    uint32_t ccode[27];      // image code << kJBits
+    float4 csh[27];          // cell shift (x, y, z) of the image
+    float4 oi[32];           // the batch's offsets
+    double xi[32], yi[32], zi[32], rni[32];
+    uint32_t origi[32];
+};
 
-// 64 registers (four blocks per SM) measured fastest: EAM Cu 1M rebuild
-// 2.6 ms against 3.3 ms with the compiler's unbounded choice.
-constexpr int kNbuildMinBlocks = 4;
-template <int WIDTH>
-__global__ void __launch_bounds__(kBlock, kNbuildMinBlocks) k_nbuild(NbArgs A, const GridParams* __restrict__ gp) {
+constexpr int kNbWarps = 4;
+
+__device__ __forceinline__ void nbuild_cell_warp(const NbArgs& A, const GridParams& g, int bin, int lane,
+                                                 bool uniform_rns, NbWarpSmem& S) {
+    const unsigned full = 0xffffffffu;
+    const float lo2 = (float)(g.max_rns * g.max_rns * (1.0 - 1e-5));
+    const float hi2 = (float)(g.max_rns * g.max_rns * (1.0 + 1e-5));
+    const uint32_t s0 = A.bin_start[bin], s1 = A.bin_start[bin + 1];
+    if (s0 == s1) return;
+    int cx, cy, cz;
+    unpack_cell(A.cellp[s0], cx, cy, cz);
+    int gc[3] = {cx + g.offset[0], cy + g.offset[1], cz + g.offset[2]};
+    if (g.dim < 3) gc[2] = 0;
+    if (g.dim < 2) gc[1] = 0;
+    bool edge[3] = {false, false, false};
+    for (int a = 0; a < g.dim; ++a) edge[a] = gc[a] == 0 || gc[a] == g.num[a] - 1;
+
+    // lane t < 27: neighbour cell (t / 9 - 1, t / 3 % 3 - 1, t % 3 - 1)
+    bool valid = false;
+    uint32_t j0 = 0, ncand = 0, code = 0;
+    float4 sh = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lane < 27) {
+        const int dl[3] = {lane / 9 - 1, (lane / 3) % 3 - 1, lane % 3 - 1};
+        valid = true;
+        for (int a = 0; a < 3; ++a)
+            if (g.periodic[a] && ((g.dom_n[a] == 1 && dl[a] != 0) || (g.dom_n[a] == 2 && dl[a] == 1))) valid = false;
+        if (valid) {
+            int nb[3] = {gc[0] + dl[0], gc[1] + dl[1], gc[2] + dl[2]};
+            for (int a = 0; a < 3; ++a)
+                if (g.periodic[a]) nb[a] = (nb[a] + g.dom_n[a]) % g.dom_n[a];
+            const int lc[3] = {nb[0] - g.offset[0], nb[1] - g.offset[1], nb[2] - g.offset[2]};
+            if (lc[0] < 0 || lc[0] >= g.num[0] || lc[1] < 0 || lc[1] >= g.num[1] || lc[2] < 0 || lc[2] >= g.num[2]) {
+                valid = false;
+            } else {
+                const int bk = bin_key(g, lc[0], lc[1], lc[2]);
+                j0 = A.bin_start[bk];
+                ncand = A.bin_start[bk + 1] - j0;
+                sh = make_float4((float)dl[0] * g.csf[0], (float)dl[1] * g.csf[1], (float)dl[2] * g.csf[2], 0.f);
+                const int own[3] = {cx, cy, cz};
+                for (int a = 0; a < 3; ++a) {
+                    code |= (uint32_t)(dl[a] + 1) << (2 * a);
+                    if (dl[a] != lc[a] - own[a]) code |= 1u << 6;  // the image crossed a periodic face
+                }
+            }
+        }
+    }
+    const bool use = valid && ncand > 0;
+    const unsigned vm = __ballot_sync(full, use);
+    const int slot = __popc(vm & ((1u << lane) - 1u));
+    const int nc = __popc(vm);
+    uint32_t incl = use ? ncand : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(full, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (use) {
+        S.cj0[slot] = j0;
+        S.cpre[slot] = incl - ncand;
+        S.ccode[slot] = code << kJBits;
+        S.csh[slot] = sh;
+    }
+    const uint32_t T = __shfl_sync(full, incl, 31);
+    if (lane == 0) S.cpre[nc] = T;
+    __syncwarp();
+
+    const unsigned lt = (1u << lane) - 1u;
+    for (uint32_t base = s0; base < s1; base += 32) {
+        const uint32_t ni = s1 - base < 32u ? s1 - base : 32u;
+        const bool act = (uint32_t)lane < ni;
+        const uint32_t me = base + lane;
+        if (act) {
+            S.oi[lane] = A.o0[me];
+            S.xi[lane] = A.rx[me];
+            S.yi[lane] = A.ry[me];
+            S.zi[lane] = A.rz[me];
+            S.rni[lane] = A.rns[me];
+            S.origi[lane] = A.orig[me];
+        }
+        __syncwarp();
+        int cnt = 0;  // list length of atom `me`
+        int c = 0;    // neighbour cell of this lane's candidate
+        for (uint32_t tb = 0; tb < T; tb += 32) {
+            const uint32_t t = tb + lane;
+            const bool have = t < T;
+            uint32_t j = 0, jcode = 0;
+            float4 oj = make_float4(0.f, 0.f, 0.f, 0.f), shj = oj;
+            uint32_t origj = 0;
+            if (have) {
+                while (S.cpre[c + 1] <= t) ++c;
+                j = S.cj0[c] + (t - S.cpre[c]);
+                oj = A.o0[j];
+                shj = S.csh[c];
+                jcode = S.ccode[c];
+                if (A.half) origj = A.orig[j];
+            }
+            for (uint32_t ii = 0; ii < ni; ++ii) {
+                const float4 oi = S.oi[ii];
+                const uint32_t i = base + ii;
+                bool acc = false;
+                if (have && j != i && !(A.half && origj < S.origi[ii])) {
+                    const float dx = oi.x - oj.x - shj.x;
+                    const float dy = oi.y - oj.y - shj.y;
+                    const float dz = oi.z - oj.z - shj.z;
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    const bool pf = uniform_rns && oi.w == 0.0f && oj.w == 0.0f;
+                    if (pf && d2 < lo2) acc = true;
+                    else if (pf && d2 > hi2) acc = false;
+                    else
+                        acc = are_neibs_exact(g, S.xi[ii], S.yi[ii], S.zi[ii], S.rni[ii], A.rx[j], A.ry[j], A.rz[j],
+                                              A.rns[j], edge);
+                }
+                const unsigned m = __ballot_sync(full, acc);
+                const int ci = __shfl_sync(full, cnt, ii);
+                if (acc) {
+                    const int k = ci + __popc(m & lt);
+                    if (k < A.K) A.nbr[nidx(k, i, A.np)] = j | jcode;
+                }
+                if ((uint32_t)lane == ii) cnt += __popc(m);
+            }
+        }
+        if (act) {
+            const int padded = (cnt + 3) & ~3;
+            for (int k = cnt; k < padded && k < A.K; ++k) A.nbr[nidx(k, me, A.np)] = me | kSelfCode;
+            A.ncnt[me] = padded < A.K ? padded : A.K;
+            if (cnt > A.K) {
+                atomicOr(&A.st->flags, FLAG_OVERFLOW);
+                atomicOr(&A.st->build_flags, FLAG_OVERFLOW);
+            }
+            atomicMax(&A.st->max_count, (uint32_t)cnt);
+            A.r0x[me] = S.xi[lane];
+            A.r0y[me] = S.yi[lane];
+            A.r0z[me] = S.zi[lane];
+            A.saved_rcut[me] = A.rcut[me];
+            A.saved_rns[me] = S.rni[lane];
+            A.saved_uid[me] = A.uid[me];
+        }
+        __syncwarp();
+    }
+}
+
+// Block of kNbWarps warps, a warp per bin; bins of grids with a periodic
+// axis of 3 cells or fewer take the per-atom body.
+__global__ void __launch_bounds__(kNbWarps * 32, 8) k_nbuild_warp(NbArgs A, const GridParams* __restrict__ gp) {
     __shared__ GridParams g;
+    __shared__ NbWarpSmem S[kNbWarps];
     if (threadIdx.x == 0) g = *gp;
     __syncthreads();
-    // WIDTH lanes per bin (16 or 32)
-    int bin = (blockIdx.x * blockDim.x + threadIdx.x) / WIDTH;
-    int lane = threadIdx.x & (WIDTH - 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bin = blockIdx.x * kNbWarps + warp;
     if (g.empty || bin >= g.nbins) return;
-    nbuild_bin(A, g, bin, lane, A.st->nonuniform == 0, WIDTH);
+    const bool uniform = A.st->nonuniform == 0;
+    if (g.small_box) nbuild_bin(A, g, bin, lane, uniform, 32);
+    else nbuild_cell_warp(A, g, bin, lane, uniform, S[warp]);
 }
 
 // VerletList::optimize_search_radius (verlet-list.cxx:72-92):
@@ -496,11 +654,6 @@ DomainDev domain_of(const mdg_system* sys) { return domain_dev(sys); }
 
 // Lanes per cell of the list build: 16, or 32 when the cells of the last
 // sized grid hold more than 16 atoms on average.
-static int nb_width(const mdg_system* sys) {
-    const GridParams& g = sys->grid;
-    double cells = (double)g.num[0] * g.num[1] * g.num[2];
-    return cells > 0 && (double)sys->n > 16.0 * cells ? 32 : 16;
-}
 
 int nlist_enqueue(mdg_system* sys) {
     mdg_ctx* ctx = sys->ctx;
@@ -571,8 +724,8 @@ int nlist_enqueue(mdg_system* sys) {
     NbArgs A = nb_args(sys);
     // a half warp per bin of the capacity (a whole warp where cells hold more
     // than 16 atoms on average); the live bins come from the device grid
-    if (nb_width(sys) == 32) k_nbuild<32><<<nblk(sys->bin_cap * 32), kBlock, 0, st>>>(A, sys->dgrid);
-    else k_nbuild<16><<<nblk(sys->bin_cap * 16), kBlock, 0, st>>>(A, sys->dgrid);
+    const unsigned nbw = (unsigned)((sys->bin_cap + kNbWarps - 1) / kNbWarps);
+    k_nbuild_warp<<<nbw, kNbWarps * 32, 0, st>>>(A, sys->dgrid);
     MDG_LAUNCHED(ctx);
     return MDG_OK;
 }
