@@ -141,6 +141,17 @@ __global__ void k_vec_out(int n, const uint32_t* __restrict__ slot_of, const dou
     out[3 * k + 2] = z[s];
 }
 
+// Forces of the mixed form (FP32) into caller-order doubles.
+__global__ void k_vec_out32(int n, const uint32_t* __restrict__ slot_of, const float* x, const float* y,
+                            const float* z, double* __restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t s = slot_of[k];
+    out[3 * k] = (double)x[s];
+    out[3 * k + 1] = (double)y[s];
+    out[3 * k + 2] = (double)z[s];
+}
+
 __global__ void k_iota(int n, uint32_t* a, uint32_t* b) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) {
@@ -331,6 +342,13 @@ void system_free(mdg_system* sys) {
     sys_free(sys, sys->part, sys->part_cap * 8 * sizeof(double));
     sys_free(sys, sys->nbr, (size_t)sys->K * sys->np * sizeof(uint32_t));
     sys_free(sys, sys->xfer, sys->xfer_bytes);
+    sys_free(sys, sys->step_io, sys->step_io_bytes);
+    sys->step_io = nullptr;
+    sys->step_io_bytes = 0;
+    for (cudaEvent_t& e : sys->step_ev) {
+        if (e) cudaEventDestroy(e);
+        e = nullptr;
+    }
     if (!sys->host_borrowed) {
         if (sys->hcounter) cudaFreeHost(sys->hcounter);
         cudaFreeHost(sys->hgrid);
@@ -626,6 +644,7 @@ static void ctx_release(mdg_ctx* ctx) {
         }
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
+    if (ctx->io_stream) cudaStreamDestroy(ctx->io_stream);
     delete ctx;
 }
 
@@ -1964,6 +1983,146 @@ int run_async_end(mdg_solver* s, mdg_system* sys, double dt, int* relaunched) {
 
 }  // namespace mdg
 
+// One step from host buffers with transfers overlapped with the step:
+// velocities arrive on the I/O stream while the positions-only prepare and
+// list test run; positions leave on the I/O stream once the drift has moved them,
+// forces once the force stage is done, velocities after the kick; uploads
+// and the step run on the engine's stream. A rebuild at the end of the step
+// (it wraps positions) waits for the reads of the permuted arrays and sends
+// the positions again. Needs page-locked host buffers (the caller's pinned
+// memory); otherwise mdg_run_host takes the graph path.
+static int run_host_step(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt, double* pos, double* vel,
+                         double* force) {
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    const size_t n = sys->n;
+    const size_t vb = n * 3 * sizeof(double);
+    if (!ctx->io_stream) MDG_CUDA(cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking));
+    cudaStream_t io = ctx->io_stream;
+    if (sys->step_io_bytes < 3 * vb) {
+        sys_free(sys, sys->step_io, sys->step_io_bytes);
+        sys->step_io = nullptr;
+        sys->step_io_bytes = 0;
+        int rc = sys_malloc(sys, (void**)&sys->step_io, 3 * vb);
+        if (rc) return rc;
+        sys->step_io_bytes = 3 * vb;
+    }
+    for (cudaEvent_t& e : sys->step_ev)
+        if (!e) MDG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    cudaEvent_t ev_flag = sys->step_ev[0], ev_drift = sys->step_ev[1], ev_pos_sent = sys->step_ev[2],
+                ev_forces = sys->step_ev[3], ev_reads = sys->step_ev[4], ev_io_done = sys->step_ev[5],
+                ev_vel_in = sys->step_ev[6];
+    double* xp = sys->step_io;
+    double* xf = sys->step_io + 3 * n;
+    double* xv = sys->step_io + 6 * n;
+    const int prec = s->precision;
+    const int nb = (int)((n + kBlock - 1) / kBlock);
+
+    // positions in on the engine's stream, velocities on the I/O stream
+    // (through the velocity staging slot) while the positions-only prepare
+    // and list test run
+    int rc = vec_io(sys, pos, RX, 1, 0);
+    if (rc) return rc;
+    int c = sys->cur;
+    MDG_CUDA(cudaMemcpyAsync(xv, vel, vb, cudaMemcpyHostToDevice, io));
+    k_vec_in<<<nb, kBlock, 0, io>>>((int)n, sys->slot_of, xv, sys->f64[VX][c], sys->f64[VY][c], sys->f64[VZ][c]);
+    MDG_LAUNCHED(ctx);
+    MDG_CUDA(cudaEventRecord(ev_vel_in, io));
+    if (prec == MDG_PREC_MIXED) {
+        // prepare (rcut, boundary flags) with the list test in one pass, and
+        // a rebuild first when the uploaded positions left the list's skin
+        MDG_CUDA(cudaMemsetAsync(&sys->dstat->need_rebuild, 0, sizeof(uint32_t), st));
+        rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 1);
+        if (rc) return rc;
+        MDG_CUDA(cudaMemcpyAsync(&sys->hstat->need_rebuild, &sys->dstat->need_rebuild, sizeof(uint32_t),
+                                 cudaMemcpyDeviceToHost, st));
+        MDG_CUDA(cudaStreamSynchronize(st));
+        if (sys->hstat->need_rebuild) {
+            MDG_CUDA(cudaStreamWaitEvent(st, ev_vel_in, 0));  // the rebuild permutes the velocities
+            rc = nlist_build(sys, -1.0, 0);
+            if (rc && rc != MDG_ERR_RANGE) return rc;
+            rc = launch_trig(sys);
+            if (rc) return rc;
+            c = sys->cur;
+        }
+        rc = launch_offsets(sys);
+        if (rc) return rc;
+    }
+    MDG_CUDA(cudaStreamWaitEvent(st, ev_vel_in, 0));
+    if (sys->force_prec != prec) {
+        rc = launch_force_copy(sys, prec == MDG_PREC_FP64);
+        if (rc) return rc;
+        sys->force_prec = prec;
+    }
+    MDG_CUDA(cudaMemsetAsync(&sys->dstat->need_rebuild, 0, sizeof(uint32_t), st));
+    rc = launch_drift(sys, dt, prec, pot_rcut_of(s), s->periodic, 1, 1);
+    if (rc) return rc;
+    MDG_CUDA(cudaMemcpyAsync(&sys->hstat->need_rebuild, &sys->dstat->need_rebuild, sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaEventRecord(ev_flag, st));
+    MDG_CUDA(cudaEventRecord(ev_drift, st));
+    // positions are final for this step (a rebuild below may wrap them)
+    MDG_CUDA(cudaStreamWaitEvent(io, ev_drift, 0));
+    k_vec_out<<<nb, kBlock, 0, io>>>((int)n, sys->slot_of, sys->f64[RX][c], sys->f64[RY][c], sys->f64[RZ][c], xp);
+    MDG_LAUNCHED(ctx);
+    MDG_CUDA(cudaMemcpyAsync(pos, xp, vb, cudaMemcpyDeviceToHost, io));
+    MDG_CUDA(cudaEventRecord(ev_pos_sent, io));
+    for (int q = 0; q < s->nstages; ++q) {
+        rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q], thermo_of(s));
+        if (rc) return rc;
+    }
+    sys->force_prec = prec;
+    if (force) {
+        MDG_CUDA(cudaEventRecord(ev_forces, st));
+        MDG_CUDA(cudaStreamWaitEvent(io, ev_forces, 0));
+        if (prec == MDG_PREC_MIXED)
+            k_vec_out32<<<nb, kBlock, 0, io>>>((int)n, sys->slot_of, sys->f32[0][c], sys->f32[1][c], sys->f32[2][c], xf);
+        else
+            k_vec_out<<<nb, kBlock, 0, io>>>((int)n, sys->slot_of, sys->f64[FX][c], sys->f64[FY][c], sys->f64[FZ][c], xf);
+        MDG_LAUNCHED(ctx);
+    }
+    // the I/O stream's reads of the permuted arrays end here
+    MDG_CUDA(cudaEventRecord(ev_reads, io));
+    if (force) MDG_CUDA(cudaMemcpyAsync(force, xf, vb, cudaMemcpyDeviceToHost, io));
+    MDG_CUDA(cudaEventRecord(ev_io_done, io));
+    rc = launch_kick(sys, dt, prec);
+    if (rc) return rc;
+    k_vec_out<<<nb, kBlock, 0, st>>>((int)n, sys->slot_of, sys->f64[VX][c], sys->f64[VY][c], sys->f64[VZ][c], xv);
+    MDG_LAUNCHED(ctx);
+    MDG_CUDA(cudaMemcpyAsync(vel, xv, vb, cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaEventSynchronize(ev_flag));
+    if (sys->hstat->need_rebuild) {
+        // the rebuild permutes what the I/O stream reads
+        MDG_CUDA(cudaStreamWaitEvent(st, ev_reads, 0));
+        rc = nlist_build(sys, -1.0, 0);
+        if (rc && rc != MDG_ERR_RANGE) return rc;
+        rc = launch_trig(sys);
+        if (rc) return rc;
+        if (prec == MDG_PREC_MIXED) {
+            rc = launch_offsets(sys);
+            if (rc) return rc;
+        }
+        c = sys->cur;
+        MDG_CUDA(cudaStreamWaitEvent(st, ev_pos_sent, 0));
+        k_vec_out<<<nb, kBlock, 0, st>>>((int)n, sys->slot_of, sys->f64[RX][c], sys->f64[RY][c], sys->f64[RZ][c], xp);
+        MDG_LAUNCHED(ctx);
+        MDG_CUDA(cudaMemcpyAsync(pos, xp, vb, cudaMemcpyDeviceToHost, st));
+    }
+    MDG_CUDA(cudaStreamWaitEvent(st, ev_io_done, 0));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    return MDG_OK;
+}
+
+static bool page_locked(const void* p) {
+    if (!p) return true;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 extern "C" {
 
 int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
@@ -2064,6 +2223,11 @@ done:
 int mdg_run_host(mdg_solver* s, mdg_system* sys, double dt, long steps, double* pos, double* vel, double* force) {
     if (!s || !sys || !pos || !vel) return MDG_ERR_INVALID;
     PotSet ps;
+    if (steps == 1 && !sys->ctx->timing && sys->n > 0 && !sys->half && check_ready(s, sys, &ps) == MDG_OK &&
+        page_locked(pos) && page_locked(vel) && page_locked(force)) {
+        MDG_CUDA(cudaSetDevice(sys->ctx->device));
+        return run_host_step(s, sys, ps, dt, pos, vel, force);
+    }
     if (steps > 0 && !sys->ctx->timing && sys->n > 0 && !sys->half && check_ready(s, sys, &ps) == MDG_OK) {
         // the whole call in stream order with one wait: uploads, the graph
         // loop, its status read-back, the downloads (the transfer buffer is

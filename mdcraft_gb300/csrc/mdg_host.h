@@ -45,6 +45,7 @@ struct DevArray {
 struct mdg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t io_stream = nullptr;  // result downloads overlapped with a step (created on first use)
     uint64_t launches = 0;
     int num_sms = 0;
     // lifetime: the caller's handle plus one per live system; the context
@@ -192,6 +193,11 @@ struct mdg_system {
     size_t xfer_bytes = 0;
     size_t dev_bytes = 0;  // device bytes held now
     int lazy_init = 0;     // buffers cleared by their first kernel (fused loop), not on the stream
+    // one-step host runs: caller-order staging of positions, forces and
+    // velocities (3 x n x 3 doubles) and the events that order them
+    double* step_io = nullptr;
+    size_t step_io_bytes = 0;
+    cudaEvent_t step_ev[7] = {};
 
     double* cur64(int f) { return f64[f][cur]; }
     float* cur32(int c) { return f32[c][cur]; }

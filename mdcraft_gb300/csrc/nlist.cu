@@ -231,8 +231,9 @@ __global__ void k_cells(int n, const double* __restrict__ rx, const double* __re
 // ---- list build, a warp per cell with lanes over candidates -------------------
 // The cell's candidates are the atoms of its neighbour cells in the
 // reference's cell order (x outer, z inner), each cell's atoms in slot order.
-// Lanes take 32 consecutive candidates; the warp then walks the cell's atoms
-// and appends, for each, the accepted lanes in lane order (ballot + popc).
+// Lanes take 32 consecutive candidates; the warp walks the cell's atoms, one
+// ballot per atom, so lane i ends with atom i's row of the chunk's accept
+// matrix and appends those candidates in lane order.
 // Entry order per atom is therefore the order of the per-atom loop in
 // nbuild_bin, and the lists are the same, entry for entry. Used when no
 // periodic axis has 3 cells or fewer (no minimum-image adjustment of the
@@ -245,6 +246,7 @@ struct NbWarpSmem {
     float4 oi[32];           // the batch's offsets
     double xi[32], yi[32], zi[32], rni[32];
     uint32_t origi[32];
+    uint32_t cand[32];       // the chunk's list entries (slot | image code)
 };
 
 constexpr int kNbWarps = 4;
@@ -331,41 +333,57 @@ __device__ __forceinline__ void nbuild_cell_warp(const NbArgs& A, const GridPara
         for (uint32_t tb = 0; tb < T; tb += 32) {
             const uint32_t t = tb + lane;
             const bool have = t < T;
-            uint32_t j = 0, jcode = 0;
-            float4 oj = make_float4(0.f, 0.f, 0.f, 0.f), shj = oj;
-            uint32_t origj = 0;
+            uint32_t j = 0xffffffffu, origj = 0;
+            float px = 0.f, py = 0.f, pz = 0.f;
+            bool pfj = false;
             if (have) {
                 while (S.cpre[c + 1] <= t) ++c;
                 j = S.cj0[c] + (t - S.cpre[c]);
-                oj = A.o0[j];
-                shj = S.csh[c];
-                jcode = S.ccode[c];
+                const float4 oj = A.o0[j];
+                const float4 shj = S.csh[c];
+                // the candidate seen from the cell: offset + image shift
+                px = oj.x + shj.x;
+                py = oj.y + shj.y;
+                pz = oj.z + shj.z;
+                pfj = uniform_rns && oj.w == 0.0f;
                 if (A.half) origj = A.orig[j];
+                S.cand[lane] = j | S.ccode[c];
             }
+            __syncwarp();
+            // row ii of the chunk's accept matrix lands in lane ii; pairs
+            // within 1e-5 of rns (or of atoms whose offsets are not exact)
+            // are marked in a second row and settled in FP64 below
+            unsigned mine = 0, mine_x = 0;
+#pragma unroll 2
             for (uint32_t ii = 0; ii < ni; ++ii) {
                 const float4 oi = S.oi[ii];
-                const uint32_t i = base + ii;
-                bool acc = false;
-                if (have && j != i && !(A.half && origj < S.origi[ii])) {
-                    const float dx = oi.x - oj.x - shj.x;
-                    const float dy = oi.y - oj.y - shj.y;
-                    const float dz = oi.z - oj.z - shj.z;
-                    const float d2 = dx * dx + dy * dy + dz * dz;
-                    const bool pf = uniform_rns && oi.w == 0.0f && oj.w == 0.0f;
-                    if (pf && d2 < lo2) acc = true;
-                    else if (pf && d2 > hi2) acc = false;
-                    else
-                        acc = are_neibs_exact(g, S.xi[ii], S.yi[ii], S.zi[ii], S.rni[ii], A.rx[j], A.ry[j], A.rz[j],
-                                              A.rns[j], edge);
+                const float dx = oi.x - px, dy = oi.y - py, dz = oi.z - pz;
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                const bool pf = pfj && oi.w == 0.0f;
+                const bool ok = have && j != base + ii && !(A.half && origj < S.origi[ii]);
+                const unsigned m = __ballot_sync(full, ok && pf && d2 < lo2);
+                const unsigned mx = __ballot_sync(full, ok && !(pf && (d2 < lo2 || d2 > hi2)));
+                if ((uint32_t)lane == ii) {
+                    mine = m;
+                    mine_x = mx;
                 }
-                const unsigned m = __ballot_sync(full, acc);
-                const int ci = __shfl_sync(full, cnt, ii);
-                if (acc) {
-                    const int k = ci + __popc(m & lt);
-                    if (k < A.K) A.nbr[nidx(k, i, A.np)] = j | jcode;
-                }
-                if ((uint32_t)lane == ii) cnt += __popc(m);
             }
+            while (mine_x) {
+                const int b = __ffs(mine_x) - 1;
+                mine_x &= mine_x - 1u;
+                const uint32_t jb = S.cand[b] & kJMask;
+                if (are_neibs_exact(g, S.xi[lane], S.yi[lane], S.zi[lane], S.rni[lane], A.rx[jb], A.ry[jb], A.rz[jb],
+                                    A.rns[jb], edge))
+                    mine |= 1u << b;
+            }
+            // append this atom's accepted candidates in candidate order
+            while (mine) {
+                const int b = __ffs(mine) - 1;
+                mine &= mine - 1u;
+                if (cnt < A.K) A.nbr[nidx(cnt, me, A.np)] = S.cand[b];
+                ++cnt;
+            }
+            __syncwarp();
         }
         if (act) {
             const int padded = (cnt + 3) & ~3;

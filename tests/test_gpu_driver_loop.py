@@ -61,6 +61,51 @@ def test_run_host_equals_run_and_download(make, prec, pinned):
     del keep
 
 
+@pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "pinned"])
+@pytest.mark.parametrize("make,prec", CASES, ids=["eam_mixed", "lj_fp64", "lj_mixed"])
+def test_one_step_host_calls_equal_run(make, prec, pinned):
+    """A host loop of one-step mdg_run_host calls (pinned buffers: result
+    downloads overlapped with the step; pageable: the graph path) gives the
+    bits of mdg_run over the same steps, rebuilds included."""
+    atoms, p, a = _pair(make, prec)
+    a["stepper"].run(a["sys"], p["dt"], 60)
+    ref = a["sys"].download()
+    _, _, b = _pair(make, prec)
+    keep = []
+    if pinned:
+        (pos, t1), (vel, t2), (frc, t3) = (_host(atoms["r"], True), _host(atoms["v"], True),
+                                            _host(np.zeros_like(atoms["r"]), True))
+        keep = [t1, t2, t3]
+    else:
+        pos, vel, frc = _host(atoms["r"], False), _host(atoms["v"], False), np.zeros((len(atoms), 3))
+    for step in range(60):
+        b["stepper"].run_host(b["sys"], p["dt"], 1, pos, vel, frc if step % 2 == 0 else None)
+    assert np.array_equal(pos, ref["r"])
+    assert np.array_equal(vel, ref["v"])
+    assert np.array_equal(b["sys"].forces(), ref["f"])
+    assert a["nl"].rebuilds() == b["nl"].rebuilds()
+    del keep
+
+
+def test_one_step_host_calls_through_rebuilds():
+    """Hot atoms: the one-step overlapped path rebuilds often (positions are
+    sent again after each rebuild's wrap) and still matches mdg_run."""
+    make = lambda: W.eam_cu_fcc(ncell=8, T=3000.0)
+    atoms, p, a = _pair(make, "mixed")
+    a["stepper"].run(a["sys"], p["dt"], 40)
+    ref = a["sys"].download()
+    _, _, b = _pair(make, "mixed")
+    (pos, t1), (vel, t2), (frc, t3) = (_host(atoms["r"], True), _host(atoms["v"], True),
+                                        _host(np.zeros_like(atoms["r"]), True))
+    for _ in range(40):
+        b["stepper"].run_host(b["sys"], p["dt"], 1, pos, vel, frc)
+    assert b["nl"].rebuilds() == a["nl"].rebuilds() >= 3
+    assert np.array_equal(pos, ref["r"])
+    assert np.array_equal(vel, ref["v"])
+    assert np.array_equal(frc, ref["f"])
+    del t1, t2, t3
+
+
 @pytest.mark.parametrize("make", [lambda: W.eam_cu_fcc(ncell=8), lambda: W.lj_argon_fcc(jitter=0.01)],
                          ids=["eam", "lj"])
 def test_graph_prologue_rebuilds_after_upload(make):
