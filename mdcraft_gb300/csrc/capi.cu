@@ -33,7 +33,7 @@ int cuda_status(cudaError_t e, const char* what) {
 }
 
 int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int precision, int stage,
-                 const ThermoDev* th);
+                 const ThermoDev* th, double kick_dt = 0.0);
 int launch_virials(mdg_system* sys, const PotSet* dps, const PotSet& ps);
 int launch_drift(mdg_system* sys, double dt, int precision, double pot_rcut, int periodic_boundary, int drift,
                  int check);
@@ -1467,6 +1467,32 @@ int mdg_solver_set_precision(mdg_solver* s, int precision) {
     return MDG_OK;
 }
 
+// The step's second half-kick rides in the force pass for the mixed form
+// without a thermostat (the thermostat adds its forces after that pass):
+// returns the dt to hand to the last stage, 0 when a kick pass follows.
+static double fused_kick(mdg_solver* s, int prec, double dt) {
+    return prec == MDG_PREC_MIXED && !s->thermo ? dt : 0.0;
+}
+
+// The step's stages, the last one carrying the fused kick where it applies,
+// then the kick pass where it does not.
+static int step_stages(mdg_solver* s, mdg_system* sys, const PotSet& ps, int prec, double dt) {
+    const double fk = fused_kick(s, prec, dt);
+    for (int q = 0; q < s->nstages; ++q) {
+        cudaEvent_t t0 = timer_begin(sys->ctx);
+        int rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q], thermo_of(s),
+                              q == s->nstages - 1 ? fk : 0.0);
+        timer_end(sys->ctx, s->stages[q] == 0 ? MDG_TIME_DENSITY : MDG_TIME_FORCES, t0);
+        if (rc) return rc;
+    }
+    sys->force_prec = prec;
+    if (fk > 0.0) return MDG_OK;
+    cudaEvent_t t0 = timer_begin(sys->ctx);
+    int rc = launch_kick(sys, dt, prec);
+    timer_end(sys->ctx, MDG_TIME_KICK, t0);
+    return rc;
+}
+
 static int check_ready(mdg_solver* s, mdg_system* sys, PotSet* ps) {
     if (!s || !sys) return MDG_ERR_INVALID;
     if (s->nstages == 0) {
@@ -1582,12 +1608,7 @@ static int step_impl(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt
     }
     rc = launch_drift(sys, dt, prec, pot_rcut_of(s), s->periodic, 1, 1);
     if (rc) return rc;
-    for (int k = 0; k < s->nstages; ++k) {
-        rc = launch_stage(sys, e->d.dev, ps, prec, s->stages[k], thermo_of(s));
-        if (rc) return rc;
-    }
-    sys->force_prec = prec;
-    return launch_kick(sys, dt, prec);
+    return step_stages(s, sys, ps, prec, dt);
 }
 
 int mdg_verlet_make_step(mdg_solver* s, mdg_system* sys, double dt) {
@@ -1748,9 +1769,7 @@ static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, dou
     l0 = ctx->launches;
     MDG_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     int rc = launch_drift(sys, dt, prec, s->multi ? -1.0 : s->pot[0][0]->rcut, s->periodic, 1, 1);
-    for (int q = 0; rc == 0 && q < s->nstages; ++q)
-        rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q], thermo_of(s));
-    if (rc == 0) rc = launch_kick(sys, dt, prec);
+    if (rc == 0) rc = step_stages(s, sys, ps, prec, dt);
     if (rc == 0) {
         k_rebuild_cond<<<1, 32, 0, st>>>(hrb, sys->dstat);
         ctx->launches++;
@@ -2067,8 +2086,10 @@ static int run_host_step(mdg_solver* s, mdg_system* sys, const PotSet& ps, doubl
     MDG_LAUNCHED(ctx);
     MDG_CUDA(cudaMemcpyAsync(pos, xp, vb, cudaMemcpyDeviceToHost, io));
     MDG_CUDA(cudaEventRecord(ev_pos_sent, io));
+    const double fk = fused_kick(s, prec, dt);
     for (int q = 0; q < s->nstages; ++q) {
-        rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q], thermo_of(s));
+        rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q], thermo_of(s),
+                          q == s->nstages - 1 ? fk : 0.0);
         if (rc) return rc;
     }
     sys->force_prec = prec;
@@ -2085,8 +2106,10 @@ static int run_host_step(mdg_solver* s, mdg_system* sys, const PotSet& ps, doubl
     MDG_CUDA(cudaEventRecord(ev_reads, io));
     if (force) MDG_CUDA(cudaMemcpyAsync(force, xf, vb, cudaMemcpyDeviceToHost, io));
     MDG_CUDA(cudaEventRecord(ev_io_done, io));
-    rc = launch_kick(sys, dt, prec);
-    if (rc) return rc;
+    if (fk == 0.0) {
+        rc = launch_kick(sys, dt, prec);
+        if (rc) return rc;
+    }
     k_vec_out<<<nb, kBlock, 0, st>>>((int)n, sys->slot_of, sys->f64[VX][c], sys->f64[VY][c], sys->f64[VZ][c], xv);
     MDG_LAUNCHED(ctx);
     MDG_CUDA(cudaMemcpyAsync(vel, xv, vb, cudaMemcpyDeviceToHost, st));
@@ -2179,18 +2202,7 @@ int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
             rc = cuda_status(ce, "flag copy");
             goto done;
         }
-        for (int q = 0; q < s->nstages; ++q) {
-            cudaEvent_t t0 = timer_begin(sys->ctx);
-            rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q], thermo_of(s));
-            timer_end(sys->ctx, s->stages[q] == 0 ? MDG_TIME_DENSITY : MDG_TIME_FORCES, t0);
-            if (rc) goto done;
-        }
-        sys->force_prec = prec;
-        {
-            cudaEvent_t t0 = timer_begin(sys->ctx);
-            rc = launch_kick(sys, dt, prec);
-            timer_end(sys->ctx, MDG_TIME_KICK, t0);
-        }
+        rc = step_stages(s, sys, ps, prec, dt);
         if (rc) goto done;
         // overlap: wait for the flag while the force kernels run
         ce = cudaEventSynchronize(ev);

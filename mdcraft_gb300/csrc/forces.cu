@@ -330,10 +330,10 @@ __global__ void __launch_bounds__(kBlock) k_virials64(FArgs A, const PotSet* __r
 // density kernel at 5; more registers lose occupancy, fewer spill).
 constexpr int kForceMinBlocks = 4;
 constexpr int kDensityMinBlocks = 5;
-template <bool MULTI>
+template <bool MULTI, bool KICK>
 __global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_lj_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < A.n) lj_mixed_one<MULTI>(A, ps, i);
+    if (i < A.n) lj_mixed_one<MULTI, KICK>(A, ps, i);
 }
 
 template <bool MULTI>
@@ -342,17 +342,17 @@ __global__ void __launch_bounds__(kBlock, kDensityMinBlocks) k_density_mixed(FAr
     if (i < A.n) density_mixed_one<MULTI>(A, ps, i);
 }
 
-template <bool MULTI>
+template <bool MULTI, bool KICK>
 __global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_eam_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < A.n) eam_mixed_one<MULTI>(A, ps, i);
+    if (i < A.n) eam_mixed_one<MULTI, KICK>(A, ps, i);
 }
 
 
-template <bool MULTI, int FORM>
+template <bool MULTI, int FORM, bool KICK>
 __global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_pair_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < A.n) pair_mixed_one<MULTI, FORM>(A, ps, i);
+    if (i < A.n) pair_mixed_one<MULTI, FORM, KICK>(A, ps, i);
 }
 
 // ---- Langevin thermostat (langevin.cxx:29-42) ----------------------------------
@@ -476,6 +476,11 @@ FArgs force_args(mdg_system* sys) {
     A.Em = sys->f64[EM][c];
     for (int k = 0; k < 9; ++k) A.V[k] = sys->f64[V0 + k][c];
     A.st = sys->dstat;
+    A.m = sys->f64[MASS][c];
+    A.vx = sys->f64[VX][c];
+    A.vy = sys->f64[VY][c];
+    A.vz = sys->f64[VZ][c];
+    A.kick_hdt = 0.0f;
     return A;
 }
 
@@ -509,9 +514,30 @@ static int launch_thermostat(mdg_system* sys, const ThermoDev* th, int precision
     return MDG_OK;
 }
 
-// stage: 0 = charge (density), 1 = forces (then the thermostat, if any)
+template <bool KICK>
+static void launch_forces_mixed(const FArgs& A, const PotSet* dps, const PotSet& ps, int nb, cudaStream_t st) {
+    const bool multi = ps.multi != 0;
+    if (ps.any_eam) {
+        if (multi) k_eam_mixed<true, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+        else k_eam_mixed<false, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+    } else if (ps.any_tab || ps.any_ljs) {
+        const int kinds = ps.any_lj + ps.any_tab + ps.any_ljs;
+        if (!multi && ps.any_tab) k_pair_mixed<false, 3, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+        else if (!multi) k_pair_mixed<false, 4, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+        else if (kinds > 1) k_pair_mixed<true, 0, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+        else if (ps.any_tab) k_pair_mixed<true, 3, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+        else k_pair_mixed<true, 4, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+    } else {
+        if (multi) k_lj_mixed<true, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+        else k_lj_mixed<false, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+    }
+}
+
+// stage: 0 = charge (density), 1 = forces (then the thermostat, if any).
+// kick_dt > 0 (mixed form, force stage, no thermostat): the step's second
+// half-kick is applied in the force pass.
 int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int precision, int stage,
-                 const ThermoDev* th) {
+                 const ThermoDev* th, double kick_dt) {
     mdg_ctx* ctx = sys->ctx;
     cudaStream_t st = ctx->stream;
     FArgs A = force_args(sys);
@@ -537,19 +563,11 @@ int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int preci
         if (stage == 0) {
             if (multi) k_density_mixed<true><<<nb, kBlock, 0, st>>>(A, dps);
             else k_density_mixed<false><<<nb, kBlock, 0, st>>>(A, dps);
-        } else if (ps.any_eam) {
-            if (multi) k_eam_mixed<true><<<nb, kBlock, 0, st>>>(A, dps);
-            else k_eam_mixed<false><<<nb, kBlock, 0, st>>>(A, dps);
-        } else if (ps.any_tab || ps.any_ljs) {
-            const int kinds = ps.any_lj + ps.any_tab + ps.any_ljs;
-            if (!multi && ps.any_tab) k_pair_mixed<false, 3><<<nb, kBlock, 0, st>>>(A, dps);
-            else if (!multi) k_pair_mixed<false, 4><<<nb, kBlock, 0, st>>>(A, dps);
-            else if (kinds > 1) k_pair_mixed<true, 0><<<nb, kBlock, 0, st>>>(A, dps);
-            else if (ps.any_tab) k_pair_mixed<true, 3><<<nb, kBlock, 0, st>>>(A, dps);
-            else k_pair_mixed<true, 4><<<nb, kBlock, 0, st>>>(A, dps);
+        } else if (kick_dt > 0.0 && !th) {
+            A.kick_hdt = 0.5f * (float)kick_dt;
+            launch_forces_mixed<true>(A, dps, ps, nb, st);
         } else {
-            if (multi) k_lj_mixed<true><<<nb, kBlock, 0, st>>>(A, dps);
-            else k_lj_mixed<false><<<nb, kBlock, 0, st>>>(A, dps);
+            launch_forces_mixed<false>(A, dps, ps, nb, st);
         }
     }
     MDG_LAUNCHED(ctx);

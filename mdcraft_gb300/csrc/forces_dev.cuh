@@ -33,7 +33,26 @@ struct FArgs {
     double *Ep, *Em;
     double* V[9];
     DevStatus* st;
+    // second half-kick fused into the force pass (mixed form): v += g * hdt / m
+    const double* m;
+    double *vx, *vy, *vz;
+    float kick_hdt;  // 0.5f * (float)dt
 };
+
+// Stores the atom's FP32 force and, with KICK, applies the second half-kick
+// exactly as kick_mixed_one does (same FP32 product, same rounding).
+template <bool KICK>
+__device__ __forceinline__ void store_force(const FArgs& A, int i, float fx, float fy, float fz) {
+    A.gx[i] = fx;
+    A.gy[i] = fy;
+    A.gz[i] = fz;
+    if (KICK) {
+        const float hm = A.kick_hdt * __frcp_rn((float)A.m[i]);
+        A.vx[i] += (double)(fx * hm);
+        A.vy[i] += (double)(fy * hm);
+        A.vz[i] += (double)(fz * hm);
+    }
+}
 
 // ---------------------------------------------------------------------------
 // mixed precision
@@ -125,7 +144,7 @@ __device__ __forceinline__ bool pair_in(const FArgs& A, int i, uint32_t e, float
 // the four neighbour records, so the loads of a group overlap; the four
 // contributions are summed in FP32 and the group sum enters a Kahan sum.
 
-template <bool MULTI>
+template <bool MULTI, bool KICK = false>
 __device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
     if (A.tag[i] == 0) return;
     const float4 pi = A.pos32[i];
@@ -169,9 +188,7 @@ __device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __res
         acc.add(1, fy);
         acc.add(2, fz);
     }
-    A.gx[i] = acc.s[0];
-    A.gy[i] = acc.s[1];
-    A.gz[i] = acc.s[2];
+    store_force<KICK>(A, i, acc.s[0], acc.s[1], acc.s[2]);
 }
 
 // Force / r of a tabulated Pair term (pair.cxx:316-346) in FP32 from the
@@ -212,7 +229,7 @@ __device__ __forceinline__ float analytic_ff32(const PotParams& P, float r2) {
 // Pair-type forces (no EAM term) beyond the plain LJsCut kernel: FORM 3 =
 // every pair a tabulated Pair, 4 = every pair LJs, 0 = chosen per kind pair
 // among LJsCut, Pair and LJs.
-template <bool MULTI, int FORM>
+template <bool MULTI, int FORM, bool KICK = false>
 __device__ __forceinline__ void pair_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
     if (A.tag[i] == 0) return;
     const float4 pi = A.pos32[i];
@@ -256,9 +273,7 @@ __device__ __forceinline__ void pair_mixed_one(const FArgs& A, const PotSet* __r
         acc.add(1, fy);
         acc.add(2, fz);
     }
-    A.gx[i] = acc.s[0];
-    A.gy[i] = acc.s[1];
-    A.gz[i] = acc.s[2];
+    store_force<KICK>(A, i, acc.s[0], acc.s[1], acc.s[2]);
 }
 
 __device__ __forceinline__ void embed32(const PotParams& P, float rho, float* F, float* dF,
@@ -335,7 +350,7 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
     A.pos32b[i] = make_float4(pi.x, pi.y, pi.z, Fp0);
 }
 
-template <bool MULTI>
+template <bool MULTI, bool KICK = false>
 __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
     if (A.tag[i] == 0) return;
     const float4 pi = A.pos32b[i];
@@ -404,9 +419,7 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
         acc.add(1, fy);
         acc.add(2, fz);
     }
-    A.gx[i] = acc.s[0];
-    A.gy[i] = acc.s[1];
-    A.gz[i] = acc.s[2];
+    store_force<KICK>(A, i, acc.s[0], acc.s[1], acc.s[2]);
 }
 
 }  // namespace mdg
