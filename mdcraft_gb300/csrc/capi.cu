@@ -2010,8 +2010,23 @@ int run_async_end(mdg_solver* s, mdg_system* sys, double dt, int* relaunched) {
 // (it wraps positions) waits for the reads of the permuted arrays and sends
 // the positions again. Needs page-locked host buffers (the caller's pinned
 // memory); otherwise mdg_run_host takes the graph path.
+static int run_host_step_body(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt, double* pos,
+                              double* vel, double* force);
+
 static int run_host_step(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt, double* pos, double* vel,
                          double* force) {
+    int rc = run_host_step_body(s, sys, ps, dt, pos, vel, force);
+    // no transfer into or out of the caller's buffers may outlive the call,
+    // on any exit
+    cudaError_t e1 = sys->ctx->io_stream ? cudaStreamSynchronize(sys->ctx->io_stream) : cudaSuccess;
+    cudaError_t e2 = cudaStreamSynchronize(sys->ctx->stream);
+    if (rc == MDG_OK && e1 != cudaSuccess) rc = cuda_status(e1, "one-step host run");
+    if (rc == MDG_OK && e2 != cudaSuccess) rc = cuda_status(e2, "one-step host run");
+    return rc;
+}
+
+static int run_host_step_body(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt, double* pos,
+                              double* vel, double* force) {
     mdg_ctx* ctx = sys->ctx;
     cudaStream_t st = ctx->stream;
     const size_t n = sys->n;
@@ -2132,7 +2147,6 @@ static int run_host_step(mdg_solver* s, mdg_system* sys, const PotSet& ps, doubl
         MDG_CUDA(cudaMemcpyAsync(pos, xp, vb, cudaMemcpyDeviceToHost, st));
     }
     MDG_CUDA(cudaStreamWaitEvent(st, ev_io_done, 0));
-    MDG_CUDA(cudaStreamSynchronize(st));
     return MDG_OK;
 }
 
