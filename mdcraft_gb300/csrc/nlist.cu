@@ -228,182 +228,7 @@ __global__ void k_cells(int n, const double* __restrict__ rx, const double* __re
 // Verlet list
 // ---------------------------------------------------------------------------
 
-// ---- list build, a warp per cell with lanes over candidates -------------------
-// The cell's candidates are the atoms of its neighbour cells in the
-// reference's cell order (x outer, z inner), each cell's atoms in slot order.
-// Lanes take 32 consecutive candidates; the warp walks the cell's atoms, one
-// ballot per atom, so lane i ends with atom i's row of the chunk's accept
-// matrix and appends those candidates in lane order.
-// Entry order per atom is therefore the order of the per-atom loop in
-// nbuild_bin, and the lists are the same, entry for entry. Used when no
-// periodic axis has 3 cells or fewer (no minimum-image adjustment of the
-// image code); otherwise nbuild_bin runs.
-struct NbWarpSmem {
-    uint32_t cj0[27];        // first slot of each non-empty neighbour cell
-    uint32_t cpre[28];       // candidate prefix over those cells
-    uint32_t ccode[27];      // image code << kJBits
-    float4 csh[27];          // cell shift (x, y, z) of the image
-    float4 oi[32];           // the batch's offsets
-    double xi[32], yi[32], zi[32], rni[32];
-    uint32_t origi[32];
-    uint32_t cand[32];       // the chunk's list entries (slot | image code)
-};
-
 constexpr int kNbWarps = 4;
-
-__device__ __forceinline__ void nbuild_cell_warp(const NbArgs& A, const GridParams& g, int bin, int lane,
-                                                 bool uniform_rns, NbWarpSmem& S) {
-    const unsigned full = 0xffffffffu;
-    const float lo2 = (float)(g.max_rns * g.max_rns * (1.0 - 1e-5));
-    const float hi2 = (float)(g.max_rns * g.max_rns * (1.0 + 1e-5));
-    const uint32_t s0 = A.bin_start[bin], s1 = A.bin_start[bin + 1];
-    if (s0 == s1) return;
-    int cx, cy, cz;
-    unpack_cell(A.cellp[s0], cx, cy, cz);
-    int gc[3] = {cx + g.offset[0], cy + g.offset[1], cz + g.offset[2]};
-    if (g.dim < 3) gc[2] = 0;
-    if (g.dim < 2) gc[1] = 0;
-    bool edge[3] = {false, false, false};
-    for (int a = 0; a < g.dim; ++a) edge[a] = gc[a] == 0 || gc[a] == g.num[a] - 1;
-
-    // lane t < 27: neighbour cell (t / 9 - 1, t / 3 % 3 - 1, t % 3 - 1)
-    bool valid = false;
-    uint32_t j0 = 0, ncand = 0, code = 0;
-    float4 sh = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (lane < 27) {
-        const int dl[3] = {lane / 9 - 1, (lane / 3) % 3 - 1, lane % 3 - 1};
-        valid = true;
-        for (int a = 0; a < 3; ++a)
-            if (g.periodic[a] && ((g.dom_n[a] == 1 && dl[a] != 0) || (g.dom_n[a] == 2 && dl[a] == 1))) valid = false;
-        if (valid) {
-            int nb[3] = {gc[0] + dl[0], gc[1] + dl[1], gc[2] + dl[2]};
-            for (int a = 0; a < 3; ++a)
-                if (g.periodic[a]) nb[a] = (nb[a] + g.dom_n[a]) % g.dom_n[a];
-            const int lc[3] = {nb[0] - g.offset[0], nb[1] - g.offset[1], nb[2] - g.offset[2]};
-            if (lc[0] < 0 || lc[0] >= g.num[0] || lc[1] < 0 || lc[1] >= g.num[1] || lc[2] < 0 || lc[2] >= g.num[2]) {
-                valid = false;
-            } else {
-                const int bk = bin_key(g, lc[0], lc[1], lc[2]);
-                j0 = A.bin_start[bk];
-                ncand = A.bin_start[bk + 1] - j0;
-                sh = make_float4((float)dl[0] * g.csf[0], (float)dl[1] * g.csf[1], (float)dl[2] * g.csf[2], 0.f);
-                const int own[3] = {cx, cy, cz};
-                for (int a = 0; a < 3; ++a) {
-                    code |= (uint32_t)(dl[a] + 1) << (2 * a);
-                    if (dl[a] != lc[a] - own[a]) code |= 1u << 6;  // the image crossed a periodic face
-                }
-            }
-        }
-    }
-    const bool use = valid && ncand > 0;
-    const unsigned vm = __ballot_sync(full, use);
-    const int slot = __popc(vm & ((1u << lane) - 1u));
-    const int nc = __popc(vm);
-    uint32_t incl = use ? ncand : 0u;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(full, incl, o);
-        if (lane >= o) incl += v;
-    }
-    if (use) {
-        S.cj0[slot] = j0;
-        S.cpre[slot] = incl - ncand;
-        S.ccode[slot] = code << kJBits;
-        S.csh[slot] = sh;
-    }
-    const uint32_t T = __shfl_sync(full, incl, 31);
-    if (lane == 0) S.cpre[nc] = T;
-    __syncwarp();
-
-    const unsigned lt = (1u << lane) - 1u;
-    for (uint32_t base = s0; base < s1; base += 32) {
-        const uint32_t ni = s1 - base < 32u ? s1 - base : 32u;
-        const bool act = (uint32_t)lane < ni;
-        const uint32_t me = base + lane;
-        if (act) {
-            S.oi[lane] = A.o0[me];
-            S.xi[lane] = A.rx[me];
-            S.yi[lane] = A.ry[me];
-            S.zi[lane] = A.rz[me];
-            S.rni[lane] = A.rns[me];
-            S.origi[lane] = A.orig[me];
-        }
-        __syncwarp();
-        int cnt = 0;  // list length of atom `me`
-        int c = 0;    // neighbour cell of this lane's candidate
-        for (uint32_t tb = 0; tb < T; tb += 32) {
-            const uint32_t t = tb + lane;
-            const bool have = t < T;
-            uint32_t j = 0xffffffffu, origj = 0;
-            float px = 0.f, py = 0.f, pz = 0.f;
-            bool pfj = false;
-            if (have) {
-                while (S.cpre[c + 1] <= t) ++c;
-                j = S.cj0[c] + (t - S.cpre[c]);
-                const float4 oj = A.o0[j];
-                const float4 shj = S.csh[c];
-                // the candidate seen from the cell: offset + image shift
-                px = oj.x + shj.x;
-                py = oj.y + shj.y;
-                pz = oj.z + shj.z;
-                pfj = uniform_rns && oj.w == 0.0f;
-                if (A.half) origj = A.orig[j];
-                S.cand[lane] = j | S.ccode[c];
-            }
-            __syncwarp();
-            // row ii of the chunk's accept matrix lands in lane ii; pairs
-            // within 1e-5 of rns (or of atoms whose offsets are not exact)
-            // are marked in a second row and settled in FP64 below
-            unsigned mine = 0, mine_x = 0;
-#pragma unroll 2
-            for (uint32_t ii = 0; ii < ni; ++ii) {
-                const float4 oi = S.oi[ii];
-                const float dx = oi.x - px, dy = oi.y - py, dz = oi.z - pz;
-                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                const bool pf = pfj && oi.w == 0.0f;
-                const bool ok = have && j != base + ii && !(A.half && origj < S.origi[ii]);
-                const unsigned m = __ballot_sync(full, ok && pf && d2 < lo2);
-                const unsigned mx = __ballot_sync(full, ok && !(pf && (d2 < lo2 || d2 > hi2)));
-                if ((uint32_t)lane == ii) {
-                    mine = m;
-                    mine_x = mx;
-                }
-            }
-            while (mine_x) {
-                const int b = __ffs(mine_x) - 1;
-                mine_x &= mine_x - 1u;
-                const uint32_t jb = S.cand[b] & kJMask;
-                if (are_neibs_exact(g, S.xi[lane], S.yi[lane], S.zi[lane], S.rni[lane], A.rx[jb], A.ry[jb], A.rz[jb],
-                                    A.rns[jb], edge))
-                    mine |= 1u << b;
-            }
-            // append this atom's accepted candidates in candidate order
-            while (mine) {
-                const int b = __ffs(mine) - 1;
-                mine &= mine - 1u;
-                if (cnt < A.K) A.nbr[nidx(cnt, me, A.np)] = S.cand[b];
-                ++cnt;
-            }
-            __syncwarp();
-        }
-        if (act) {
-            const int padded = (cnt + 3) & ~3;
-            for (int k = cnt; k < padded && k < A.K; ++k) A.nbr[nidx(k, me, A.np)] = me | kSelfCode;
-            A.ncnt[me] = padded < A.K ? padded : A.K;
-            if (cnt > A.K) {
-                atomicOr(&A.st->flags, FLAG_OVERFLOW);
-                atomicOr(&A.st->build_flags, FLAG_OVERFLOW);
-            }
-            atomicMax(&A.st->max_count, (uint32_t)cnt);
-            A.r0x[me] = S.xi[lane];
-            A.r0y[me] = S.yi[lane];
-            A.r0z[me] = S.zi[lane];
-            A.saved_rcut[me] = A.rcut[me];
-            A.saved_rns[me] = S.rni[lane];
-            A.saved_uid[me] = A.uid[me];
-        }
-        __syncwarp();
-    }
-}
 
 // Block of kNbWarps warps, a warp per bin; bins of grids with a periodic
 // axis of 3 cells or fewer take the per-atom body.

@@ -191,7 +191,14 @@ __device__ bool solo_rebuild(const SoloArgs& S, GridParams& g, double (*red)[NT 
     __syncthreads();
     {
         const bool uniform = S.st->nonuniform == 0;
-        if (n > 16 * g.ncells) {
+        if (!g.small_box) {
+            // a warp per cell, lanes over candidates (the per-stage list
+            // build's body); its per-warp state is the launch's dynamic
+            // shared memory
+            extern __shared__ __align__(16) unsigned char solo_dyn[];
+            NbWarpSmem* nbs = reinterpret_cast<NbWarpSmem*>(solo_dyn);
+            for (int b = w; b < nb; b += NT / 32) nbuild_cell_warp(S.N, g, b, lane, uniform, nbs[w]);
+        } else if (n > 16 * g.ncells) {
             for (int b = w; b < nb; b += NT / 32) nbuild_bin(S.N, g, b, lane, uniform, 32);
         } else {
             for (int b = 2 * w + (lane >> 4); b < nb; b += NT / 16) nbuild_bin(S.N, g, b, lane & 15, uniform, 16);
@@ -491,23 +498,52 @@ int solo_out_read(const void* out_host, uint32_t* done, unsigned long long* left
     return MDG_OK;
 }
 
+// Dynamic shared memory of a launch: the list build's state, one per warp.
+static size_t solo_dyn_bytes(int threads) { return (size_t)(threads / 32) * sizeof(NbWarpSmem); }
+
+template <int NT>
+static cudaError_t solo_prepare_attr() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_solo_persistent<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)solo_dyn_bytes(NT));
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
 int solo_persistent_launch(cudaStream_t stream, int threads, int blocks, const void* desc_dev, SoloQueue* q_dev,
                            uint32_t* head, int idle_limit, int gen) {
     const SoloArgs* d = reinterpret_cast<const SoloArgs*>(desc_dev);
     if (blocks <= 0) return MDG_OK;
     if (blocks > kSoloMaxBlocks || gen < 0 || gen > 1) return MDG_ERR_INVALID;
-    if (threads == 256) k_solo_persistent<256><<<blocks, 256, 0, stream>>>(d, q_dev, head, idle_limit, gen);
-    else if (threads == 1024) k_solo_persistent<1024><<<blocks, 1024, 0, stream>>>(d, q_dev, head, idle_limit, gen);
-    else k_solo_persistent<512><<<blocks, 512, 0, stream>>>(d, q_dev, head, idle_limit, gen);
+    const size_t dyn = solo_dyn_bytes(threads);
+    if (threads == 256) {
+        MDG_CUDA(solo_prepare_attr<256>());
+        k_solo_persistent<256><<<blocks, 256, dyn, stream>>>(d, q_dev, head, idle_limit, gen);
+    } else if (threads == 1024) {
+        MDG_CUDA(solo_prepare_attr<1024>());
+        k_solo_persistent<1024><<<blocks, 1024, dyn, stream>>>(d, q_dev, head, idle_limit, gen);
+    } else {
+        MDG_CUDA(solo_prepare_attr<512>());
+        k_solo_persistent<512><<<blocks, 512, dyn, stream>>>(d, q_dev, head, idle_limit, gen);
+    }
     MDG_CUDA(cudaGetLastError());
     return MDG_OK;
 }
 
 int solo_blocks_per_sm(int threads, int* blocks) {
     cudaError_t e;
-    if (threads == 256) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solo_persistent<256>, 256, 0);
-    else if (threads == 1024) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solo_persistent<1024>, 1024, 0);
-    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solo_persistent<512>, 512, 0);
+    const size_t dyn = solo_dyn_bytes(threads);
+    if (threads == 256) {
+        MDG_CUDA(solo_prepare_attr<256>());
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solo_persistent<256>, 256, dyn);
+    } else if (threads == 1024) {
+        MDG_CUDA(solo_prepare_attr<1024>());
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solo_persistent<1024>, 1024, dyn);
+    } else {
+        MDG_CUDA(solo_prepare_attr<512>());
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solo_persistent<512>, 512, dyn);
+    }
     MDG_CUDA(e);
     return MDG_OK;
 }
