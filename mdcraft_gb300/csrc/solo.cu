@@ -103,7 +103,7 @@ __device__ __forceinline__ void copy_back_block(const GatherAll& G, int n) {
 // Block-uniform result: false when a capacity overflowed (the loop stops and
 // the host grows the capacities).
 template <int NT>
-__device__ bool solo_rebuild(const SoloArgs& S, GridParams& g, double (*red)[NT / 32], uint32_t* scan_sh) {
+__device__ __noinline__ bool solo_rebuild(const SoloArgs& S, GridParams& g, double (*red)[NT / 32], uint32_t* scan_sh) {
     const int t = threadIdx.x, lane = t & 31, w = t >> 5, n = S.n;
     if (t == 0) {
         S.st->max_count = 0;
@@ -214,7 +214,7 @@ __device__ bool solo_rebuild(const SoloArgs& S, GridParams& g, double (*red)[NT 
 
 // The input records (mdg_system_upload_atoms' scatter) from host memory.
 template <int NT>
-__device__ void solo_read_atoms(const SoloArgs& S) {
+__device__ __noinline__ void solo_read_atoms(const SoloArgs& S) {
     const GatherAll& G = S.G;
     for (int k = threadIdx.x; k < S.n; k += NT) {
         const mdg_atom& a = S.atoms_in[k];
@@ -269,7 +269,7 @@ __device__ __forceinline__ void solo_stages(const SoloArgs& S) {
 // (upload, prepare, update(-1), offsets, prepare, stages). False when the
 // first list outgrew the capacities sized on the host.
 template <bool EAM, int NT>
-__device__ bool solo_setup(const SoloArgs& S, GridParams& g, double (*red)[NT / 32], uint32_t* scan_sh) {
+__device__ __noinline__ bool solo_setup(const SoloArgs& S, GridParams& g, double (*red)[NT / 32], uint32_t* scan_sh) {
     const int t = threadIdx.x, n = S.n;
     // the fresh system's buffers (what system_alloc clears on a stream)
     for (int k = t; k < S.np; k += NT) {
@@ -305,7 +305,7 @@ __device__ bool solo_setup(const SoloArgs& S, GridParams& g, double (*red)[NT / 
 // The result records (mdg_system_download_atoms' layout) straight into host
 // memory; mixed forces are widened to FP64 as the download does.
 template <int NT>
-__device__ void solo_write_atoms(const SoloArgs& S) {
+__device__ __noinline__ void solo_write_atoms(const SoloArgs& S) {
     const GatherAll& G = S.G;
     for (int k = threadIdx.x; k < S.n; k += NT) {
         const uint32_t s = S.slot_of[k];
