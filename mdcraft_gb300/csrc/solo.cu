@@ -253,15 +253,17 @@ __device__ __forceinline__ void solo_zero_one(const SoloArgs& S, int i) {
     }
 }
 
-template <bool EAM, int NT>
+// The force stages; with KICK the second half-kick rides in the force body
+// (the step loop), without it the forces alone (the set-up's initial forces).
+template <bool EAM, bool KICK, int NT>
 __device__ __forceinline__ void solo_stages(const SoloArgs& S) {
     const int t = threadIdx.x, n = S.n;
     if (EAM) {
         for (int i = t; i < n; i += NT) density_mixed_one<false>(S.F, S.ps, i);
         __syncthreads();
-        for (int i = t; i < n; i += NT) eam_mixed_one<false>(S.F, S.ps, i);
+        for (int i = t; i < n; i += NT) eam_mixed_one<false, KICK>(S.F, S.ps, i);
     } else {
-        for (int i = t; i < n; i += NT) lj_mixed_one<false>(S.F, S.ps, i);
+        for (int i = t; i < n; i += NT) lj_mixed_one<false, KICK>(S.F, S.ps, i);
     }
 }
 
@@ -297,7 +299,7 @@ __device__ __noinline__ bool solo_setup(const SoloArgs& S, GridParams& g, double
     __syncthreads();
     for (int i = t; i < n; i += NT) drift64_one(S.I, i, 0, 0);
     __syncthreads();
-    solo_stages<EAM, NT>(S);
+    solo_stages<EAM, false, NT>(S);
     __syncthreads();
     return true;
 }
@@ -349,9 +351,7 @@ __device__ void solo_run(SoloArgs& S, GridParams& g, double (*red)[NT / 32], uin
         bool need = false;
         for (int i = t; i < n; i += NT) need |= drift_mixed_one(S.I, i);
         const int any = __syncthreads_or(need);
-        solo_stages<EAM, NT>(S);
-        // each thread kicks the atoms whose forces it just wrote
-        for (int i = t; i < n; i += NT) kick_mixed_one(S.I, i);
+        solo_stages<EAM, true, NT>(S);
         __syncthreads();
         --left;
         if (any) {
@@ -451,6 +451,7 @@ void solo_fill(void* args, mdg_system* sys, const PotSet* dps, int any_eam, doub
     S.any_eam = any_eam;
     S.atoms_in = reinterpret_cast<const mdg_atom*>(atoms_in_dev);
     S.F = force_args(sys);
+    S.F.kick_hdt = 0.5f * (float)dt;  // the step loop's second half-kick, in the force body
     S.N = nb_args(sys);
     S.G = gather_sets(sys);
     S.D = domain_of(sys);
