@@ -16,6 +16,8 @@
 // shared launches. Nothing in the loop waits on another block.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "forces_dev.cuh"
 #include "integrate_dev.cuh"
 #include "mdg_host.h"
@@ -502,13 +504,19 @@ int solo_out_read(const void* out_host, uint32_t* done, unsigned long long* left
 // Dynamic shared memory of a launch: the list build's state, one per warp.
 static size_t solo_dyn_bytes(int threads) { return (size_t)(threads / 32) * sizeof(NbWarpSmem); }
 
+// The launch's dynamic shared memory exceeds the default 48 KB at 1024
+// threads; the attribute is per device, so it is set once per device.
 template <int NT>
 static cudaError_t solo_prepare_attr() {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_solo_persistent<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)solo_dyn_bytes(NT));
-    if (e == cudaSuccess) done = true;
+    static std::atomic<uint64_t> done{0};  // bit d: set on device d (devices 0..63)
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+    if (bit && (done.load() & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(k_solo_persistent<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)solo_dyn_bytes(NT));
+    if (e == cudaSuccess && bit) done.fetch_or(bit);
     return e;
 }
 
