@@ -822,6 +822,8 @@ int download_atoms_enqueue(mdg_system* sys, size_t n) {
     if (rc) return rc;
     rc = sync_forces64(sys);
     if (rc) return rc;
+    rc = settle_outputs(sys);
+    if (rc) return rc;
     k_atoms_out<<<nblk(n), kBlock, 0, st>>>(xfer_args(sys), sys->bc, (mdg_atom*)dbuf);
     MDG_LAUNCHED(sys->ctx);
     MDG_CUDA(cudaMemcpyAsync(sys->pin, dbuf, bytes, cudaMemcpyDeviceToHost, st));
@@ -1467,6 +1469,12 @@ int mdg_solver_set_precision(mdg_solver* s, int precision) {
     return MDG_OK;
 }
 
+// After steps, the outputs each step's prepare clears (Ep and V; Em for EAM
+// and for Multi, multi.cxx:51-63) are stale until read or recomputed.
+static void mark_stepped(mdg_solver* s, mdg_system* sys, const PotSet& ps) {
+    sys->stale_out |= STALE_EP_V | ((ps.any_eam || s->multi) ? STALE_EM : 0);
+}
+
 // The step's second half-kick rides in the force pass for the mixed form
 // without a thermostat (the thermostat adds its forces after that pass):
 // returns the dt to hand to the last stage, 0 when a kick pass follows.
@@ -1527,7 +1535,7 @@ int mdg_solver_prepare(mdg_solver* s, mdg_system* sys) {
     PotSet ps;
     int rc = check_ready(s, sys, &ps);
     if (rc) return rc;
-    rc = launch_zero(sys, ps.any_eam);
+    rc = launch_zero(sys, ps.any_eam || s->multi);
     if (rc) return rc;
     rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
     if (rc) return rc;
@@ -1581,6 +1589,9 @@ int mdg_solver_virials(mdg_solver* s, mdg_system* sys) {
     PotSet ps;
     int rc = check_ready(s, sys, &ps);
     if (rc) return rc;
+    // what the last step's prepare cleared, cleared before the virial pass
+    rc = settle_outputs(sys);
+    if (rc) return rc;
     mdg_solver_ext* e = ext(s);
     if (ps.any_eam && s->precision == MDG_PREC_MIXED) {
         rc = launch_stage(sys, e->d.dev, ps, MDG_PREC_FP64, 0, nullptr);
@@ -1608,6 +1619,7 @@ static int step_impl(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt
     }
     rc = launch_drift(sys, dt, prec, pot_rcut_of(s), s->periodic, 1, 1);
     if (rc) return rc;
+    mark_stepped(s, sys, ps);
     return step_stages(s, sys, ps, prec, dt);
 }
 
@@ -1921,6 +1933,7 @@ int run_async_begin(mdg_solver* s, mdg_system* sys, double dt, long steps) {
     if (rc) return rc;
     sys->run_launched = 0;
     if (steps <= 0) return MDG_OK;
+    mark_stepped(s, sys, ps);
     return run_graph_launch(s, sys, ps, dt, steps);
 }
 
@@ -1966,7 +1979,7 @@ int request_begin(mdg_solver* s, mdg_system* sys, const mdg_atom* atoms, double 
         rc = launch_offsets(sys);
         if (rc) return rc;
     }
-    rc = launch_zero(sys, ps.any_eam);
+    rc = launch_zero(sys, ps.any_eam || s->multi);
     if (rc) return rc;
     rc = launch_drift(sys, 0.0, MDG_PREC_FP64, pot_rcut_of(s), s->periodic, 0, 0);
     if (rc) return rc;
@@ -1976,6 +1989,7 @@ int request_begin(mdg_solver* s, mdg_system* sys, const mdg_atom* atoms, double 
     }
     sys->run_launched = 0;
     if (steps <= 0) return MDG_OK;
+    mark_stepped(s, sys, ps);
     return run_graph_launch(s, sys, ps, dt, steps);
 }
 
@@ -2167,6 +2181,7 @@ int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
     int rc = check_ready(s, sys, &ps);
     if (rc) return rc;
     if (steps <= 0) return MDG_OK;
+    mark_stepped(s, sys, ps);
     if (!sys->ctx->timing && sys->n > 0 && !sys->half) {
         rc = graph_prologue(s, sys);
         if (rc) return rc;
@@ -2252,9 +2267,11 @@ int mdg_run_host(mdg_solver* s, mdg_system* sys, double dt, long steps, double* 
     if (steps == 1 && !sys->ctx->timing && sys->n > 0 && !sys->half && check_ready(s, sys, &ps) == MDG_OK &&
         page_locked(pos) && page_locked(vel) && page_locked(force)) {
         MDG_CUDA(cudaSetDevice(sys->ctx->device));
+        mark_stepped(s, sys, ps);
         return run_host_step(s, sys, ps, dt, pos, vel, force);
     }
     if (steps > 0 && !sys->ctx->timing && sys->n > 0 && !sys->half && check_ready(s, sys, &ps) == MDG_OK) {
+        mark_stepped(s, sys, ps);
         // the whole call in stream order with one wait: uploads, the graph
         // loop, its status read-back, the downloads (the transfer buffer is
         // reused in order, so no transfer waits for another)
@@ -2299,8 +2316,10 @@ int mdg_run_host(mdg_solver* s, mdg_system* sys, double dt, long steps, double* 
 int mdg_system_measure(mdg_system* sys, mdg_state* out) {
     if (!sys || !out) return MDG_ERR_INVALID;
     MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    int rc = settle_outputs(sys);
+    if (rc) return rc;
     double r[11];
-    int rc = launch_measure(sys, r);
+    rc = launch_measure(sys, r);
     if (rc) return rc;
     out->Ep = r[0];
     out->Em = r[1];

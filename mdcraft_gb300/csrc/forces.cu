@@ -563,6 +563,7 @@ int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int preci
         if (stage == 0) {
             if (multi) k_density_mixed<true><<<nb, kBlock, 0, st>>>(A, dps);
             else k_density_mixed<false><<<nb, kBlock, 0, st>>>(A, dps);
+            sys->fp_ok = 0;  // nc rewritten (FP32 sums); Fp64 no longer matches it
         } else if (kick_dt > 0.0 && !th) {
             A.kick_hdt = 0.5f * (float)kick_dt;
             launch_forces_mixed<true>(A, dps, ps, nb, st);

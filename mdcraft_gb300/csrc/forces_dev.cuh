@@ -339,6 +339,8 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
         }
     }
     float rho = s;
+    // the atom's density as the reference's charge stage leaves it (FP32 sum here)
+    if (A.tag[i] != 0) A.nc[i] = (double)rho;
     float Fp0 = 0.f;
     for (int b = 0; b < ps->nkinds; ++b) {
         const PotParams& P = ps->p[ki][b];

@@ -108,13 +108,20 @@ struct ZeroArgs {
     double* V[9];  // nine separate allocations
 };
 
-__global__ void k_zero_outputs(int n, const uint16_t* __restrict__ tag, ZeroArgs Z, int eam) {
+// Pair::prepare's resets for atoms with tag != 0: fields selected by
+// `what` (ZERO_* bits).
+enum : int { ZERO_F = 1, ZERO_EP_V = 2, ZERO_EM = 4, ZERO_NC = 8 };
+
+__global__ void k_zero_outputs(int n, const uint16_t* __restrict__ tag, ZeroArgs Z, int what) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || tag[i] == 0) return;
-    Z.fx[i] = 0.0; Z.fy[i] = 0.0; Z.fz[i] = 0.0;
-    Z.Ep[i] = 0.0;
-    for (int k = 0; k < 9; ++k) Z.V[k][i] = 0.0;
-    if (eam) { Z.Em[i] = 0.0; Z.nc[i] = 0.0; }
+    if (what & ZERO_F) { Z.fx[i] = 0.0; Z.fy[i] = 0.0; Z.fz[i] = 0.0; }
+    if (what & ZERO_EP_V) {
+        Z.Ep[i] = 0.0;
+        for (int k = 0; k < 9; ++k) Z.V[k][i] = 0.0;
+    }
+    if (what & ZERO_EM) Z.Em[i] = 0.0;
+    if (what & ZERO_NC) Z.nc[i] = 0.0;
 }
 
 // ---- FP64 reductions: measure_state (md_test_utils.h:214-239) --------------
@@ -286,9 +293,26 @@ int launch_force_copy(mdg_system* sys, int to64) {
     return MDG_OK;
 }
 
+static int launch_zero_fields(mdg_system* sys, int what);
+
 int launch_zero(mdg_system* sys, int eam) {
     if (sys->n == 0) return MDG_OK;
     if (eam) sys->fp_ok = 0;  // nc cleared
+    // prepare clears the measurement outputs as well
+    sys->stale_out &= eam ? 0 : ~STALE_EP_V;
+    return launch_zero_fields(sys, ZERO_F | ZERO_EP_V | (eam ? ZERO_EM | ZERO_NC : 0));
+}
+
+// The measurement outputs a step's prepare would have cleared, cleared now
+// that something reads them (they are not rewritten every step).
+int settle_outputs(mdg_system* sys) {
+    if (sys->n == 0 || !sys->stale_out) return MDG_OK;
+    const int what = ((sys->stale_out & STALE_EP_V) ? ZERO_EP_V : 0) | ((sys->stale_out & STALE_EM) ? ZERO_EM : 0);
+    sys->stale_out = 0;
+    return launch_zero_fields(sys, what);
+}
+
+static int launch_zero_fields(mdg_system* sys, int what) {
     int c = sys->cur;
     ZeroArgs Z;
     Z.fx = sys->f64[FX][c];
@@ -298,7 +322,7 @@ int launch_zero(mdg_system* sys, int eam) {
     Z.Em = sys->f64[EM][c];
     Z.nc = sys->f64[NC][c];
     for (int k = 0; k < 9; ++k) Z.V[k] = sys->f64[V0 + k][c];
-    k_zero_outputs<<<nblk(sys->n), kBlock, 0, sys->ctx->stream>>>((int)sys->n, sys->u16[TAG][c], Z, eam);
+    k_zero_outputs<<<nblk(sys->n), kBlock, 0, sys->ctx->stream>>>((int)sys->n, sys->u16[TAG][c], Z, what);
     MDG_LAUNCHED(sys->ctx);
     return MDG_OK;
 }

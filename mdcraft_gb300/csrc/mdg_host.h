@@ -61,6 +61,7 @@ struct mdg_ctx {
 };
 
 namespace mdg {
+enum : int { STALE_EP_V = 1, STALE_EM = 2 };
 // Records a start event for `which` when timing is on (else returns null).
 cudaEvent_t timer_begin(mdg_ctx* ctx);
 void timer_end(mdg_ctx* ctx, int which, cudaEvent_t start);
@@ -131,6 +132,10 @@ struct mdg_system {
     float* trig32 = nullptr;      // (skin/2)^2 per atom for the mixed half-skin test
     int force_prec = MDG_PREC_FP64;  // arithmetic of the forces last computed
     int fp_ok = 0;                   // Fp64 = F'(nc) of the current nc (set by the FP64 density pass)
+    // Measurement outputs a step's prepare clears (Pair::prepare_one) and
+    // this build leaves in place during steps: cleared when next read
+    // (STALE_* bits; settle_outputs).
+    int stale_out = 0;
 
     // rebuild scratch
     uint32_t* key = nullptr;
@@ -239,6 +244,7 @@ int download_atoms_enqueue(mdg_system* sys, size_t n);
 // system of that device) and, optionally, their host copy.
 const PotSet* solver_potsets(mdg_solver* s, PotSet* host);
 const ThermoDev* thermo_of(mdg_solver* s);
+int settle_outputs(mdg_system* sys);
 int nlist_capacity_host(mdg_system* sys, const mdg_atom* atoms, size_t n, int half);
 // The fused one-block driver loop (solo.cu): small mixed-precision systems,
 // one request per block of a persistent kernel fed through a queue.
