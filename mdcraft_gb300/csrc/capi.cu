@@ -1486,6 +1486,11 @@ static double fused_kick(mdg_solver* s, int prec, double dt) {
 // then the kick pass where it does not.
 static int step_stages(mdg_solver* s, mdg_system* sys, const PotSet& ps, int prec, double dt) {
     const double fk = fused_kick(s, prec, dt);
+    if (sys->half) {
+        // half lists accumulate both sides of a pair: prepare's clear first
+        int rc = launch_zero(sys, ps.any_eam || s->multi);
+        if (rc) return rc;
+    }
     for (int q = 0; q < s->nstages; ++q) {
         cudaEvent_t t0 = timer_begin(sys->ctx);
         int rc = launch_stage(sys, ext(s)->d.dev, ps, prec, s->stages[q], thermo_of(s),
@@ -1507,8 +1512,8 @@ static int check_ready(mdg_solver* s, mdg_system* sys, PotSet* ps) {
         set_error("solver has no potential");
         return MDG_ERR_STATE;
     }
-    if (sys->have_list && sys->half && sys->n) {
-        set_error("the force stages need a full Verlet list (half lists are export-only)");
+    if (sys->have_list && sys->half && sys->n && s->precision == MDG_PREC_MIXED) {
+        set_error("the mixed form needs a full Verlet list (half lists run in the FP64 form)");
         return MDG_ERR_STATE;
     }
     if (!sys->have_list && sys->n) {
@@ -2087,7 +2092,7 @@ static int run_host_step_body(mdg_solver* s, mdg_system* sys, const PotSet& ps, 
         MDG_CUDA(cudaStreamSynchronize(st));
         if (sys->hstat->need_rebuild) {
             MDG_CUDA(cudaStreamWaitEvent(st, ev_vel_in, 0));  // the rebuild permutes the velocities
-            rc = nlist_build(sys, -1.0, 0);
+            rc = nlist_build(sys, -1.0, sys->half);
             if (rc && rc != MDG_ERR_RANGE) return rc;
             rc = launch_trig(sys);
             if (rc) return rc;
@@ -2146,7 +2151,7 @@ static int run_host_step_body(mdg_solver* s, mdg_system* sys, const PotSet& ps, 
     if (sys->hstat->need_rebuild) {
         // the rebuild permutes what the I/O stream reads
         MDG_CUDA(cudaStreamWaitEvent(st, ev_reads, 0));
-        rc = nlist_build(sys, -1.0, 0);
+        rc = nlist_build(sys, -1.0, sys->half);
         if (rc && rc != MDG_ERR_RANGE) return rc;
         rc = launch_trig(sys);
         if (rc) return rc;
@@ -2200,7 +2205,7 @@ int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
         rc = mdg_nlist_decide(sys, &need);
         if (rc) goto done;
         if (need) {
-            rc = mdg_nlist_update(sys, -1.0, 0);
+            rc = mdg_nlist_update(sys, -1.0, sys->half);
             if (rc && rc != MDG_ERR_RANGE) goto done;
         }
         rc = launch_offsets(sys);
@@ -2241,7 +2246,7 @@ int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
         }
         if (sys->hstat->need_rebuild) {
             cudaEvent_t t0 = timer_begin(sys->ctx);
-            rc = nlist_build(sys, -1.0, 0);
+            rc = nlist_build(sys, -1.0, sys->half);
             timer_end(sys->ctx, MDG_TIME_REBUILD, t0);
             if (rc && rc != MDG_ERR_RANGE) goto done;
             rc = launch_trig(sys);

@@ -193,13 +193,18 @@ __global__ void __launch_bounds__(kBlock) k_embed64(FArgs A, const PotSet* __res
 }
 
 // ---- LJsCut / EAM forces, FP64 ------------------------------------------------
-template <bool MULTI>
+// HALF (half lists, verlet-list.cxx:345): the pair-type potentials push the
+// pair force onto the neighbour as well (LJs-cut.cxx:57-62, pair.cxx:387-420,
+// LJs.cxx:196-222); EAM uses the atom's half alone, as EAM::force does; the
+// ghost pass acts on the atom alone (its ghost list is a full one,
+// periodic.cxx:77-88). Both sides accumulate with atomics onto the outputs
+// prepare cleared, as the reference's += does.
+template <bool MULTI, bool HALF>
 __global__ void __launch_bounds__(kBlock) k_forces64(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.n || A.tag[i] == 0) return;
     int ki = MULTI ? (A.kind[i] & 3) : 0;
     double fm[3] = {0, 0, 0}, fg[3] = {0, 0, 0};
-    const int nk = ps->nkinds;
     visit64<MULTI>(A, i, [&](int kj, int j, double dx, double dy, double dz, double r2, bool ghost) {
         const PotParams& P = ps->p[ki][kj];
         if (r2 > P.R2cut || r2 < 1e-15) return;
@@ -220,13 +225,23 @@ __global__ void __launch_bounds__(kBlock) k_forces64(FArgs A, const PotSet* __re
         f[0] += dx * pref;
         f[1] += dy * pref;
         f[2] += dz * pref;
+        if (HALF && !ghost && P.type != 2) {
+            atomicAdd(&A.fx[j], -(dx * pref));
+            atomicAdd(&A.fy[j], -(dy * pref));
+            atomicAdd(&A.fz[j], -(dz * pref));
+        }
     });
-    (void)nk;
     double fx = fm[0] + fg[0], fy = fm[1] + fg[1], fz = fm[2] + fg[2];
     if (!isfinite(fx) || !isfinite(fy) || !isfinite(fz)) atomicOr(&A.st->flags, FLAG_NONFINITE);
-    A.fx[i] = fx;
-    A.fy[i] = fy;
-    A.fz[i] = fz;
+    if (HALF) {
+        atomicAdd(&A.fx[i], fx);
+        atomicAdd(&A.fy[i], fy);
+        atomicAdd(&A.fz[i], fz);
+    } else {
+        A.fx[i] = fx;
+        A.fy[i] = fy;
+        A.fz[i] = fz;
+    }
 }
 
 // ---- EAM density + embedding derivative, FP64 ------------------------------
@@ -265,8 +280,9 @@ __global__ void __launch_bounds__(kBlock) k_density64(FArgs A, const PotSet* __r
     }
 }
 
-// ---- energies and virials, FP64 (LJs-cut.cxx:70-131, EAM.cxx:306-415) ------
-template <bool MULTI>
+// ---- energies and virials, FP64 (LJs-cut.cxx:70-131, EAM.cxx:306-415,
+// pair.cxx:228-314, LJs.cxx:103-151); HALF as for the forces above.
+template <bool MULTI, bool HALF>
 __global__ void __launch_bounds__(kBlock) k_virials64(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.n || A.tag[i] == 0) return;
@@ -279,38 +295,46 @@ __global__ void __launch_bounds__(kBlock) k_virials64(FArgs A, const PotSet* __r
         if (P.type == 2) last_kind = kj > last_kind || ghost ? kj : last_kind;
         if (r2 > P.R2cut || r2 < 1e-15) return;
         double d[3] = {dx, dy, dz};
+        double E = 0.0, Mp[9];
         if (P.type == 1) {
             double r2inv = 1.0 / r2;
             double r6inv = r2inv * r2inv * r2inv;
             double pref = -0.5 * P.factor * (P.lj1 * r6inv - P.lj2) * r6inv * r2inv;
             double tmp = P.s6 * r6inv;
-            Ep += 0.5 * 4 * P.a * tmp * (tmp - 1);
+            E = 0.5 * 4 * P.a * tmp * (tmp - 1);
             for (int c = 0; c < 3; ++c)
-                for (int r = 0; r < 3; ++r) M[r + 3 * c] += 0.5 * (pref * d[r]) * d[c];
+                for (int r = 0; r < 3; ++r) Mp[r + 3 * c] = 0.5 * (pref * d[r]) * d[c];
         } else if (P.type == 2) {
             double AdF = A.Fp64[(size_t)ki * A.np + j] + A.Fp64[(size_t)kj * A.np + i];
-            double Vr;
-            double FF = eam_ff64(P, r2, AdF, &Vr);
+            double FF = eam_ff64(P, r2, AdF, &E);
             double h = 0.5 * FF;
             for (int c = 0; c < 3; ++c)
-                for (int r = 0; r < 3; ++r) M[r + 3 * c] += h * d[r] * d[c];
-            Ep += Vr;
+                for (int r = 0; r < 3; ++r) Mp[r + 3 * c] = h * d[r] * d[c];
         } else if (P.type == POT_TAB) {
-            double Vr;
-            double h = 0.5 * tab_ff64(P, r2, &Vr);
+            double h = 0.5 * tab_ff64(P, r2, &E);
             for (int c = 0; c < 3; ++c)
-                for (int r = 0; r < 3; ++r) M[r + 3 * c] += h * d[r] * d[c];
-            Ep += Vr;
+                for (int r = 0; r < 3; ++r) Mp[r + 3 * c] = h * d[r] * d[c];
         } else if (P.type == POT_LJS) {
-            double E;
             double FF = ljs_ff64(P, r2, &E);
             for (int c = 0; c < 3; ++c)
-                for (int r = 0; r < 3; ++r) M[r + 3 * c] += 0.5 * (FF * d[r]) * d[c];
-            Ep += E;
+                for (int r = 0; r < 3; ++r) Mp[r + 3 * c] = 0.5 * (FF * d[r]) * d[c];
+        } else {
+            return;
+        }
+        Ep += E;
+        for (int k = 0; k < 9; ++k) M[k] += Mp[k];
+        if (HALF && !ghost && P.type != 2) {
+            atomicAdd(&A.Ep[j], E);
+            for (int k = 0; k < 9; ++k) atomicAdd(&A.V[k][j], Mp[k]);
         }
     });
-    A.Ep[i] = Ep;
-    for (int k = 0; k < 9; ++k) A.V[k][i] = M[k];
+    if (HALF) {
+        atomicAdd(&A.Ep[i], Ep);
+        for (int k = 0; k < 9; ++k) atomicAdd(&A.V[k][i], M[k]);
+    } else {
+        A.Ep[i] = Ep;
+        for (int k = 0; k < 9; ++k) A.V[k][i] = M[k];
+    }
     if (ps->any_eam) {
         int kb = MULTI ? (last_kind >= 0 ? last_kind : ki) : 0;
         const PotParams& P = ps->p[ki][kb];
@@ -556,8 +580,13 @@ int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int preci
                 MDG_LAUNCHED(ctx);
                 sys->fp_ok = 1;
             }
-            if (multi) k_forces64<true><<<nb, kBlock, 0, st>>>(A, dps);
-            else k_forces64<false><<<nb, kBlock, 0, st>>>(A, dps);
+            if (sys->half) {
+                if (multi) k_forces64<true, true><<<nb, kBlock, 0, st>>>(A, dps);
+                else k_forces64<false, true><<<nb, kBlock, 0, st>>>(A, dps);
+            } else {
+                if (multi) k_forces64<true, false><<<nb, kBlock, 0, st>>>(A, dps);
+                else k_forces64<false, false><<<nb, kBlock, 0, st>>>(A, dps);
+            }
         }
     } else {
         if (stage == 0) {
@@ -581,8 +610,16 @@ int launch_virials(mdg_system* sys, const PotSet* dps, const PotSet& ps) {
     if (sys->n == 0) return MDG_OK;
     FArgs A = force_args(sys);
     int nb = nblk(sys->n);
-    if (ps.multi) k_virials64<true><<<nb, kBlock, 0, ctx->stream>>>(A, dps);
-    else k_virials64<false><<<nb, kBlock, 0, ctx->stream>>>(A, dps);
+    if (sys->half) {
+        // accumulates onto the outputs: cleared first, as prepare leaves them
+        int rc = launch_zero_meas(sys);
+        if (rc) return rc;
+        if (ps.multi) k_virials64<true, true><<<nb, kBlock, 0, ctx->stream>>>(A, dps);
+        else k_virials64<false, true><<<nb, kBlock, 0, ctx->stream>>>(A, dps);
+    } else {
+        if (ps.multi) k_virials64<true, false><<<nb, kBlock, 0, ctx->stream>>>(A, dps);
+        else k_virials64<false, false><<<nb, kBlock, 0, ctx->stream>>>(A, dps);
+    }
     MDG_LAUNCHED(ctx);
     return MDG_OK;
 }

@@ -312,6 +312,11 @@ int settle_outputs(mdg_system* sys) {
     return launch_zero_fields(sys, what);
 }
 
+int launch_zero_meas(mdg_system* sys) {
+    if (sys->n == 0) return MDG_OK;
+    return launch_zero_fields(sys, ZERO_EP_V);
+}
+
 static int launch_zero_fields(mdg_system* sys, int what) {
     int c = sys->cur;
     ZeroArgs Z;

@@ -245,6 +245,8 @@ int download_atoms_enqueue(mdg_system* sys, size_t n);
 const PotSet* solver_potsets(mdg_solver* s, PotSet* host);
 const ThermoDev* thermo_of(mdg_solver* s);
 int settle_outputs(mdg_system* sys);
+// Ep and V of atoms with tag != 0 cleared (before an accumulating pass).
+int launch_zero_meas(mdg_system* sys);
 int nlist_capacity_host(mdg_system* sys, const mdg_atom* atoms, size_t n, int half);
 // The fused one-block driver loop (solo.cu): small mixed-precision systems,
 // one request per block of a persistent kernel fed through a queue.
