@@ -129,7 +129,9 @@ int mdg_system_get_forces(mdg_system* sys, double* xyz);
  * list (verlet-list.cxx:72-92). Half lists (j >= i in caller order,
  * verlet-list.cxx:345) run in the FP64 form: pair-type potentials act on
  * both atoms of a pair, EAM on its half, as the reference does; the mixed
- * form refuses them. The run loops rebuild the list of the kind last built. */
+ * form refuses them. The run loops rebuild the list of the kind last built.
+ * Returns MDG_ERR_RANGE when an atom lies outside the grid (the reference
+ * indexes out of bounds there); the atom is clamped into the nearest cell. */
 int mdg_nlist_update(mdg_system* sys, double kbuf, int half);
 /* VerletList::decide (verlet-list.cxx:110-158): *need = 1 when a rebuild is
  * due (size/uid/rcut/rns changed, or a half-skin displacement). */
