@@ -354,6 +354,11 @@ __global__ void __launch_bounds__(kBlock) k_virials64(FArgs A, const PotSet* __r
 // density kernel at 5; more registers lose occupancy, fewer spill).
 constexpr int kForceMinBlocks = 4;
 constexpr int kDensityMinBlocks = 5;
+// Multi bodies (per-pair kind, parameters and F' columns) spill at 64
+// registers; three blocks per SM (up to 85 registers) measured fastest on
+// NiAl B2 1M atoms: 7.2e8 atom-steps/s against 6.4e8 at four blocks and
+// 6.2e8 at two.
+constexpr int kMultiMinBlocks = 3;
 template <bool MULTI, bool KICK>
 __global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_lj_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -361,13 +366,13 @@ __global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_lj_mixed(FArgs A, c
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(kBlock, kDensityMinBlocks) k_density_mixed(FArgs A, const PotSet* __restrict__ ps) {
+__global__ void __launch_bounds__(kBlock, MULTI ? kMultiMinBlocks : kDensityMinBlocks) k_density_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < A.n) density_mixed_one<MULTI>(A, ps, i);
 }
 
 template <bool MULTI, bool KICK>
-__global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_eam_mixed(FArgs A, const PotSet* __restrict__ ps) {
+__global__ void __launch_bounds__(kBlock, MULTI ? kMultiMinBlocks : kForceMinBlocks) k_eam_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < A.n) eam_mixed_one<MULTI, KICK>(A, ps, i);
 }
