@@ -349,11 +349,12 @@ __global__ void __launch_bounds__(kBlock) k_virials64(FArgs A, const PotSet* __r
 // ---------------------------------------------------------------------------
 // mixed precision (bodies in forces_dev.cuh)
 // ---------------------------------------------------------------------------
-// Blocks of 256 threads per SM the register budget must allow (measured on
-// EAM Cu 1M atoms: the force kernels are fastest at 4 (64 registers), the
-// density kernel at 5; more registers lose occupancy, fewer spill).
+// Blocks of 256 threads per SM the register budget must allow, measured on
+// EAM Cu 1M atoms: the force pass is fastest at 4 (64 registers; 0.227 ms
+// against 0.237 ms at 3), the density pass at 4 (0.165 ms against 0.177 ms
+// at 5, where it spills).
 constexpr int kForceMinBlocks = 4;
-constexpr int kDensityMinBlocks = 5;
+constexpr int kDensityMinBlocks = 4;
 // Multi bodies (per-pair kind, parameters and F' columns) spill at 64
 // registers; three blocks per SM (up to 85 registers) measured fastest on
 // NiAl B2 1M atoms: 7.2e8 atom-steps/s against 6.4e8 at four blocks and
