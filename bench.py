@@ -285,6 +285,14 @@ def run_mdg(args, rank, world, local):
     ctx.synchronize()
     fp64_rate = n * args.fp64_steps / (time.perf_counter() - t0)
 
+    # launch shapes of the mixed step kernels, measured on this system
+    # (project autotuner; cached per GPU and workload)
+    from mdcraft_gb300 import tune
+    smx.prepare(sysg)
+    smx.stages(sysg)
+    shapes, shape_sec = tune.tune_shapes(sysg, nl, mdg.Verlet(smx), p["dt"], signature=f"eam_cu_{n}",
+                                         device=local, eam=True)
+
     # mixed form: warm-up, then K timed steps bracketed by events on the
     # engine's stream
     sysg.upload(atoms)
@@ -384,6 +392,7 @@ def run_mdg(args, rank, world, local):
                                     "forces_and_kick": force_launch_ms, "rebuild": rms_ / max(rn, 1)},
             "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": n * 48, "d2h_bytes_per_step": n * 72},
             "gpu_launches": launches,
+            "shape_tuning": {"chosen": shapes, "seconds": shape_sec},
             "roofline": roof,
             "cpu_baseline": cb,
             "clocks": ck,

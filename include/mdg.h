@@ -204,6 +204,20 @@ int mdg_solver_virials(mdg_solver* s, mdg_system* sys);
 /* All of solver.stages in order (single.cxx:23-35). */
 int mdg_solver_stages(mdg_solver* s, mdg_system* sys);
 
+/* ---- launch shapes ------------------------------------------------------------- */
+/* Launch shapes of a system's kernels, set by the project's autotuner
+ * (mdcraft_gb300/tune.py: each candidate timed on the system itself, the
+ * choice cached per GPU and workload); 0 restores the measured default.
+ * No counterpart in the reference. Values:
+ *   MDG_SHAPE_LIST_CELLS_PER_BLOCK   cells (warps) per block of the list build: 2, 4, 8
+ *   MDG_SHAPE_FORCE_BLOCKS_PER_SM    register budget of the mixed force pass: 3, 4
+ *   MDG_SHAPE_DENSITY_BLOCKS_PER_SM  register budget of the mixed density pass: 3, 4, 5 */
+#define MDG_SHAPE_LIST_CELLS_PER_BLOCK 0
+#define MDG_SHAPE_FORCE_BLOCKS_PER_SM 1
+#define MDG_SHAPE_DENSITY_BLOCKS_PER_SM 2
+int mdg_system_set_shape(mdg_system* sys, int what, int value);
+int mdg_system_get_shape(mdg_system* sys, int what, int* value);
+
 /* ---- thermostats ------------------------------------------------------------ */
 /* thermostat::Langevin(beta, temperature, time_step, heat_x, heat_y, heat_z,
  * Ux, Uy, Uz, xmin, xmax) (mdcraft/solver/thermostat/langevin.h:17-29):

@@ -108,6 +108,7 @@ def lib():
         "mdg_solver_set_thermostat": ([vp, vp], ip),
         "mdg_system_thermo_calls": ([vp, C.POINTER(C.c_uint32)], ip),
         "mdg_system_set_thermo_calls": ([vp, C.c_uint32], ip),
+        "mdg_system_set_shape": ([vp, ip, ip], ip), "mdg_system_get_shape": ([vp, ip, C.POINTER(C.c_int)], ip),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -242,6 +243,18 @@ class System:
 
     def set_velocities(self, xyz):
         self._vec(lib().mdg_system_set_velocities, xyz)
+
+    SHAPES = {"list_cells_per_block": 0, "force_blocks_per_sm": 1, "density_blocks_per_sm": 2}
+
+    def set_shape(self, name: str, value: int):
+        """A launch shape of this system's kernels (0 = the measured default);
+        chosen by mdcraft_gb300.tune.tune_shapes."""
+        _check(lib().mdg_system_set_shape(self.h, self.SHAPES[name], int(value)))
+
+    def get_shape(self, name: str) -> int:
+        v = C.c_int()
+        _check(lib().mdg_system_get_shape(self.h, self.SHAPES[name], C.byref(v)))
+        return v.value
 
     def thermo_calls(self) -> int:
         v = C.c_uint32()

@@ -23,6 +23,7 @@ import time
 import numpy as np
 
 from . import EAM, Context, Domain, LJsCut, Multi, Single, System, Verlet, VerletList
+from . import tune
 from . import workloads as W
 
 
@@ -171,6 +172,11 @@ def nial(device=0, steps=500, ncell=80, cpu_steps=4):
     st64 = Verlet(s64)
     st64.run(sysg, p["dt"], 1)
     sec64 = _timed_run(ctx, sysg, st64, p["dt"], 5)
+    # launch shapes of the mixed kernels, measured on this system (state reset after)
+    smx.prepare(sysg)
+    smx.stages(sysg)
+    shapes, _ = tune.tune_shapes(sysg, nl, Verlet(smx), p["dt"], signature=f"nial_{len(atoms)}", device=device,
+                                 eam=True)
     sysg.upload(atoms)
     nl.update(-1.0)
     smx.prepare(sysg)
@@ -195,7 +201,7 @@ def nial(device=0, steps=500, ncell=80, cpu_steps=4):
            "mixed": {"value": n * steps / sec, "unit": "atom-steps/s", "ms_per_step": 1e3 * sec / steps,
                      "rebuilds": rebuilds},
            "fp64_form": {"value": n * 5 / sec64, "unit": "atom-steps/s", "steps": 5},
-           "force_error_vs_fp64": err, "force_error_vs_fp64_after_run": err_run}
+           "force_error_vs_fp64": err, "force_error_vs_fp64_after_run": err_run, "shapes": shapes}
     out["mixed_speedup"] = out["mixed"]["value"] / out["fp64_form"]["value"]
     if cpu_steps:
         rate, secc, rebuilds, _, threads = _oracle_rate(atoms, box, p, cpu_steps)
@@ -221,6 +227,13 @@ def lj_liquid(device=0, steps=200, dims=(128, 128, 256), cpu_steps=1):
     fmx = sysg.forces()
     err = _force_error(fmx, f64)
     del f64, fmx
+    # launch shapes of the mixed kernels, measured on this system (state reset after)
+    shapes, _ = tune.tune_shapes(sysg, nl, Verlet(smx), p["dt"], signature=f"lj_liquid_{len(atoms)}",
+                                 device=device, eam=False)
+    sysg.upload(atoms)
+    nl.update(-1.0)
+    smx.prepare(sysg)
+    smx.stages(sysg)
     st = Verlet(smx)
     st.run(sysg, p["dt"], 3)
     rb0 = nl.rebuilds()
@@ -230,7 +243,7 @@ def lj_liquid(device=0, steps=200, dims=(128, 128, 256), cpu_steps=1):
                      f"dt*=0.005, mixed", "atoms": n, "steps": steps,
            "mixed": {"value": n * steps / sec, "unit": "atom-steps/s", "ms_per_step": 1e3 * sec / steps,
                      "rebuilds": nl.rebuilds() - rb0},
-           "force_error_vs_fp64": err}
+           "force_error_vs_fp64": err, "shapes": shapes}
     sysg.close()
     if cpu_steps:
         rate, secc, rebuilds, _, threads = _oracle_rate(atoms, box, p, cpu_steps)

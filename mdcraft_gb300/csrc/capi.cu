@@ -1430,6 +1430,25 @@ static int thermo_sync(mdg_solver* s) {
     return MDG_OK;
 }
 
+int mdg_system_set_shape(mdg_system* sys, int what, int value) {
+    if (!sys || what < 0 || what > 2) return MDG_ERR_INVALID;
+    static const int ok[3][4] = {{0, 2, 4, 8}, {0, 3, 4, -1}, {0, 3, 4, 5}};
+    bool valid = false;
+    for (int v : ok[what]) valid = valid || v == value;
+    if (!valid) {
+        set_error("unsupported launch shape value");
+        return MDG_ERR_INVALID;
+    }
+    sys->shape[what] = value;
+    return MDG_OK;
+}
+
+int mdg_system_get_shape(mdg_system* sys, int what, int* value) {
+    if (!sys || !value || what < 0 || what > 2) return MDG_ERR_INVALID;
+    *value = sys->shape[what];
+    return MDG_OK;
+}
+
 int mdg_system_thermo_calls(mdg_system* sys, uint32_t* calls) {
     if (!sys || !calls) return MDG_ERR_INVALID;
     MDG_CUDA(cudaSetDevice(sys->ctx->device));
@@ -1844,8 +1863,9 @@ int run_graph_launch(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt
     cudaStream_t st = ctx->stream;
     uint64_t dtbits;
     memcpy(&dtbits, &dt, sizeof(dtbits));
-    uint64_t key[4] = {(uint64_t)(uintptr_t)s, dtbits, (uint64_t)s->precision + 2 * (uint64_t)ext(s)->version,
-                       sys->cap_version};
+    const uint64_t shapes = (uint64_t)sys->shape[0] | ((uint64_t)sys->shape[1] << 8) | ((uint64_t)sys->shape[2] << 16);
+    uint64_t key[4] = {(uint64_t)(uintptr_t)s, dtbits,
+                       (uint64_t)s->precision + 2 * (uint64_t)ext(s)->version + (shapes << 40), sys->cap_version};
     if (!sys->run_exec || memcmp(key, sys->run_key, sizeof(key)) != 0) {
         auto t0 = std::chrono::steady_clock::now();
         int rc = build_run_graph(s, sys, ps, dt);

@@ -360,22 +360,54 @@ constexpr int kDensityMinBlocks = 4;
 // NiAl B2 1M atoms: 7.2e8 atom-steps/s against 6.4e8 at four blocks and
 // 6.2e8 at two.
 constexpr int kMultiMinBlocks = 3;
-template <bool MULTI, bool KICK>
-__global__ void __launch_bounds__(kBlock, kForceMinBlocks) k_lj_mixed(FArgs A, const PotSet* __restrict__ ps) {
+// MB = blocks of 256 threads per SM the register budget allows: a system's
+// launch shape (mdg_system_set_shape, chosen by the project's autotuner),
+// default as above.
+template <bool MULTI, bool KICK, int MB>
+__global__ void __launch_bounds__(kBlock, MB) k_lj_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < A.n) lj_mixed_one<MULTI, KICK>(A, ps, i);
 }
 
-template <bool MULTI>
-__global__ void __launch_bounds__(kBlock, MULTI ? kMultiMinBlocks : kDensityMinBlocks) k_density_mixed(FArgs A, const PotSet* __restrict__ ps) {
+template <bool MULTI, int MB>
+__global__ void __launch_bounds__(kBlock, MB) k_density_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < A.n) density_mixed_one<MULTI>(A, ps, i);
 }
 
-template <bool MULTI, bool KICK>
-__global__ void __launch_bounds__(kBlock, MULTI ? kMultiMinBlocks : kForceMinBlocks) k_eam_mixed(FArgs A, const PotSet* __restrict__ ps) {
+template <bool MULTI, bool KICK, int MB>
+__global__ void __launch_bounds__(kBlock, MB) k_eam_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < A.n) eam_mixed_one<MULTI, KICK>(A, ps, i);
+}
+
+// The blocks-per-SM budget of a pass: the system's shape if set, else the
+// measured default for its form.
+static int force_blocks(const mdg_system* sys, bool multi) {
+    return sys->shape[MDG_SHAPE_FORCE_BLOCKS_PER_SM] ? sys->shape[MDG_SHAPE_FORCE_BLOCKS_PER_SM]
+                                                     : (multi ? kMultiMinBlocks : kForceMinBlocks);
+}
+static int density_blocks(const mdg_system* sys, bool multi) {
+    return sys->shape[MDG_SHAPE_DENSITY_BLOCKS_PER_SM] ? sys->shape[MDG_SHAPE_DENSITY_BLOCKS_PER_SM]
+                                                       : (multi ? kMultiMinBlocks : kDensityMinBlocks);
+}
+
+template <bool MULTI, bool KICK>
+static void launch_eam_lj(bool eam, int mb, const FArgs& A, const PotSet* dps, int nb, cudaStream_t st) {
+    if (eam) {
+        if (mb == 3) k_eam_mixed<MULTI, KICK, 3><<<nb, kBlock, 0, st>>>(A, dps);
+        else k_eam_mixed<MULTI, KICK, 4><<<nb, kBlock, 0, st>>>(A, dps);
+    } else {
+        if (mb == 3) k_lj_mixed<MULTI, KICK, 3><<<nb, kBlock, 0, st>>>(A, dps);
+        else k_lj_mixed<MULTI, KICK, 4><<<nb, kBlock, 0, st>>>(A, dps);
+    }
+}
+
+template <bool MULTI>
+static void launch_density(int mb, const FArgs& A, const PotSet* dps, int nb, cudaStream_t st) {
+    if (mb == 3) k_density_mixed<MULTI, 3><<<nb, kBlock, 0, st>>>(A, dps);
+    else if (mb == 5) k_density_mixed<MULTI, 5><<<nb, kBlock, 0, st>>>(A, dps);
+    else k_density_mixed<MULTI, 4><<<nb, kBlock, 0, st>>>(A, dps);
 }
 
 
@@ -545,11 +577,13 @@ static int launch_thermostat(mdg_system* sys, const ThermoDev* th, int precision
 }
 
 template <bool KICK>
-static void launch_forces_mixed(const FArgs& A, const PotSet* dps, const PotSet& ps, int nb, cudaStream_t st) {
+static void launch_forces_mixed(const mdg_system* sys, const FArgs& A, const PotSet* dps, const PotSet& ps, int nb,
+                                cudaStream_t st) {
     const bool multi = ps.multi != 0;
+    const int mb = force_blocks(sys, multi);
     if (ps.any_eam) {
-        if (multi) k_eam_mixed<true, KICK><<<nb, kBlock, 0, st>>>(A, dps);
-        else k_eam_mixed<false, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+        if (multi) launch_eam_lj<true, KICK>(true, mb, A, dps, nb, st);
+        else launch_eam_lj<false, KICK>(true, mb, A, dps, nb, st);
     } else if (ps.any_tab || ps.any_ljs) {
         const int kinds = ps.any_lj + ps.any_tab + ps.any_ljs;
         if (!multi && ps.any_tab) k_pair_mixed<false, 3, KICK><<<nb, kBlock, 0, st>>>(A, dps);
@@ -558,8 +592,8 @@ static void launch_forces_mixed(const FArgs& A, const PotSet* dps, const PotSet&
         else if (ps.any_tab) k_pair_mixed<true, 3, KICK><<<nb, kBlock, 0, st>>>(A, dps);
         else k_pair_mixed<true, 4, KICK><<<nb, kBlock, 0, st>>>(A, dps);
     } else {
-        if (multi) k_lj_mixed<true, KICK><<<nb, kBlock, 0, st>>>(A, dps);
-        else k_lj_mixed<false, KICK><<<nb, kBlock, 0, st>>>(A, dps);
+        if (multi) launch_eam_lj<true, KICK>(false, mb, A, dps, nb, st);
+        else launch_eam_lj<false, KICK>(false, mb, A, dps, nb, st);
     }
 }
 
@@ -596,14 +630,14 @@ int launch_stage(mdg_system* sys, const PotSet* dps, const PotSet& ps, int preci
         }
     } else {
         if (stage == 0) {
-            if (multi) k_density_mixed<true><<<nb, kBlock, 0, st>>>(A, dps);
-            else k_density_mixed<false><<<nb, kBlock, 0, st>>>(A, dps);
+            if (multi) launch_density<true>(density_blocks(sys, true), A, dps, nb, st);
+            else launch_density<false>(density_blocks(sys, false), A, dps, nb, st);
             sys->fp_ok = 0;  // nc rewritten (FP32 sums); Fp64 no longer matches it
         } else if (kick_dt > 0.0 && !th) {
             A.kick_hdt = 0.5f * (float)kick_dt;
-            launch_forces_mixed<true>(A, dps, ps, nb, st);
+            launch_forces_mixed<true>(sys, A, dps, ps, nb, st);
         } else {
-            launch_forces_mixed<false>(A, dps, ps, nb, st);
+            launch_forces_mixed<false>(sys, A, dps, ps, nb, st);
         }
     }
     MDG_LAUNCHED(ctx);

@@ -136,6 +136,8 @@ struct mdg_system {
     // this build leaves in place during steps: cleared when next read
     // (STALE_* bits; settle_outputs).
     int stale_out = 0;
+    // launch shapes (MDG_SHAPE_*; 0 = the measured default)
+    int shape[3] = {0, 0, 0};
 
     // rebuild scratch
     uint32_t* key = nullptr;

@@ -228,17 +228,17 @@ __global__ void k_cells(int n, const double* __restrict__ rx, const double* __re
 // Verlet list
 // ---------------------------------------------------------------------------
 
-constexpr int kNbWarps = 4;
-
-// Block of kNbWarps warps, a warp per bin; bins of grids with a periodic
-// axis of 3 cells or fewer take the per-atom body.
-__global__ void __launch_bounds__(kNbWarps * 32, 8) k_nbuild_warp(NbArgs A, const GridParams* __restrict__ gp) {
+// Block of NW warps (cells per block: a system's launch shape, default 4),
+// a warp per bin; bins of grids with a periodic axis of 3 cells or fewer
+// take the per-atom body. 64 registers.
+template <int NW>
+__global__ void __launch_bounds__(NW * 32, 32 / NW) k_nbuild_warp(NbArgs A, const GridParams* __restrict__ gp) {
     __shared__ GridParams g;
-    __shared__ NbWarpSmem S[kNbWarps];
+    __shared__ NbWarpSmem S[NW];
     if (threadIdx.x == 0) g = *gp;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int bin = blockIdx.x * kNbWarps + warp;
+    const int bin = blockIdx.x * NW + warp;
     if (g.empty || bin >= g.nbins) return;
     const bool uniform = A.st->nonuniform == 0;
     if (g.small_box) nbuild_bin(A, g, bin, lane, uniform, 32);
@@ -567,8 +567,11 @@ int nlist_enqueue(mdg_system* sys) {
     NbArgs A = nb_args(sys);
     // a half warp per bin of the capacity (a whole warp where cells hold more
     // than 16 atoms on average); the live bins come from the device grid
-    const unsigned nbw = (unsigned)((sys->bin_cap + kNbWarps - 1) / kNbWarps);
-    k_nbuild_warp<<<nbw, kNbWarps * 32, 0, st>>>(A, sys->dgrid);
+    const int cpb = sys->shape[MDG_SHAPE_LIST_CELLS_PER_BLOCK] ? sys->shape[MDG_SHAPE_LIST_CELLS_PER_BLOCK] : 4;
+    const unsigned nbw = (unsigned)((sys->bin_cap + cpb - 1) / cpb);
+    if (cpb == 2) k_nbuild_warp<2><<<nbw, 2 * 32, 0, st>>>(A, sys->dgrid);
+    else if (cpb == 8) k_nbuild_warp<8><<<nbw, 8 * 32, 0, st>>>(A, sys->dgrid);
+    else k_nbuild_warp<4><<<nbw, 4 * 32, 0, st>>>(A, sys->dgrid);
     MDG_LAUNCHED(ctx);
     return MDG_OK;
 }

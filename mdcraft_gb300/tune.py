@@ -3,14 +3,16 @@
 Serving: the threads of the fused per-request block (256, 512 or 1024; the
 block count follows from occupancy) are timed on a sample of the request
 stream itself, each candidate on the same sample through its own server, and
-the fastest is kept. Results are cached per (GPU, workload signature) in
-`_build/tune.json` beside the library, so a later run on the same GPU and
-workload reuses the choice without measuring.
+the fastest is kept.
 
-The per-stage kernels' shapes (threads per block, register budgets, lanes
-per cell of the list build) were chosen by the same kind of measurement and
-are fixed in the sources; the list build picks its lanes per cell from the
-cell occupancy of each grid at run time.
+A system's step kernels (`tune_shapes`): the cells per block of the list
+build (2, 4 or 8 warps, a cell each) are timed on the system's own
+rebuilds, then the register budgets of the mixed force and density passes
+(blocks of 256 threads per SM) on its own steps, one dimension at a time.
+
+Results are cached per (GPU, workload signature) in `_build/tune.json`
+beside the library, so a later run on the same GPU and workload reuses the
+choice without measuring.
 """
 from __future__ import annotations
 
@@ -93,3 +95,58 @@ def tune_serving(specs, solvers, device=0, candidates=(256, 512, 1024), sample=1
                       "steps": steps}
         _store(table)
     return best, rates
+
+
+SHAPE_CANDIDATES = {"list_cells_per_block": (2, 4, 8), "force_blocks_per_sm": (3, 4),
+                    "density_blocks_per_sm": (3, 4, 5)}
+
+
+def _timed(ctx, fn, reps):
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        fn()
+    ctx.synchronize()
+    return (time.perf_counter() - t0) / reps
+
+
+def tune_shapes(system, nlist, stepper, dt, signature, device=0, eam=True, steps=30, rebuilds=6, use_cache=True):
+    """Launch shapes for one system (a Context's System with its VerletList
+    and Verlet stepper). The system's state advances while it is measured.
+    Returns ({shape: value}, {shape: {value: seconds}}) and leaves the
+    chosen shapes set on the system."""
+    key = f"shapes|{_gpu_name(device)}|{signature}"
+    table = _load() if use_cache else {}
+    if key in table:
+        got = table[key]
+        for name, v in got["best"].items():
+            system.set_shape(name, v)
+        return got["best"], got["seconds"]
+    ctx = system.ctx
+    best, seconds = {}, {}
+    # the list build, on its own rebuilds
+    sec = {}
+    for v in SHAPE_CANDIDATES["list_cells_per_block"]:
+        system.set_shape("list_cells_per_block", v)
+        nlist.update(-1.0)
+        sec[v] = _timed(ctx, lambda: nlist.update(-1.0), rebuilds)
+    best["list_cells_per_block"] = min(sec, key=sec.get)
+    seconds["list_cells_per_block"] = sec
+    system.set_shape("list_cells_per_block", best["list_cells_per_block"])
+    # the force and density passes, on steps (a warm-up run captures the graph)
+    for name in ("force_blocks_per_sm", "density_blocks_per_sm"):
+        if name == "density_blocks_per_sm" and not eam:
+            continue
+        sec = {}
+        for v in SHAPE_CANDIDATES[name]:
+            system.set_shape(name, v)
+            stepper.run(system, dt, 2)
+            sec[v] = _timed(ctx, lambda: stepper.run(system, dt, steps), 1) / steps
+        best[name] = min(sec, key=sec.get)
+        seconds[name] = sec
+        system.set_shape(name, best[name])
+    if use_cache:
+        table = _load()
+        table[key] = {"best": best, "seconds": {k: {str(a): b for a, b in v.items()} for k, v in seconds.items()}}
+        _store(table)
+    return best, seconds
