@@ -143,6 +143,17 @@ int mdg_nlist_total(mdg_system* sys, size_t* total);
  * atom's entries are sorted ascending (the set equals the reference's). */
 int mdg_nlist_export(mdg_system* sys, uint64_t* offsets, uint64_t* idx,
                      size_t cap);
+/* VerletList::sort(atoms) (verlet-list.cxx:237-249): wraps `atoms` into the
+ * period in place (put_atoms_in_cells, verlet-list.cxx:176-199) and writes to
+ * `sorted` (n records, not aliasing `atoms`) the same records ordered by the
+ * index of their owning cell on the grid built from them (Grid::cell_index,
+ * grid.cxx:134-136, x fastest), atoms of a cell in ascending input order (the
+ * reference compares cells only, grid.h:31-33, so its order inside a cell is
+ * unspecified). Runs on the system's device and domain; the system's atoms,
+ * list and grid are not changed (the reference's sort replaces the grid that
+ * later list_for calls use). MDG_ERR_RANGE: an atom lay outside the grid and
+ * was sorted into the nearest cell (the reference's behaviour is undefined). */
+int mdg_nlist_sort(mdg_system* sys, mdg_atom* atoms, size_t n, mdg_atom* sorted);
 /* VerletList::list_for(x) (verlet-list.cxx:251-276). */
 int mdg_nlist_list_for(mdg_system* sys, const double x[3], uint64_t* out,
                        size_t cap, size_t* count);

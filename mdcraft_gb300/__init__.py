@@ -79,6 +79,7 @@ def lib():
         "mdg_nlist_update": ([vp, dp, ip], ip), "mdg_nlist_decide": ([vp, C.POINTER(C.c_int)], ip),
         "mdg_nlist_total": ([vp, C.POINTER(C.c_size_t)], ip), "mdg_nlist_export": ([vp, vp, vp, sz], ip),
         "mdg_nlist_list_for": ([vp, vp, vp, sz, C.POINTER(C.c_size_t)], ip),
+        "mdg_nlist_sort": ([vp, vp, sz, vp], ip),
         "mdg_nlist_grid": ([vp, vp, vp], ip), "mdg_nlist_rebuilds": ([vp, u64p], ip),
         "mdg_pot_ljcut_create": ([dp, dp, dp, pp], ip),
         "mdg_pot_eam_create": ([dp, vp, vp, vp, ip, dp, ip, dp, pp], ip),
@@ -323,6 +324,17 @@ class VerletList:
         cnt = C.c_size_t()
         _check(lib().mdg_nlist_list_for(self.sys.h, _ptr(x), _ptr(out), len(out), C.byref(cnt)))
         return out[: min(cnt.value, len(out))]
+
+    def sort(self, atoms: np.ndarray) -> np.ndarray:
+        """VerletList::sort (mdcraft/neibs/verlet-list.cxx:237-249): wraps
+        `atoms` (a C-contiguous ATOM_DTYPE array) into the period in place and
+        returns a copy ordered by owning cell (x fastest), ascending index
+        inside a cell. Computed on the device; this list is not changed."""
+        if atoms.dtype != ATOM_DTYPE or not atoms.flags["C_CONTIGUOUS"]:
+            raise ValueError("atoms must be a C-contiguous ATOM_DTYPE array")
+        out = np.zeros_like(atoms)
+        _check(lib().mdg_nlist_sort(self.sys.h, _ptr(atoms), len(atoms), _ptr(out)), allow=(-4,))
+        return out
 
     def grid(self) -> dict:
         ints = np.zeros(9, dtype=np.int32)

@@ -1078,6 +1078,47 @@ int mdg_nlist_list_for(mdg_system* sys, const double x[3], uint64_t* out, size_t
     return MDG_OK;
 }
 
+int mdg_nlist_sort(mdg_system* sys, mdg_atom* atoms, size_t n, mdg_atom* sorted) {
+    if (!sys || ((!atoms || !sorted) && n) || (n && atoms == sorted)) return MDG_ERR_INVALID;
+    if (n == 0) return MDG_OK;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    // the atoms go through a scratch system on the same device and domain:
+    // its rebuild wraps them and bins them on the grid built from them
+    mdg_system* tmp = nullptr;
+    int rc = mdg_system_create(sys->ctx, &sys->dom, n, &tmp);
+    if (rc) return rc;
+    std::vector<uint32_t> perm(n);
+    std::vector<double> r(3 * n);
+    uint32_t* dperm = nullptr;
+    rc = mdg_system_upload_atoms(tmp, atoms, n);
+    int range = 0;
+    if (!rc) {
+        rc = nlist_build(tmp, -1.0, 0);
+        if (rc == MDG_ERR_RANGE) {  // clamped into the nearest cell, as update() does
+            range = 1;
+            rc = MDG_OK;
+        }
+    }
+    if (!rc && cudaMalloc(&dperm, n * sizeof(uint32_t)) != cudaSuccess) rc = MDG_ERR_NOMEM;
+    if (!rc) rc = nlist_sort_perm(tmp, dperm);
+    if (!rc && cudaMemcpy(perm.data(), dperm, n * sizeof(uint32_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = MDG_ERR_CUDA;
+    if (!rc) rc = mdg_system_get_positions(tmp, r.data());
+    if (dperm) cudaFree(dperm);
+    mdg_system_destroy(tmp);
+    if (rc) return rc;
+    // the caller's atoms take the wrapped positions (put_atoms_in_cells,
+    // verlet-list.cxx:182-185); the copy is every record as it is, reordered
+    for (size_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) atoms[i].r[a] = r[3 * i + a];
+    for (size_t p = 0; p < n; ++p) sorted[p] = atoms[perm[p]];
+    if (range) {
+        set_error("an atom lies outside the cell grid; it was sorted into the nearest cell");
+        return MDG_ERR_RANGE;
+    }
+    return MDG_OK;
+}
+
 // ---- potentials ----------------------------------------------------------
 int mdg_pot_ljcut_create(double a, double s, double rcut, mdg_potential** out) {
     if (!out || !(rcut > 0.0)) return MDG_ERR_INVALID;

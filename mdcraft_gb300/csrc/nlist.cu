@@ -225,6 +225,41 @@ __global__ void k_cells(int n, const double* __restrict__ rx, const double* __re
 }
 
 // ---------------------------------------------------------------------------
+// VerletList::sort (verlet-list.cxx:237-249): atoms by Grid::cell_index
+// (grid.cxx:134-136), x fastest. After a rebuild each cell's atoms are one
+// run of slots (bricked keys) in ascending caller order, so an atom's place
+// is its cell's start in x-fastest order plus its rank inside its bin.
+// ---------------------------------------------------------------------------
+
+__global__ void k_sort_cell_counts(const GridParams* __restrict__ gp, const uint32_t* __restrict__ bin_start,
+                                   uint32_t* __restrict__ cnt, long long cap) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cap) return;
+    const GridParams& g = *gp;
+    if (g.empty || c >= (long long)g.num[0] * g.num[1] * g.num[2]) {
+        cnt[c] = 0u;
+        return;
+    }
+    const int cx = (int)(c % g.num[0]), cy = (int)((c / g.num[0]) % g.num[1]);
+    const int cz = (int)(c / ((long long)g.num[0] * g.num[1]));
+    const int b = bin_key(g, cx, cy, cz);
+    cnt[c] = bin_start[b + 1] - bin_start[b];
+}
+
+__global__ void k_sort_place(int n, const GridParams* __restrict__ gp, const uint32_t* __restrict__ cellp,
+                             const uint32_t* __restrict__ bin_start, const uint32_t* __restrict__ cell_start,
+                             const uint32_t* __restrict__ orig, uint32_t* __restrict__ perm) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || gp->empty) return;
+    const GridParams& g = *gp;
+    int cx, cy, cz;
+    unpack_cell(cellp[k], cx, cy, cz);
+    const int b = bin_key(g, cx, cy, cz);
+    const int c = cx + g.num[0] * (cy + g.num[1] * cz);
+    perm[cell_start[c] + ((uint32_t)k - bin_start[b])] = orig[k];
+}
+
+// ---------------------------------------------------------------------------
 // Verlet list
 // ---------------------------------------------------------------------------
 
@@ -576,7 +611,48 @@ int nlist_enqueue(mdg_system* sys) {
     return MDG_OK;
 }
 
+static int sort_perm_enqueue(mdg_system* sys, uint32_t* cell_start, uint32_t* perm) {
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    const int n = (int)sys->n;
+    const long long cap = (long long)sys->bin_cap;
+    // the bin counts are free after the rebuild's scan: they take the
+    // per-cell counts in x-fastest order, scanned like the bins
+    k_sort_cell_counts<<<nblk((size_t)cap), kBlock, 0, st>>>(sys->dgrid, sys->bin_start, sys->bin_count, cap);
+    MDG_LAUNCHED(ctx);
+    const int nscan = (int)((cap + kScanT * kScanItems - 1) / (kScanT * kScanItems));
+    k_scan_partial<<<nscan, kScanT, 0, st>>>(sys->bin_count, sys->dgrid, sys->scan_tmp);
+    MDG_LAUNCHED(ctx);
+    k_scan_top<<<1, kScanT, 0, st>>>(sys->scan_tmp, sys->dgrid);
+    MDG_LAUNCHED(ctx);
+    k_scan_final<<<nscan, kScanT, 0, st>>>(sys->bin_count, sys->dgrid, sys->scan_tmp, cell_start);
+    MDG_LAUNCHED(ctx);
+    k_sort_place<<<nblk(n), kBlock, 0, st>>>(n, sys->dgrid, sys->cellp, sys->bin_start, cell_start,
+                                             sys->u32[ORIG][sys->cur], perm);
+    MDG_LAUNCHED(ctx);
+    MDG_CUDA(cudaStreamSynchronize(st));
+    return MDG_OK;
+}
+
+// perm[p] = caller index of the atom at place p of VerletList::sort, from
+// the grid and bins of the rebuild just done on `sys` (waits for it). The
+// bin counts are overwritten; the list and the atoms are not touched.
+int nlist_sort_perm(mdg_system* sys, uint32_t* perm) {
+    if (sys->n == 0) return MDG_OK;
+    if (!sys->have_list || sys->grid.empty) {
+        set_error("no cell grid to sort by");
+        return MDG_ERR_INVALID;
+    }
+    uint32_t* cell_start = nullptr;
+    MDG_CUDA(cudaMalloc(&cell_start, ((size_t)sys->bin_cap + 1) * sizeof(uint32_t)));
+    const int rc = sort_perm_enqueue(sys, cell_start, perm);
+    cudaFree(cell_start);
+    return rc;
+}
+
 int launch_trig(mdg_system* sys);
+
+// VerletList::updateint launch_trig(mdg_system* sys);
 
 // VerletList::update (verlet-list.cxx:41-55) for the API: enqueue, wait,
 // and rebuild again with larger capacities when the grid or a list outgrew

@@ -253,6 +253,18 @@ public:
         return r;
     }
 
+    // VerletList::sort (verlet-list.cxx:237-249): wraps `atoms` into the
+    // period in place and returns them ordered by owning cell (x fastest),
+    // ascending index inside a cell; this list is not changed.
+    Atoms sort(Atoms& atoms) {
+        Atoms sorted(atoms.size());
+        if (atoms.empty()) return sorted;
+        if (!m_sys) upload();  // the device system gives the device and the domain
+        int rc = mdg_nlist_sort(m_sys, data::as_mdg(atoms), atoms.size(), data::as_mdg(sorted));
+        if (rc != MDG_OK && rc != MDG_ERR_RANGE) gpu::check(rc, "VerletList::sort");
+        return sorted;
+    }
+
     // Device system of these atoms (uploading the host copy first).
     mdg_system* sync_up() {
         upload();

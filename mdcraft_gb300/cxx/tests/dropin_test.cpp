@@ -162,6 +162,23 @@ static void test_verlet_lists() {
         CHECK(nlist.decide());
     }
     {
+        // test/cxx/neibs/test_verlet_list.cxx:107-122 (SortOrdersAtomsByOwningCell)
+        Atoms atoms(3);
+        atoms[0].r << 1.60, 0.10, 0.10;
+        atoms[1].r << 0.15, 0.10, 0.10;
+        atoms[2].r << 0.95, 0.10, 0.10;
+        for (auto& a : atoms) {
+            a.rcut = 0.40;
+            a.rns = 0.40;
+            a.m = 1.0;
+        }
+        lattice::Domain domain(0.0, 2.0, 0.0, 1.0, 0.0, 1.0);
+        neibs::VerletList nlist(atoms, atoms, domain, threads);
+        auto sorted = nlist.sort(atoms);
+        CHECK(sorted.size() == 3U);
+        CHECK(sorted[0].r.x() < sorted[1].r.x() && sorted[1].r.x() < sorted[2].r.x());
+    }
+    {
         tools::Threads two(2);
         Atoms atoms(1);
         lattice::Domain domain(0.0, 1.0, 0.0, 1.0, 0.0, 1.0);

@@ -5,7 +5,7 @@ import numpy as np
 
 import mdcraft_gb300 as _mdg
 
-from ._engine import DeviceAtoms
+from ._engine import DeviceAtoms, engine_view
 
 
 class VerletList:
@@ -34,3 +34,15 @@ class VerletList:
 
     def list_for(self, x, y=0.0, z=0.0):
         return np.asarray(self._nl.list_for((x, y, z)))
+
+    def sort(self, elems):
+        """Atoms ordered by owning cell (_neibs.cxx:80-97, verlet-list.cxx:237-249);
+        `elems` are wrapped into the period in place, as the reference does."""
+        from .data import Atoms
+        data = np.ascontiguousarray(elems.data)
+        flat = engine_view(data)
+        out = Atoms(0)
+        out._data = np.empty_like(data)
+        engine_view(out._data)[:] = self._nl.sort(flat)
+        elems._data = data
+        return out

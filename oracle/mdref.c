@@ -582,6 +582,38 @@ size_t md_nlist_list_for(const md_nlist* nl, const md_domain* d,
     return m;
 }
 
+int md_sort_atoms(const md_domain* d, md_atom* atoms, size_t n, md_atom* sorted) {
+    /* VerletList::sort (verlet-list.cxx:237-249): put_atoms_in_cells
+     * (verlet-list.cxx:176-199) wraps the atoms in place and builds the grid
+     * from them; the copy lists them by Grid::cell_index (grid.cxx:134-136).
+     * The reference compares cells only (grid.h:31-33), so its order inside a
+     * cell is unspecified; here it is ascending index (a stable counting
+     * sort). Cells outside the local grid are clamped, as in update(). */
+    if (n == 0) return MDREF_OK;
+    int status = MDREF_OK;
+    for (size_t i = 0; i < n; ++i) md_domain_fit_in_period(d, atoms[i].r);
+    md_grid g;
+    md_grid_build(&g, d, atoms, n);
+    size_t nc = (size_t)md_grid_cells_number(&g);
+    size_t* start = (size_t*)calloc(nc + 1, sizeof(size_t));
+    int* cell = (int*)malloc(n * sizeof(int));
+    for (size_t i = 0; i < n; ++i) {
+        int ijk[3];
+        md_grid_local_index3D(&g, d, atoms[i].r, ijk);
+        for (int a = 0; a < 3; ++a) {
+            if (ijk[a] < 0) { ijk[a] = 0; status = MDREF_ERR_RANGE; }
+            if (ijk[a] >= g.num_cells[a]) { ijk[a] = g.num_cells[a] - 1; status = MDREF_ERR_RANGE; }
+        }
+        cell[i] = md_grid_cell_index(&g, ijk);
+        start[cell[i] + 1]++;
+    }
+    for (size_t c = 0; c < nc; ++c) start[c + 1] += start[c];
+    for (size_t i = 0; i < n; ++i) sorted[start[cell[i]]++] = atoms[i];
+    free(cell);
+    free(start);
+    return status;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Potentials — mdcraft/solver/potential/{LJs-cut,EAM}.cxx                  */
 /* ------------------------------------------------------------------------ */

@@ -102,6 +102,9 @@ size_t md_nlist_list_for(const md_nlist* nl, const md_domain* d,
                          const md_atom* atoms, const double x[3],
                          uint64_t* out, size_t cap);
 void md_nlist_grid(const md_nlist* nl, md_grid* out);
+/* VerletList::sort(atoms): wraps atoms in place; sorted[] lists them by
+ * owning cell (x fastest), ascending index inside a cell. */
+int md_sort_atoms(const md_domain* d, md_atom* atoms, size_t n, md_atom* sorted);
 
 /* Potentials (mdcraft/solver/potential). MD_POT_PAIR is LJsCut and
  * MD_POT_TAB the tabulated Pair; both are potential::type::pair in the

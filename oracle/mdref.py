@@ -88,6 +88,7 @@ def lib():
         L.md_nlist_list_for.argtypes = [vp, vp, vp, vp, vp, sz]
         L.md_nlist_list_for.restype = sz
         L.md_nlist_grid.argtypes = [vp, vp]
+        L.md_sort_atoms.argtypes = [vp, vp, sz, vp]
         L.md_pot_ljcut_create.argtypes = [dp, dp, dp]
         L.md_pot_ljcut_create.restype = vp
         L.md_pot_eam_create.argtypes = [dp, vp, vp, vp, ip, dp, ip, dp]
@@ -248,6 +249,17 @@ class Grid:
 assert Grid._DT.itemsize == 4 * 3 + 4 + 8 * 3 + 4 * 6 + 8 * 6
 
 
+def sort_atoms(domain: "Domain", atoms: np.ndarray) -> np.ndarray:
+    """md_sort_atoms: VerletList::sort of `atoms` (wrapped in place)."""
+    if atoms.dtype != ATOM_DTYPE or not atoms.flags["C_CONTIGUOUS"]:
+        raise ValueError("atoms must be a C-contiguous ATOM_DTYPE array")
+    out = np.zeros_like(atoms)
+    st = lib().md_sort_atoms(domain.ptr, _ptr(atoms), len(atoms), _ptr(out))
+    if st not in (0, -4):
+        raise RuntimeError(f"md_sort_atoms failed ({st})")
+    return out
+
+
 class VerletList:
     """mdcraft::neibs::VerletList (mdcraft/neibs/verlet-list.h:134-470)."""
 
@@ -295,6 +307,12 @@ class VerletList:
         g = Grid(self.domain)
         lib().md_nlist_grid(self.h, _ptr(g.buf))
         return g
+
+    def sort(self, atoms: np.ndarray) -> np.ndarray:
+        """VerletList::sort (verlet-list.cxx:237-249): wraps `atoms` in place
+        and returns a copy ordered by owning cell (x fastest), ascending
+        index inside a cell."""
+        return sort_atoms(self.domain, atoms)
 
 
 class LJsCut:

@@ -103,6 +103,42 @@ def test_verlet_list_for_query_point():
     assert sorted(nl.list_for([0.40, 0.10, 0.10])) == [0, 1]
 
 
+def test_verlet_sort_orders_atoms_by_owning_cell():
+    # test/cxx/neibs/test_verlet_list.cxx:107-122
+    atoms = _mk([(1.60, 0.10, 0.10, 0.40, 0.40), (0.15, 0.10, 0.10, 0.40, 0.40),
+                 (0.95, 0.10, 0.10, 0.40, 0.40)])
+    d = R.Domain(0.0, 2.0, 0.0, 1.0, 0.0, 1.0)
+    nl = R.VerletList(atoms, d, threads=1)
+    out = nl.sort(atoms)
+    assert len(out) == 3
+    assert out["r"][0][0] < out["r"][1][0] < out["r"][2][0]
+
+
+def test_sort_wraps_and_orders_by_cell_index():
+    """put_atoms_in_cells (verlet-list.cxx:176-199) wraps the caller's atoms;
+    the copy is ordered by Grid::cell_index (x fastest), ascending index
+    inside a cell."""
+    rng = np.random.default_rng(8)
+    n = 500
+    rows = [(*rng.uniform(-0.5, 3.5, 3), 0.45, 0.4) for _ in range(n)]
+    atoms = _mk(rows)
+    atoms["uid"] = np.arange(n)
+    d = R.Domain(0.0, 3.0, 0.0, 3.0, 0.0, 3.0)
+    for k in range(3):
+        d.set_periodic(k, True)
+    out = R.sort_atoms(d, atoms)
+    assert np.all((atoms["r"] >= 0.0) & (atoms["r"] < 3.0))
+    g = R.Grid(d)
+    g.build(atoms)
+    cells = np.array([g.cell_index(g.local_index3D(r)) for r in out["r"]])
+    assert np.all(np.diff(cells) >= 0)
+    same = np.diff(cells) == 0
+    assert np.all(np.diff(out["uid"].astype(np.int64))[same] > 0)
+    assert np.array_equal(np.sort(out["uid"]), np.arange(n))
+    assert np.array_equal(out.view(np.uint8).reshape(n, -1),
+                          atoms[out["uid"]].view(np.uint8).reshape(n, -1))
+
+
 def test_verlet_kbuf_uses_actual_neighbours():
     atoms = _mk([(0.10, 0.10, 0.10, 0.35, 0.20), (0.35, 0.10, 0.10, 0.35, 0.60),
                  (1.80, 0.10, 0.10, 0.35, 0.10)])
