@@ -1018,61 +1018,12 @@ int mdg_nlist_rebuilds(mdg_system* sys, uint64_t* count) {
 // VerletList::list_for (verlet-list.cxx:251-276), evaluated on the host from
 // the device's last grid and positions; radius = Grid::cell_size().
 int mdg_nlist_list_for(mdg_system* sys, const double x[3], uint64_t* out, size_t cap, size_t* count) {
-    if (!sys || !x || !count) return MDG_ERR_INVALID;
+    if (!sys || !x || !count || (!out && cap)) return MDG_ERR_INVALID;
     if (!sys->have_list) return MDG_ERR_STATE;
     MDG_CUDA(cudaSetDevice(sys->ctx->device));
-    cudaStream_t st = sys->ctx->stream;
-    const GridParams& g = sys->grid;
-    size_t n = sys->n;
-    std::vector<double> rx(n), ry(n), rz(n), rns(n);
-    std::vector<uint32_t> orig(n), start((size_t)g.nbins + 1);
-    int c = sys->cur;
-    MDG_CUDA(cudaMemcpyAsync(rx.data(), sys->f64[RX][c], n * 8, cudaMemcpyDeviceToHost, st));
-    MDG_CUDA(cudaMemcpyAsync(ry.data(), sys->f64[RY][c], n * 8, cudaMemcpyDeviceToHost, st));
-    MDG_CUDA(cudaMemcpyAsync(rz.data(), sys->f64[RZ][c], n * 8, cudaMemcpyDeviceToHost, st));
-    MDG_CUDA(cudaMemcpyAsync(rns.data(), sys->f64[RNS][c], n * 8, cudaMemcpyDeviceToHost, st));
-    MDG_CUDA(cudaMemcpyAsync(orig.data(), sys->u32[ORIG][c], n * 4, cudaMemcpyDeviceToHost, st));
-    MDG_CUDA(cudaMemcpyAsync(start.data(), sys->bin_start, start.size() * 4, cudaMemcpyDeviceToHost, st));
-    MDG_CUDA(cudaStreamSynchronize(st));
-    int cell[3] = {0, 0, 0};
-    for (int a = 0; a < g.dim; ++a) cell[a] = (int)std::floor((x[a] - g.bmin[a]) / g.cs[a]);
-    bool edge[3] = {false, false, false};
-    for (int a = 0; a < g.dim; ++a) edge[a] = cell[a] == 0 || cell[a] == g.num[a] - 1;
-    double rad = std::max(g.cs[0], std::max(g.cs[1], g.cs[2]));
     std::vector<uint64_t> found;
-    for (int dx = -1; dx <= 1; ++dx) {
-        if (g.periodic[0] && ((g.dom_n[0] == 1 && dx != 0) || (g.dom_n[0] == 2 && dx == 1))) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
-            if (g.periodic[1] && ((g.dom_n[1] == 1 && dy != 0) || (g.dom_n[1] == 2 && dy == 1))) continue;
-            for (int dz = -1; dz <= 1; ++dz) {
-                if (g.periodic[2] && ((g.dom_n[2] == 1 && dz != 0) || (g.dom_n[2] == 2 && dz == 1))) continue;
-                int nb[3] = {cell[0] + dx, cell[1] + dy, cell[2] + dz};
-                for (int a = 0; a < 3; ++a)
-                    if (g.periodic[a]) nb[a] = (nb[a] + g.dom_n[a]) % g.dom_n[a];
-                int lc[3] = {nb[0] - g.offset[0], nb[1] - g.offset[1], nb[2] - g.offset[2]};
-                bool in = true;
-                for (int a = 0; a < 3; ++a) in = in && lc[a] >= 0 && lc[a] < g.num[a];
-                if (!in) continue;
-                int b = bin_key(g, lc[0], lc[1], lc[2]);
-                for (uint32_t j = start[b]; j < start[b + 1]; ++j) {
-                    double dd = rad < rns[j] ? rns[j] : rad;
-                    double d2 = dd * dd;
-                    double d[3] = {x[0] - rx[j], x[1] - ry[j], x[2] - rz[j]};
-                    for (int a = 0; a < 3; ++a) {
-                        double L = g.size[a];
-                        if (edge[a] && g.periodic[a] && (2 * d[a] < -L)) d[a] += L;
-                        if (edge[a] && g.periodic[a] && (2 * d[a] > L)) d[a] -= L;
-                    }
-                    volatile double s0 = d[0] * d[0];
-                    volatile double s1 = d[1] * d[1];
-                    volatile double s2 = d[2] * d[2];
-                    volatile double s01 = s0 + s1;
-                    if (s01 + s2 <= d2) found.push_back(orig[j]);
-                }
-            }
-        }
-    }
-    std::sort(found.begin(), found.end());
+    int rc = nlist_list_for(sys, x, found);
+    if (rc) return rc;
     *count = found.size();
     for (size_t k = 0; k < found.size() && k < cap; ++k) out[k] = found[k];
     return MDG_OK;

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "mdg_host.h"
 #include "nlist_dev.cuh"
@@ -257,6 +258,31 @@ __global__ void k_sort_place(int n, const GridParams* __restrict__ gp, const uin
     const int b = bin_key(g, cx, cy, cz);
     const int c = cx + g.num[0] * (cy + g.num[1] * cz);
     perm[cell_start[c] + ((uint32_t)k - bin_start[b])] = orig[k];
+}
+
+// ---------------------------------------------------------------------------
+// VerletList::list_for (verlet-list.cxx:251-276): the listed atoms of the
+// query's adjacent cells within max(cell size, rns_j), a block per cell
+// ---------------------------------------------------------------------------
+
+struct ListForArgs {
+    double x[3];
+    double rad;
+    bool edge[3];
+    int bins[27];
+};
+
+__global__ void k_list_for(ListForArgs q, const GridParams* __restrict__ gp, const uint32_t* __restrict__ bin_start,
+                           const double* __restrict__ rx, const double* __restrict__ ry,
+                           const double* __restrict__ rz, const double* __restrict__ rns,
+                           const uint32_t* __restrict__ orig, uint32_t* __restrict__ out,
+                           uint32_t* __restrict__ count) {
+    const GridParams& g = *gp;
+    const int b = q.bins[blockIdx.x];
+    for (uint32_t j = bin_start[b] + threadIdx.x; j < bin_start[b + 1]; j += blockDim.x) {
+        if (are_neibs_exact(g, q.x[0], q.x[1], q.x[2], q.rad, rx[j], ry[j], rz[j], rns[j], q.edge))
+            out[atomicAdd(count, 1u)] = orig[j];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -650,7 +676,65 @@ int nlist_sort_perm(mdg_system* sys, uint32_t* perm) {
     return rc;
 }
 
+// The caller indices list_for(x) finds, ascending (the reference's list in
+// cell-walk order, as a set). The adjacent cells follow Grid::adjacent_cells
+// (grid.cxx:138-207) on the grid of the last rebuild.
+int nlist_list_for(mdg_system* sys, const double x[3], std::vector<uint64_t>& found) {
+    found.clear();
+    if (sys->n == 0) return MDG_OK;
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    // the grid of the last rebuild, which may have run inside a device loop
+    GridParams g;
+    MDG_CUDA(cudaMemcpyAsync(&g, sys->dgrid, sizeof(GridParams), cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    if (g.empty) return MDG_OK;
+    ListForArgs q;
+    memset(&q, 0, sizeof(q));
+    int cell[3] = {0, 0, 0};
+    for (int a = 0; a < 3; ++a) q.x[a] = x[a];
+    for (int a = 0; a < g.dim; ++a) cell[a] = (int)std::floor((x[a] - g.bmin[a]) / g.cs[a]);
+    for (int a = 0; a < g.dim; ++a) q.edge[a] = cell[a] == 0 || cell[a] == g.num[a] - 1;
+    q.rad = std::max(g.cs[0], std::max(g.cs[1], g.cs[2]));
+    int nb = 0;
+    for (int dx = -1; dx <= 1; ++dx) {
+        if (g.periodic[0] && ((g.dom_n[0] == 1 && dx != 0) || (g.dom_n[0] == 2 && dx == 1))) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            if (g.periodic[1] && ((g.dom_n[1] == 1 && dy != 0) || (g.dom_n[1] == 2 && dy == 1))) continue;
+            for (int dz = -1; dz <= 1; ++dz) {
+                if (g.periodic[2] && ((g.dom_n[2] == 1 && dz != 0) || (g.dom_n[2] == 2 && dz == 1))) continue;
+                int c[3] = {cell[0] + dx, cell[1] + dy, cell[2] + dz};
+                for (int a = 0; a < 3; ++a)
+                    if (g.periodic[a]) c[a] = (c[a] + g.dom_n[a]) % g.dom_n[a];
+                int lc[3] = {c[0] - g.offset[0], c[1] - g.offset[1], c[2] - g.offset[2]};
+                bool in = true;
+                for (int a = 0; a < 3; ++a) in = in && lc[a] >= 0 && lc[a] < g.num[a];
+                if (in) q.bins[nb++] = bin_key(g, lc[0], lc[1], lc[2]);
+            }
+        }
+    }
+    if (nb == 0) return MDG_OK;
+    const int c = sys->cur;
+    // results land in the spare slot-order buffers (free between rebuilds)
+    uint32_t* out = sys->key;
+    uint32_t* cnt = sys->rank;
+    MDG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(uint32_t), st));
+    k_list_for<<<nb, 128, 0, st>>>(q, sys->dgrid, sys->bin_start, sys->f64[RX][c], sys->f64[RY][c],
+                                   sys->f64[RZ][c], sys->f64[RNS][c], sys->u32[ORIG][c], out, cnt);
+    MDG_LAUNCHED(ctx);
+    uint32_t m = 0;
+    MDG_CUDA(cudaMemcpyAsync(&m, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    std::vector<uint32_t> idx(m);
+    if (m) MDG_CUDA(cudaMemcpy(idx.data(), out, m * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    found.assign(idx.begin(), idx.end());
+    std::sort(found.begin(), found.end());
+    return MDG_OK;
+}
+
 int launch_trig(mdg_system* sys);
+
+// VerletList::updateint launch_trig(mdg_system* sys);
 
 // VerletList::updateint launch_trig(mdg_system* sys);
 

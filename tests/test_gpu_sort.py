@@ -26,6 +26,7 @@ def _random_atoms(n, lo, hi, rns, seed):
     a["m"] = 1.0
     a["uid"] = np.arange(1, n + 1)
     a["kind"] = rng.integers(0, 3, n)
+    a["tag"] = 0xFFFF  # moved by the stepper (tag 0 atoms stay put)
     return a
 
 
@@ -112,3 +113,46 @@ def test_sort_python_dropin():
     nl = VerletList(atoms=atoms, neighbors=atoms, domain=Domain(0.0, 2.0, 0.0, 1.0, 0.0, 1.0))
     out = nl.sort(atoms)
     assert list(out.data["r"]["x"]) == [0.15, 0.95, 1.60]
+
+
+@pytest.mark.parametrize("periodic", [(1, 1, 1), (1, 0, 1)])
+def test_list_for_matches_oracle(periodic):
+    """VerletList::list_for (verlet-list.cxx:251-276) on a random system:
+    query points in every kind of cell (faces, edges, interior), on the first
+    list and again after steps (rebuilds inside the device loop) and a
+    rebuild, against the oracle's list_for on the same atoms."""
+    box = (0.0, 2.6, -1.0, 1.3, 0.5, 2.8)
+    atoms = _random_atoms(1500, (0.0, -1.0, 0.5), (2.6, 1.3, 2.8), 0.33, seed=5 + periodic[1])
+    do, dg = H.domains(box, periodic)
+    sysg = mdg.System(H.ctx(), dg, atoms)
+    nlg = mdg.VerletList(sysg)
+    nlg.update(-1.0)
+    rng = np.random.default_rng(21)
+    lo = np.array([box[0], box[2], box[4]])
+    hi = np.array([box[1], box[3], box[5]])
+    queries = np.concatenate([rng.uniform(lo, hi, (40, 3)), [lo + 0.01], [hi - 0.01],
+                              np.array([[lo[0] + 0.001, 0.0, hi[2] - 0.001], [hi[0] - 0.02, lo[1] + 0.02, 1.6]])])
+
+    def compare():
+        ao = H.to_oracle_atoms(sysg.download())
+        nlo = R.VerletList(ao, do, threads=1)
+        nlo.update(-1.0)  # wrapped already: the same grid as the device's last rebuild
+        for x in queries:
+            assert list(nlg.list_for(x)) == sorted(nlo.list_for(x)), x
+
+    compare()
+    # free flight (a zero-strength LJsCut) along the periodic axes, with
+    # rebuilds inside the device loop, then a rebuild on the final positions
+    v = rng.normal(0.0, 2.0, (len(atoms), 3))
+    for a in range(3):
+        if not periodic[a]:
+            v[:, a] = 0.0
+    sysg.set_velocities(v)
+    pot = mdg.LJsCut(0.0, 0.1, 0.3)
+    solver = mdg.Single(pot, periodic=True)
+    solver.prepare(sysg)
+    solver.stages(sysg)
+    mdg.Verlet(solver).run(sysg, 0.002, 60)
+    assert nlg.rebuilds() >= 3
+    nlg.update(-1.0)
+    compare()
