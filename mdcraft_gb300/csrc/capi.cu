@@ -939,45 +939,14 @@ int mdg_nlist_decide(mdg_system* sys, int* need) {
     return MDG_OK;
 }
 
-// host copies of the list in caller order
-static int host_lists(mdg_system* sys, std::vector<uint64_t>& off, std::vector<uint64_t>& idx) {
-    size_t n = sys->n, np = sys->np;
-    cudaStream_t st = sys->ctx->stream;
-    std::vector<uint32_t> cnt(n), orig(n), slot(n), nbr((size_t)sys->K * np);
-    if (n) {
-        MDG_CUDA(cudaMemcpyAsync(cnt.data(), sys->ncnt, n * 4, cudaMemcpyDeviceToHost, st));
-        MDG_CUDA(cudaMemcpyAsync(orig.data(), sys->u32[ORIG][sys->cur], n * 4, cudaMemcpyDeviceToHost, st));
-        MDG_CUDA(cudaMemcpyAsync(slot.data(), sys->slot_of, n * 4, cudaMemcpyDeviceToHost, st));
-        if (sys->K) MDG_CUDA(cudaMemcpyAsync(nbr.data(), sys->nbr, nbr.size() * 4, cudaMemcpyDeviceToHost, st));
-        MDG_CUDA(cudaStreamSynchronize(st));
-    }
-    // self entry first (the reference lists each atom as its own neighbour),
-    // then the stored entries without the self padding
-    off.assign(n + 1, 0);
-    idx.clear();
-    idx.reserve(n * 64);
-    for (size_t c = 0; c < n; ++c) {
-        uint32_t s = slot[c];
-        size_t b = idx.size();
-        idx.push_back(c);
-        for (uint32_t k = 0; k < cnt[s]; ++k) {
-            uint32_t j = nbr[nidx((int)k, s, np)] & kJMask;
-            if (j != s) idx.push_back(orig[j]);
-        }
-        std::sort(idx.begin() + b, idx.end());
-        off[c + 1] = idx.size();
-    }
-    return MDG_OK;
-}
-
 int mdg_nlist_total(mdg_system* sys, size_t* total) {
     if (!sys || !total) return MDG_ERR_INVALID;
     if (!sys->have_list) return MDG_ERR_STATE;
     MDG_CUDA(cudaSetDevice(sys->ctx->device));
-    std::vector<uint64_t> off, ix;
-    int rc = host_lists(sys, off, ix);
+    std::vector<uint64_t> off;
+    int rc = nlist_export_offsets(sys, off);
     if (rc) return rc;
-    *total = ix.size();
+    *total = (size_t)off[sys->n];
     return MDG_OK;
 }
 
@@ -985,26 +954,33 @@ int mdg_nlist_export(mdg_system* sys, uint64_t* offsets, uint64_t* idx, size_t c
     if (!sys || !offsets) return MDG_ERR_INVALID;
     if (!sys->have_list) return MDG_ERR_STATE;
     MDG_CUDA(cudaSetDevice(sys->ctx->device));
-    std::vector<uint64_t> off, ix;
-    int rc = host_lists(sys, off, ix);
+    std::vector<uint64_t> off;
+    int rc = nlist_export_offsets(sys, off);
     if (rc) return rc;
-    if (ix.size() > cap || (!idx && !ix.empty())) {
+    const size_t total = (size_t)off[sys->n];
+    if (total > cap || (!idx && total)) {
         set_error("export capacity too small");
         return MDG_ERR_INVALID;
     }
+    rc = nlist_export_entries(sys, off, idx);
+    if (rc) return rc;
     memcpy(offsets, off.data(), off.size() * sizeof(uint64_t));
-    if (!ix.empty()) memcpy(idx, ix.data(), ix.size() * sizeof(uint64_t));
     return MDG_OK;
 }
 
 int mdg_nlist_grid(mdg_system* sys, int32_t ints[9], double dbls[3]) {
     if (!sys || !ints || !dbls) return MDG_ERR_INVALID;
     if (!sys->have_list) return MDG_ERR_STATE;
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    // the grid of the last rebuild, which may have run inside a device loop
+    GridParams g;
+    MDG_CUDA(cudaMemcpyAsync(&g, sys->dgrid, sizeof(GridParams), cudaMemcpyDeviceToHost, sys->ctx->stream));
+    MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
     for (int a = 0; a < 3; ++a) {
-        ints[a] = sys->grid.dom_n[a];
-        ints[3 + a] = sys->grid.offset[a];
-        ints[6 + a] = sys->grid.num[a];
-        dbls[a] = sys->grid.cs[a];
+        ints[a] = g.dom_n[a];
+        ints[3 + a] = g.offset[a];
+        ints[6 + a] = g.num[a];
+        dbls[a] = g.cs[a];
     }
     return MDG_OK;
 }

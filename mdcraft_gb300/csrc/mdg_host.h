@@ -279,6 +279,8 @@ int solo_blocks_per_sm(int threads, int* blocks);
 int nlist_build(mdg_system* sys, double kbuf, int half);
 int nlist_sort_perm(mdg_system* sys, uint32_t* perm);
 int nlist_list_for(mdg_system* sys, const double x[3], std::vector<uint64_t>& found);
+int nlist_export_offsets(mdg_system* sys, std::vector<uint64_t>& off);
+int nlist_export_entries(mdg_system* sys, const std::vector<uint64_t>& off, uint64_t* idx);
 int nlist_capacity(mdg_system* sys, int half);
 int nlist_enqueue(mdg_system* sys);
 int potset_build(mdg_solver* s, mdg_system* sys, PotSet* out);

@@ -286,6 +286,44 @@ __global__ void k_list_for(ListForArgs q, const GridParams* __restrict__ gp, con
 }
 
 // ---------------------------------------------------------------------------
+// VerletList::get() as CSR in caller order: per atom the atom itself and its
+// stored entries (self padding dropped) as caller indices, ascending
+// ---------------------------------------------------------------------------
+
+__global__ void k_export_counts(int n, const uint32_t* __restrict__ slot_of, const uint32_t* __restrict__ ncnt,
+                                const uint32_t* __restrict__ nbr, size_t np, uint32_t* __restrict__ cnt) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const uint32_t s = slot_of[c];
+    uint32_t m = 1;
+    for (uint32_t k = 0; k < ncnt[s]; ++k) m += (nbr[nidx((int)k, s, np)] & kJMask) != s;
+    cnt[c] = m;
+}
+
+__global__ void k_export_fill(int n, const uint32_t* __restrict__ slot_of, const uint32_t* __restrict__ ncnt,
+                              const uint32_t* __restrict__ nbr, size_t np, const uint32_t* __restrict__ orig,
+                              const uint64_t* __restrict__ off, uint64_t* __restrict__ idx) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const uint32_t s = slot_of[c];
+    uint64_t* seg = idx + off[c];
+    const uint64_t len = off[c + 1] - off[c];
+    seg[0] = (uint64_t)c;
+    uint64_t m = 1;
+    for (uint32_t k = 0; k < ncnt[s] && m < len; ++k) {
+        const uint32_t j = nbr[nidx((int)k, s, np)] & kJMask;
+        if (j == s) continue;
+        const uint64_t v = orig[j];
+        uint64_t p = m++;
+        while (p > 0 && seg[p - 1] > v) {  // insertion: the segment stays ascending
+            seg[p] = seg[p - 1];
+            --p;
+        }
+        seg[p] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Verlet list
 // ---------------------------------------------------------------------------
 
@@ -732,7 +770,57 @@ int nlist_list_for(mdg_system* sys, const double x[3], std::vector<uint64_t>& fo
     return MDG_OK;
 }
 
+// CSR offsets (n + 1) of the exported list, counted on the device.
+int nlist_export_offsets(mdg_system* sys, std::vector<uint64_t>& off) {
+    const size_t n = sys->n;
+    off.assign(n + 1, 0);
+    if (n == 0) return MDG_OK;
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    // the spare slot-order buffer takes the counts (free between rebuilds)
+    uint32_t* cnt = sys->key;
+    k_export_counts<<<nblk(n), kBlock, 0, st>>>((int)n, sys->slot_of, sys->ncnt, sys->nbr, sys->np, cnt);
+    MDG_LAUNCHED(ctx);
+    std::vector<uint32_t> h(n);
+    MDG_CUDA(cudaMemcpyAsync(h.data(), cnt, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    for (size_t c = 0; c < n; ++c) off[c + 1] = off[c] + h[c];
+    return MDG_OK;
+}
+
+// The exported entries (off[n] of them) into the host array idx.
+int nlist_export_entries(mdg_system* sys, const std::vector<uint64_t>& off, uint64_t* idx) {
+    const size_t n = sys->n, total = off[n];
+    if (total == 0) return MDG_OK;
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    uint64_t *doff = nullptr, *didx = nullptr;
+    MDG_CUDA(cudaMalloc(&doff, (n + 1) * sizeof(uint64_t)));
+    if (cudaMalloc(&didx, total * sizeof(uint64_t)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(doff);
+        set_error("no device memory for the list export");
+        return MDG_ERR_NOMEM;
+    }
+    int rc = MDG_OK;
+    cudaError_t e = cudaMemcpyAsync(doff, off.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        k_export_fill<<<nblk(n), kBlock, 0, st>>>((int)n, sys->slot_of, sys->ncnt, sys->nbr, sys->np,
+                                                  sys->u32[ORIG][sys->cur], doff, didx);
+        ctx->launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(idx, didx, total * sizeof(uint64_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_status(e, "list export");
+    cudaFree(didx);
+    cudaFree(doff);
+    return rc;
+}
+
 int launch_trig(mdg_system* sys);
+
+// VerletList::updateint launch_trig(mdg_system* sys);
 
 // VerletList::updateint launch_trig(mdg_system* sys);
 

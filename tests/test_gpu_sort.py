@@ -139,6 +139,11 @@ def test_list_for_matches_oracle(periodic):
         nlo.update(-1.0)  # wrapped already: the same grid as the device's last rebuild
         for x in queries:
             assert list(nlg.list_for(x)) == sorted(nlo.list_for(x)), x
+        # the exported list (CSR in caller order, each atom's entries ascending)
+        off, idx = nlg.csr()
+        lists_o = nlo.lists()
+        for i in range(len(ao)):
+            assert np.array_equal(idx[off[i]:off[i + 1]], np.sort(np.asarray(lists_o[i], dtype=np.uint64))), i
 
     compare()
     # free flight (a zero-strength LJsCut) along the periodic axes, with
