@@ -355,10 +355,11 @@ __global__ void __launch_bounds__(kBlock) k_virials64(FArgs A, const PotSet* __r
 // at 5, where it spills).
 constexpr int kForceMinBlocks = 4;
 constexpr int kDensityMinBlocks = 4;
-// Multi bodies (per-pair kind, parameters and F' columns) spill at 64
-// registers; three blocks per SM (up to 85 registers) measured fastest on
+// The Multi force body (per-pair kind, parameters and F' columns) spills at
+// 64 registers; three blocks per SM (up to 85 registers) measured fastest on
 // NiAl B2 1M atoms: 7.2e8 atom-steps/s against 6.4e8 at four blocks and
-// 6.2e8 at two.
+// 6.2e8 at two. The Multi density body fits 64 registers without spills and
+// runs best at four blocks like the single one (7.39e8 against 7.20e8).
 constexpr int kMultiMinBlocks = 3;
 // MB = blocks of 256 threads per SM the register budget allows: a system's
 // launch shape (mdg_system_set_shape, chosen by the project's autotuner),
@@ -388,8 +389,9 @@ static int force_blocks(const mdg_system* sys, bool multi) {
                                                      : (multi ? kMultiMinBlocks : kForceMinBlocks);
 }
 static int density_blocks(const mdg_system* sys, bool multi) {
+    (void)multi;  // the Multi body fits the same budget
     return sys->shape[MDG_SHAPE_DENSITY_BLOCKS_PER_SM] ? sys->shape[MDG_SHAPE_DENSITY_BLOCKS_PER_SM]
-                                                       : (multi ? kMultiMinBlocks : kDensityMinBlocks);
+                                                       : kDensityMinBlocks;
 }
 
 template <bool MULTI, bool KICK>
