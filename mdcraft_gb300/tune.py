@@ -121,7 +121,7 @@ def tune_shapes(system, nlist, stepper, dt, signature, device=0, eam=True, steps
         got = table[key]
         for name, v in got["best"].items():
             system.set_shape(name, v)
-        return got["best"], got["seconds"]
+        return got["best"], {k: {int(a): b for a, b in v.items()} for k, v in got["seconds"].items()}
     ctx = system.ctx
     best, seconds = {}, {}
     # the list build, on its own rebuilds
