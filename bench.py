@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="mdg", choices=["mdg", "reference"])
     ap.add_argument("--ncell", type=int, default=63)
-    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=60)  # spans about two list rebuilds
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
