@@ -6,9 +6,12 @@ stream itself, each candidate on the same sample through its own server, and
 the fastest is kept.
 
 A system's step kernels (`tune_shapes`): the cells per block of the list
-build (2, 4 or 8 warps, a cell each) are timed on the system's own
-rebuilds, then the register budgets of the mixed force and density passes
-(blocks of 256 threads per SM) on its own steps, one dimension at a time.
+build (2, 4 or 8 warps, a cell each) are timed on the system's own rebuilds
+(median of single rebuilds), then the register budgets of the mixed force
+and density passes (blocks of 256 threads per SM) by the CUDA events the
+step loop puts around each of its force and density launches, one
+dimension at a time. Whole-step times are not used: a list rebuild (about
+three steps' worth of work) lands in some windows and not others.
 
 Results are cached per (GPU, workload signature) in `_build/tune.json`
 beside the library, so a later run on the same GPU and workload reuses the
@@ -101,16 +104,35 @@ SHAPE_CANDIDATES = {"list_cells_per_block": (2, 4, 8), "force_blocks_per_sm": (3
                     "density_blocks_per_sm": (3, 4, 5)}
 
 
-def _timed(ctx, fn, reps):
-    ctx.synchronize()
-    t0 = time.perf_counter()
+def _median_call(ctx, fn, reps):
+    """Median wall time of `reps` single calls (each synchronised)."""
+    ts = []
     for _ in range(reps):
+        ctx.synchronize()
+        t0 = time.perf_counter()
         fn()
-    ctx.synchronize()
-    return (time.perf_counter() - t0) / reps
+        ctx.synchronize()
+        ts.append(time.perf_counter() - t0)
+    ts.sort()
+    return ts[len(ts) // 2]
 
 
-def tune_shapes(system, nlist, stepper, dt, signature, device=0, eam=True, steps=30, rebuilds=6, use_cache=True):
+def _stage_seconds(ctx, run, stage):
+    """Mean device time of one launch of `stage` ("forces", "density") over
+    the launches `run()` makes, from the events of the context's timing
+    mode."""
+    ctx.set_timing(True)
+    try:
+        run()
+        ms, count = ctx.stage_time(stage)
+    finally:
+        ctx.set_timing(False)
+    if count == 0:
+        raise RuntimeError(f"no {stage} launches to time")
+    return ms / count / 1e3
+
+
+def tune_shapes(system, nlist, stepper, dt, signature, device=0, eam=True, steps=30, rebuilds=7, use_cache=True):
     """Launch shapes for one system (a Context's System with its VerletList
     and Verlet stepper). The system's state advances while it is measured.
     Returns ({shape: value}, {shape: {value: seconds}}) and leaves the
@@ -129,19 +151,20 @@ def tune_shapes(system, nlist, stepper, dt, signature, device=0, eam=True, steps
     for v in SHAPE_CANDIDATES["list_cells_per_block"]:
         system.set_shape("list_cells_per_block", v)
         nlist.update(-1.0)
-        sec[v] = _timed(ctx, lambda: nlist.update(-1.0), rebuilds)
+        sec[v] = _median_call(ctx, lambda: nlist.update(-1.0), rebuilds)
     best["list_cells_per_block"] = min(sec, key=sec.get)
     seconds["list_cells_per_block"] = sec
     system.set_shape("list_cells_per_block", best["list_cells_per_block"])
-    # the force and density passes, on steps (a warm-up run captures the graph)
-    for name in ("force_blocks_per_sm", "density_blocks_per_sm"):
+    # the force and density passes, per launch (a short run first loads the
+    # candidate's kernels)
+    for name, stage in (("force_blocks_per_sm", "forces"), ("density_blocks_per_sm", "density")):
         if name == "density_blocks_per_sm" and not eam:
             continue
         sec = {}
         for v in SHAPE_CANDIDATES[name]:
             system.set_shape(name, v)
             stepper.run(system, dt, 2)
-            sec[v] = _timed(ctx, lambda: stepper.run(system, dt, steps), 1) / steps
+            sec[v] = _stage_seconds(ctx, lambda: stepper.run(system, dt, steps), stage)
         best[name] = min(sec, key=sec.get)
         seconds[name] = sec
         system.set_shape(name, best[name])

@@ -2,7 +2,9 @@
 on CPU with stand-ins for the system, list and stepper: it times every
 candidate of each shape, keeps the fastest, leaves it set on the system,
 skips the density budget for pair-only systems, and a second call with the
-same GPU and workload signature takes the cached choice without measuring."""
+same GPU and workload signature takes the cached choice without measuring.
+The force and density budgets are compared by per-launch device times,
+which the list rebuilds inside the timed steps do not enter."""
 import time
 
 import pytest
@@ -11,15 +13,34 @@ from mdcraft_gb300 import tune
 
 
 class _Ctx:
+    """Stand-in for a Context's timing mode: per-stage (ms, launches)."""
+
+    def __init__(self):
+        self.timing = False
+        self.acc = {}
+
     def synchronize(self):
         pass
 
+    def set_timing(self, on=True):
+        self.timing = bool(on)
+        self.acc = {}
+
+    def stage_time(self, stage):
+        return self.acc.get(stage, (0.0, 0))
+
+    def record(self, stage, seconds):
+        if self.timing:
+            ms, n = self.acc.get(stage, (0.0, 0))
+            self.acc[stage] = (ms + seconds * 1e3, n + 1)
+
 
 class _System:
-    def __init__(self):
+    def __init__(self, eam=True):
         self.ctx = _Ctx()
         self.shape = {}
         self.calls = []
+        self.eam = eam
 
     def set_shape(self, name, v):
         self.shape[name] = v
@@ -41,11 +62,18 @@ class _List:
 
 
 class _Stepper:
+    """Each step: a force launch (and a density launch for EAM) whose device
+    time is the candidate's cost, plus a rebuild every third step that the
+    per-launch times must not see."""
+
     def run(self, system, dt, steps):
-        c = _COST["force_blocks_per_sm"][system.shape["force_blocks_per_sm"]]
-        if "density_blocks_per_sm" in system.shape:
-            c += _COST["density_blocks_per_sm"][system.shape["density_blocks_per_sm"]]
-        time.sleep(c * steps)
+        for k in range(steps):
+            system.ctx.record("forces", _COST["force_blocks_per_sm"][system.shape["force_blocks_per_sm"]])
+            if system.eam:
+                d = system.shape.get("density_blocks_per_sm", 4)
+                system.ctx.record("density", _COST["density_blocks_per_sm"][d])
+            if k % 3 == 2:
+                system.ctx.record("rebuild", 1e-2)
 
 
 @pytest.fixture
@@ -68,11 +96,12 @@ def test_picks_fastest_and_caches(cache):
     best2, sec2 = tune.tune_shapes(s2, None, None, 1e-3, signature="fake")
     assert best2 == best and s2.shape == best
     assert sorted(sec2["force_blocks_per_sm"]) == [3, 4]  # integer keys, as when measured
+    assert sec["force_blocks_per_sm"][4] == pytest.approx(2.5e-4)  # per launch, rebuilds excluded
     assert len(s2.calls) == len(best)
 
 
 def test_pair_only_system_skips_density(cache):
-    s = _System()
+    s = _System(eam=False)
     best, sec = tune.tune_shapes(s, _List(s), _Stepper(), 1e-3, signature="pair", eam=False, steps=4,
                                  rebuilds=2, use_cache=False)
     assert set(best) == {"list_cells_per_block", "force_blocks_per_sm"}
