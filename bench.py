@@ -273,8 +273,7 @@ def run_mdg(args, rank, world, local):
     rms = np.sqrt(np.mean(np.sum(f64 ** 2, axis=1)))
     err_l2 = float(np.linalg.norm(fmx - f64) / np.linalg.norm(f64))
     err_max = float(dF.max() / rms)
-    off, _ = nl.csr()
-    L = float((off[-1] - n) / n)  # listed neighbours per atom, self excluded
+    L = float((nl.total() - n) / n)  # listed neighbours per atom, self excluded
 
     # FP64 form throughput (same loop, FP64 stages)
     st64 = mdg.Verlet(s64)

@@ -306,6 +306,12 @@ class VerletList:
         _check(lib().mdg_nlist_decide(self.sys.h, C.byref(v)))
         return bool(v.value)
 
+    def total(self) -> int:
+        """Entries of the whole list, self entries included (mdg_nlist_total)."""
+        tot = C.c_size_t()
+        _check(lib().mdg_nlist_total(self.sys.h, C.byref(tot)))
+        return tot.value
+
     def csr(self):
         tot = C.c_size_t()
         _check(lib().mdg_nlist_total(self.sys.h, C.byref(tot)))

@@ -167,8 +167,7 @@ def nial(device=0, steps=500, ncell=80, cpu_steps=4):
     smx.stages(sysg)
     fmx = sysg.forces()
     err = _force_error(fmx, f64)
-    off, _ = nl.csr()
-    L = float((off[-1] - len(atoms)) / len(atoms))
+    L = float((nl.total() - len(atoms)) / len(atoms))
     st64 = Verlet(s64)
     st64.run(sysg, p["dt"], 1)
     sec64 = _timed_run(ctx, sysg, st64, p["dt"], 5)

@@ -300,26 +300,58 @@ __global__ void k_export_counts(int n, const uint32_t* __restrict__ slot_of, con
     cnt[c] = m;
 }
 
-__global__ void k_export_fill(int n, const uint32_t* __restrict__ slot_of, const uint32_t* __restrict__ ncnt,
-                              const uint32_t* __restrict__ nbr, size_t np, const uint32_t* __restrict__ orig,
-                              const uint64_t* __restrict__ off, uint64_t* __restrict__ idx) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    const uint32_t s = slot_of[c];
+// A warp per atom: the entries are collected in shared memory in list order,
+// then each lane writes its entries at their ranks (the values are distinct:
+// every neighbour appears once, the atom itself once). Lists longer than
+// kExportWarpMax entries take a serial insertion on lane 0.
+constexpr int kExportWarps = 8, kExportWarpMax = 256;
+
+__global__ void __launch_bounds__(kExportWarps * 32)
+    k_export_fill(int n, const uint32_t* __restrict__ slot_of, const uint32_t* __restrict__ ncnt,
+                  const uint32_t* __restrict__ nbr, size_t np, const uint32_t* __restrict__ orig,
+                  const uint64_t* __restrict__ off, uint64_t* __restrict__ idx) {
+    __shared__ uint32_t buf[kExportWarps][kExportWarpMax];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * kExportWarps + w;
+    if (c >= n) return;  // the whole warp
+    const uint32_t s = slot_of[c], cnt = ncnt[s];
     uint64_t* seg = idx + off[c];
-    const uint64_t len = off[c + 1] - off[c];
-    seg[0] = (uint64_t)c;
-    uint64_t m = 1;
-    for (uint32_t k = 0; k < ncnt[s] && m < len; ++k) {
-        const uint32_t j = nbr[nidx((int)k, s, np)] & kJMask;
-        if (j == s) continue;
-        const uint64_t v = orig[j];
-        uint64_t p = m++;
-        while (p > 0 && seg[p - 1] > v) {  // insertion: the segment stays ascending
-            seg[p] = seg[p - 1];
-            --p;
+    const uint32_t len = (uint32_t)(off[c + 1] - off[c]);
+    if (len > (uint32_t)kExportWarpMax) {
+        if (lane != 0) return;
+        seg[0] = (uint64_t)c;
+        uint32_t m = 1;
+        for (uint32_t k = 0; k < cnt && m < len; ++k) {
+            const uint32_t j = nbr[nidx((int)k, s, np)] & kJMask;
+            if (j == s) continue;
+            const uint64_t v = orig[j];
+            uint32_t p = m++;
+            while (p > 0 && seg[p - 1] > v) {
+                seg[p] = seg[p - 1];
+                --p;
+            }
+            seg[p] = v;
         }
-        seg[p] = v;
+        return;
+    }
+    uint32_t* b = buf[w];
+    if (lane == 0) b[0] = (uint32_t)c;
+    uint32_t base = 1;
+    for (uint32_t k0 = 0; k0 < cnt; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        const uint32_t j = k < cnt ? (nbr[nidx((int)k, s, np)] & kJMask) : s;
+        const bool keep = k < cnt && j != s;
+        const unsigned mask = __ballot_sync(0xffffffffu, keep);
+        const uint32_t pos = base + __popc(mask & ((1u << lane) - 1u));
+        if (keep && pos < len) b[pos] = orig[j];
+        base += __popc(mask);
+    }
+    __syncwarp();
+    for (uint32_t p = lane; p < len; p += 32) {
+        const uint32_t v = b[p];
+        uint32_t r = 0;
+        for (uint32_t q = 0; q < len; ++q) r += b[q] < v;
+        seg[r] = v;
     }
 }
 
@@ -805,8 +837,8 @@ int nlist_export_entries(mdg_system* sys, const std::vector<uint64_t>& off, uint
     int rc = MDG_OK;
     cudaError_t e = cudaMemcpyAsync(doff, off.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        k_export_fill<<<nblk(n), kBlock, 0, st>>>((int)n, sys->slot_of, sys->ncnt, sys->nbr, sys->np,
-                                                  sys->u32[ORIG][sys->cur], doff, didx);
+        k_export_fill<<<(unsigned)((n + kExportWarps - 1) / kExportWarps), kExportWarps * 32, 0, st>>>(
+            (int)n, sys->slot_of, sys->ncnt, sys->nbr, sys->np, sys->u32[ORIG][sys->cur], doff, didx);
         ctx->launches++;
         e = cudaGetLastError();
     }
