@@ -12,6 +12,9 @@ class VerletList:
     def __init__(self, atoms, neighbors, domain, threads=None, half: bool = False):
         if neighbors is not atoms:
             raise NotImplementedError("one domain: the neighbours must be the atoms themselves")
+        if half and threads is not None and threads.count > 1:  # verlet-list.cxx:28-31
+            raise RuntimeError("Half Verlet lists are currently incompatible with multithreaded pair-force "
+                               "evaluation. Disable threads or use a full neighbor list.")
         atoms._device = DeviceAtoms(atoms, domain)
         self._dev = atoms._device
         self._nl = _mdg.VerletList(self._dev.sys, half=half)
@@ -21,6 +24,10 @@ class VerletList:
         self._dev.push()
         self._nl.update(kbuf)
         self._dev.pull()  # positions fitted into the period, as the reference does
+
+    @property
+    def half(self) -> bool:
+        return self._nl.half
 
     def decide(self) -> bool:
         self._dev.push()
