@@ -192,6 +192,20 @@ int mdg_pot_pair_create_from_file(const char* path, mdg_potential** out);
 int mdg_pot_destroy(mdg_potential* pot);
 /* Base::rcut() (mdcraft/solver/potential/base.h:37). */
 int mdg_pot_rcut(mdg_potential* pot, double* rcut);
+/* Potential::value(r2[], U[], n) (EAM.cxx:141-174, pair.cxx:81-114,
+ * LJs.cxx:61-71; the Python bindings' value(), _potential.cxx:88-201): the
+ * pair energy term of each squared distance (V(r)/2r for the tabulated
+ * types, 0 past the table), with no cutoff test, as the reference; LJsCut
+ * keeps the base class's value (base.cxx:19) and gives 0. Host arrays of n
+ * doubles; evaluated on ctx's device with the FP64 bodies of the force
+ * kernels. */
+int mdg_pot_values(mdg_ctx* ctx, mdg_potential* pot, const double* r2, size_t n, double* u);
+/* EAM::embeddingEnergy(rho[], F[], dF[], n) (EAM.cxx:562-601): F(rho) and
+ * F'(rho) (dF may be NULL). Densities outside the table take the reference's
+ * extrapolation, with its output array read as zero. MDG_ERR_INVALID for a
+ * potential without an embedding table (LJsCut, LJs, Pair). */
+int mdg_pot_embedding(mdg_ctx* ctx, mdg_potential* pot, const double* rho, size_t n, double* F,
+                      double* dF);
 
 /* ---- solvers ------------------------------------------------------------------- */
 /* Single(pot, boundary) (mdcraft/solver/single.h:37-42). periodic != 0

@@ -85,6 +85,8 @@ def lib():
         "mdg_pot_eam_create": ([dp, vp, vp, vp, ip, dp, ip, dp, pp], ip),
         "mdg_pot_eam_create_from_file": ([C.c_char_p, pp], ip), "mdg_pot_destroy": ([vp], ip),
         "mdg_pot_rcut": ([vp, C.POINTER(C.c_double)], ip),
+        "mdg_pot_values": ([vp, vp, vp, sz, vp], ip),
+        "mdg_pot_embedding": ([vp, vp, vp, sz, vp, vp], ip),
         "mdg_solver_single": ([vp, ip, pp], ip), "mdg_solver_multi": ([ip, ip, pp], ip),
         "mdg_solver_add_potential": ([vp, ip, ip, vp], ip), "mdg_solver_destroy": ([vp], ip),
         "mdg_solver_num_stages": ([vp, C.POINTER(C.c_int)], ip), "mdg_solver_set_precision": ([vp, ip], ip),
@@ -360,6 +362,22 @@ class _Pot:
         v = C.c_double()
         _check(lib().mdg_pot_rcut(self.h, C.byref(v)))
         return v.value
+
+    def values(self, ctx: "Context", r2) -> np.ndarray:
+        """Potential::value of each squared distance, on ctx's device
+        (mdg_pot_values)."""
+        r2 = np.ascontiguousarray(r2, dtype=np.float64).ravel()
+        u = np.zeros(len(r2))
+        _check(lib().mdg_pot_values(ctx.h, self.h, _ptr(r2), len(r2), _ptr(u)))
+        return u
+
+    def embedding(self, ctx: "Context", rho):
+        """EAM::embeddingEnergy: (F, F') of each density (mdg_pot_embedding)."""
+        rho = np.ascontiguousarray(rho, dtype=np.float64).ravel()
+        F = np.zeros(len(rho))
+        dF = np.zeros(len(rho))
+        _check(lib().mdg_pot_embedding(ctx.h, self.h, _ptr(rho), len(rho), _ptr(F), _ptr(dF)))
+        return F, dF
 
     def __del__(self):
         try:

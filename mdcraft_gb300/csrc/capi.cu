@@ -1243,6 +1243,32 @@ int mdg_pot_rcut(mdg_potential* p, double* rcut) {
     return MDG_OK;
 }
 
+int mdg_pot_values(mdg_ctx* ctx, mdg_potential* p, const double* r2, size_t n, double* u) {
+    if (!ctx || !p || ((!r2 || !u) && n)) return MDG_ERR_INVALID;
+    if (n == 0) return MDG_OK;
+    MDG_CUDA(cudaSetDevice(ctx->device));
+    int rc = pot_upload(p, ctx->device);
+    if (rc) return rc;
+    PotParams P;
+    fill_params(p, P, nullptr, nullptr);  // analytic types read no table
+    return pot_eval(P, 0, r2, n, u, nullptr, ctx->stream);
+}
+
+int mdg_pot_embedding(mdg_ctx* ctx, mdg_potential* p, const double* rho, size_t n, double* F, double* dF) {
+    if (!ctx || !p || ((!rho || !F) && n)) return MDG_ERR_INVALID;
+    if (p->type != POT_EAM) {
+        set_error("the potential has no embedding table");
+        return MDG_ERR_INVALID;
+    }
+    if (n == 0) return MDG_OK;
+    MDG_CUDA(cudaSetDevice(ctx->device));
+    int rc = pot_upload(p, ctx->device);
+    if (rc) return rc;
+    PotParams P;
+    fill_params(p, P, nullptr, nullptr);
+    return pot_eval(P, 1, rho, n, F, dF, ctx->stream);
+}
+
 // ---- solvers ----------------------------------------------------------------
 static void set_stages(mdg_solver* s, int type, bool first) {
     if (type == POT_TAB || type == POT_LJS) type = POT_LJCUT;  // all potential::type::pair

@@ -666,4 +666,63 @@ int launch_virials(mdg_system* sys, const PotSet* dps, const PotSet& ps) {
     return MDG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Potential::value and EAM::embeddingEnergy on arrays (the analysis calls of
+// python/mdcraft/solver/potential/_potential.cxx:88-168): the FP64 bodies of
+// the force kernels. value: EAM.cxx:141-174 and pair.cxx:81-114 (V(r)/2r
+// from the Vpar spline, 0 past the table, no cutoff test), LJs.cxx:61-71;
+// LJsCut keeps Base::value (base.cxx:19): 0.
+// ---------------------------------------------------------------------------
+
+__global__ void k_pot_values(PotParams P, int n, const double* __restrict__ r2, double* __restrict__ u) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double e = 0.0;
+    if (P.type == POT_EAM) eam_ff64(P, r2[i], 0.0, &e);
+    else if (P.type == POT_TAB) tab_ff64(P, r2[i], &e);
+    else if (P.type == POT_LJS) ljs_ff64(P, r2[i], &e);
+    u[i] = e;
+}
+
+__global__ void k_pot_embedding(PotParams P, int n, const double* __restrict__ rho, double* __restrict__ F,
+                                double* __restrict__ dF, DevStatus* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double EF = 0.0, d = 0.0;
+    eam_embed64(P, rho[i], &EF, &d, st);
+    F[i] = EF;
+    dF[i] = d;
+}
+
+// what = 0: u[k] = value(x[k]); what = 1: F, dF of density x[k]. Host arrays
+// in and out through one device scratch block; waits on `st`.
+int pot_eval(const PotParams& P, int what, const double* x, size_t n, double* out0, double* out1,
+             cudaStream_t st) {
+    if (n == 0) return MDG_OK;
+    if (n > (size_t)INT32_MAX) {
+        set_error("too many values in one call");
+        return MDG_ERR_INVALID;
+    }
+    double* d = nullptr;
+    DevStatus* ds = nullptr;
+    MDG_CUDA(cudaMalloc(&d, 3 * n * sizeof(double)));
+    int rc = MDG_OK;
+    cudaError_t e = cudaMalloc(&ds, sizeof(DevStatus));
+    if (e == cudaSuccess) e = cudaMemsetAsync(ds, 0, sizeof(DevStatus), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, x, n * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        if (what == 0) k_pot_values<<<nblk(n), kBlock, 0, st>>>(P, (int)n, d, d + n);
+        else k_pot_embedding<<<nblk(n), kBlock, 0, st>>>(P, (int)n, d, d + n, d + 2 * n, ds);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out0, d + n, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && out1)
+        e = cudaMemcpyAsync(out1, d + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_status(e, "potential evaluation");
+    cudaFree(ds);
+    cudaFree(d);
+    return rc;
+}
+
 }  // namespace mdg

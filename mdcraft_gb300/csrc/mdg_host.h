@@ -278,6 +278,8 @@ int solo_persistent_launch(cudaStream_t stream, int threads, int blocks, const v
 int solo_blocks_per_sm(int threads, int* blocks);
 int nlist_build(mdg_system* sys, double kbuf, int half);
 int nlist_sort_perm(mdg_system* sys, uint32_t* perm);
+int pot_eval(const PotParams& P, int what, const double* x, size_t n, double* out0, double* out1,
+             cudaStream_t st);
 int nlist_list_for(mdg_system* sys, const double x[3], std::vector<uint64_t>& found);
 int nlist_export_offsets(mdg_system* sys, std::vector<uint64_t>& off);
 int nlist_export_entries(mdg_system* sys, const std::vector<uint64_t>& off, uint64_t* idx);

@@ -7,6 +7,14 @@ import numpy as np
 
 import mdcraft_gb300 as _mdg
 
+from .._engine import context as _context
+
+
+def _value_at(pot, r):
+    """value(r) of a scalar distance: the pair energy term at r^2 = r*r (the
+    bindings build the vector (r, 0, 0), _potential.cxx:155-159, 197-201)."""
+    return float(pot.values(_context(), np.array([float(r) * float(r)]))[0])
+
 
 class EAM:
     def __init__(self, *args, **kw):
@@ -24,6 +32,15 @@ class EAM:
     @property
     def rcut(self) -> float:
         return self._p.rcut()
+
+    def value(self, r: float) -> float:
+        """Pair energy term at distance r (_potential.cxx:155-159)."""
+        return _value_at(self._p, r)
+
+    def embeddingEnergy(self, r):
+        """F(rho) of each density (_potential.cxx:160-168)."""
+        F, _ = self._p.embedding(_context(), r)
+        return F
 
 
 class LJsCut:
@@ -45,6 +62,13 @@ class LJs:
     def rcut(self) -> float:
         return self._p.rcut()
 
+    def value(self, r2):
+        """value(array of r^2) -> array, or value(r) -> float for a scalar
+        distance (_potential.cxx:88-100)."""
+        if np.ndim(r2) == 0:
+            return _value_at(self._p, r2)
+        return self._p.values(_context(), np.asarray(r2, dtype=np.float64))
+
 
 class Pair:
     """Pair(Rcutoff, pairPotential, NrPot, drPot) or Pair(filename)
@@ -63,6 +87,11 @@ class Pair:
     @property
     def rcut(self) -> float:
         return self._p.rcut()
+
+
+    def value(self, r: float) -> float:
+        """Pair energy term at distance r (_potential.cxx:197-201)."""
+        return _value_at(self._p, r)
 
 
 # the reference's module also exports LJsCut under this name (_potential.cxx:110)

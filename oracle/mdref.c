@@ -1197,6 +1197,21 @@ static inline double ljs_ff(const md_pot* p, double r2, double* E) {
     return p->aVr2 * (Ur * (Ur - 0.5) * FV + (p->aLJ + p->bLJ * XX) * XX);
 }
 
+void md_pot_values(const md_pot* p, const double* r2, size_t n, double* u) {
+    /* Potential::value(r2[], U[], n): EAM.cxx:141-174 and pair.cxx:81-114
+     * (V(r)/2r from the Vpar spline, 0 past the table), LJs.cxx:61-71;
+     * LJsCut keeps Base::value (base.cxx:19), which leaves U alone: 0 here. */
+    for (size_t k = 0; k < n; ++k) {
+        double e = 0.0;
+        if (p->type == MD_POT_EAM || p->type == MD_POT_TAB) {
+            e = eam_value(p, &r2[k], 1);
+        } else if (p->type == MD_POT_LJS) {
+            ljs_ff(p, r2[k], &e);
+        }
+        u[k] = e;
+    }
+}
+
 /* LJs::force(self, ...) (LJs.cxx:196-256) */
 static void ljs_force(const md_pot* p, md_atom* a, const nview* v) {
     double F[3] = {0.0, 0.0, 0.0};

@@ -137,6 +137,8 @@ void md_eam_init_spline(const double* y, double* z, double H1, size_t N,
 /* Copies the knot-slope tables (sizes Nr1, Nr1, Nrh1). */
 void md_eam_slopes(const md_pot* p, double* dVpar, double* dRho,
                    double* dFemb);
+/* Potential::value on squared distances (EAM, Pair, LJs; 0 for LJsCut). */
+void md_pot_values(const md_pot* p, const double* r2, size_t n, double* u);
 /* Embedding F and F' for one density value (EAM.cxx:562-601). */
 void md_eam_embedding(const md_pot* p, double rho, double* F, double* dF);
 

@@ -103,6 +103,7 @@ def lib():
         L.md_eam_init_spline.argtypes = [vp, vp, dp, sz, ip]
         L.md_eam_slopes.argtypes = [vp, vp, vp, vp]
         L.md_eam_embedding.argtypes = [vp, dp, vp, vp]
+        L.md_pot_values.argtypes = [vp, vp, sz, vp]
         L.md_solver_single.argtypes = [vp, vp, ip]
         L.md_solver_single.restype = vp
         L.md_solver_multi.argtypes = [ip, vp, ip]
@@ -313,6 +314,14 @@ class VerletList:
         and returns a copy ordered by owning cell (x fastest), ascending
         index inside a cell."""
         return sort_atoms(self.domain, atoms)
+
+
+def pot_values(pot, r2) -> np.ndarray:
+    """md_pot_values: Potential::value of each squared distance."""
+    r2 = np.ascontiguousarray(r2, dtype=np.float64)
+    u = np.zeros(len(r2))
+    lib().md_pot_values(pot.h, _ptr(r2), len(r2), _ptr(u))
+    return u
 
 
 class LJsCut:
