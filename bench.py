@@ -122,9 +122,10 @@ def make_workload(ncell):
     return W.eam_cu_fcc(ncell=ncell)
 
 
-def cpu_baseline(ncell, steps, threads=None):
+def cpu_baseline(ncell, steps, threads=None, warmup=1):
     """The CPU oracle (C restatement of the reference path, all host threads)
-    on the same workload: one list build, then `steps` timed driver steps."""
+    on the same workload: one list build, `warmup` untimed driver steps,
+    then `steps` timed driver steps."""
     from oracle import mdref as R
     atoms, box, _, p = make_workload(ncell)
     threads = threads or R.hardware_threads()
@@ -140,13 +141,15 @@ def cpu_baseline(ncell, steps, threads=None):
     nl.update(-1.0)
     sol.prepare(ao)
     sol.stages(ao, nl)
-    sol.run(ao, nl, d, p["dt"], 1)  # warm-up step
+    if warmup > 0:
+        sol.run(ao, nl, d, p["dt"], warmup)
     t0 = time.perf_counter()
     rebuilds = sol.run(ao, nl, d, p["dt"], steps)
     dt = time.perf_counter() - t0
     return {"value": len(ao) * steps / dt, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"{len(ao)}-atom EAM Cu, {steps} timed Verlet steps after one list build "
-                      f"({rebuilds} rebuilds), {threads} threads", "seconds": dt}
+            "sample": f"{len(ao)}-atom EAM Cu, {steps} timed Verlet steps after one list build and "
+                      f"{warmup} warm-up steps ({rebuilds} rebuilds in the timed steps), {threads} threads",
+            "seconds": dt, "rebuilds": rebuilds}
 
 
 def run_reference(args, rank, world):
@@ -154,16 +157,18 @@ def run_reference(args, rank, world):
         return
     from oracle import mdref as R
     threads = R.hardware_threads()
-    # size the timed sample from one measured step: a few minutes at most
-    probe = cpu_baseline(args.ncell, 1, threads)
+    # size the timed sample from one measured step (its own run, no warm-up):
+    # the whole arm stays within a few minutes
+    probe = cpu_baseline(args.ncell, 1, threads, warmup=0)
     per_step = probe["seconds"]
+    warmup = max(0, min(args.warmup, int(30.0 / max(per_step, 1e-3))))
     steps = max(1, min(args.steps, int(90.0 / max(per_step, 1e-3))))
-    cb = cpu_baseline(args.ncell, steps, threads)
+    cb = cpu_baseline(args.ncell, steps, threads, warmup=warmup)
     line = {"metric": METRIC, "value": cb["value"], "unit": METRIC, "n_gpus": args.gpus, "steps": steps,
-            "warmup": 2, "ms_per_step": 1e3 * cb["seconds"] / steps, "higher_is_better": True,
+            "warmup": warmup, "ms_per_step": 1e3 * cb["seconds"] / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "atoms": 4 * args.ncell ** 3, "threads": threads},
-            "impl": "reference",
+            "impl": "reference", "rebuilds": cb["rebuilds"],
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -174,6 +179,48 @@ def peaks():
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         return {}
+
+
+# ncu summary of the dominant kernel (committed under profiles/): its DRAM
+# bytes of one launch and the atoms that launch processed give the traffic
+# per atom; its L1 figure names what limits the kernel
+FORCE_PROFILE = os.path.join(ROOT, "profiles", "k_eam_mixed_eam_cu_442k.md")
+
+
+def profile_figures(path):
+    """dram__bytes_read.sum + dram__bytes_write.sum (bytes), the atoms of the
+    captured launch and l1tex__throughput (%) from an ncu summary."""
+    import re
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+
+    def metric(name):
+        m = re.search(r"`" + re.escape(name) + r"`\s*\|\s*([0-9.]+)\s*(MB|GB|KB|%|us)?", text)
+        if not m:
+            return None
+        v = float(m.group(1))
+        return v * {"GB": 1e9, "MB": 1e6, "KB": 1e3}.get(m.group(2) or "", 1.0)
+
+    atoms = re.search(r"Case:\s*([0-9,]+) atoms", text)
+    rd, wr = metric("dram__bytes_read.sum"), metric("dram__bytes_write.sum")
+    if atoms is None or rd is None or wr is None:
+        return None
+    return {"bytes": rd + wr, "atoms": int(atoms.group(1).replace(",", "")),
+            "l1tex_pct": metric("l1tex__throughput.avg.pct_of_peak_sustained_active"),
+            "dram_pct": metric("gpu__dram_throughput.avg.pct_of_peak_sustained_elapsed"),
+            "file": os.path.relpath(path, ROOT)}
+
+
+def energies(sol, sysg):
+    """Ep + Em and Etot after prepare, stages and virials (the reference's
+    recompute_state, test/cxx/support/md_test_utils.h:241-253)."""
+    sol.prepare(sysg)
+    sol.stages(sysg)
+    sol.virials(sysg)
+    m = sysg.measure()
+    return m["Ep"] + m["Em"], m["Etot"]
 
 
 SERVE_WORKLOAD = ("serving stream: Poisson arrivals at 2000/s, 60% LJ argon (rc 2.5 sigma, skin 0.3 A, dt 2 fs) / "
@@ -235,7 +282,7 @@ def run_mdg(args, rank, world, local):
     dist = Dist(world, local)
     if args.config:
         if rank == 0:
-            from mdcraft_gb300 import benchmarks as BM
+            import bench_configs as BM
             clocks = Clocks(local)
             clocks.start()
             res = BM.CONFIGS[args.config](device=local)
@@ -275,7 +322,13 @@ def run_mdg(args, rank, world, local):
     err_max = float(dF.max() / rms)
     L = float((nl.total() - n) / n)  # listed neighbours per atom, self excluded
 
+    # energies of both forms at the start (both evaluate energies in FP64)
+    pot64_0, _ = energies(s64, sysg)
+    potmx_0, _ = energies(smx, sysg)
+
     # FP64 form throughput (same loop, FP64 stages)
+    s64.prepare(sysg)
+    s64.stages(sysg)
     st64 = mdg.Verlet(s64)
     st64.run(sysg, p["dt"], 1)
     ctx.synchronize()
@@ -283,6 +336,20 @@ def run_mdg(args, rank, world, local):
     st64.run(sysg, p["dt"], args.fp64_steps)
     ctx.synchronize()
     fp64_rate = n * args.fp64_steps / (time.perf_counter() - t0)
+    pot64_1, tot64_1 = energies(s64, sysg)
+    # the mixed form over the same 1 + fp64_steps steps from the same start:
+    # energy error of its trajectory against the FP64 form's
+    sysg.upload(atoms)
+    nl.update(-1.0)
+    smx.prepare(sysg)
+    smx.stages(sysg)
+    mdg.Verlet(smx).run(sysg, p["dt"], 1 + args.fp64_steps)
+    potmx_1, totmx_1 = energies(smx, sysg)
+    energy_error = {"at_start_potential_rel": abs(potmx_0 - pot64_0) / abs(pot64_0),
+                    "after_steps": 1 + args.fp64_steps,
+                    "potential_rel": abs(potmx_1 - pot64_1) / abs(pot64_1),
+                    "total_rel": abs(totmx_1 - tot64_1) / abs(tot64_1),
+                    "note": "mixed vs FP64 form from the same start; energies are evaluated in FP64 in both forms"}
 
     # launch shapes of the mixed step kernels, measured on this system
     # (project autotuner; cached per GPU and workload)
@@ -358,14 +425,17 @@ def run_mdg(args, rank, world, local):
     achieved = bytes_atom * n / (force_launch_ms / 1e3) / 1e9
     pk = peaks()
     peak = pk.get("hbm_gbs", 6800.0)
-    # DRAM bytes of one k_eam_mixed launch from ncu (read + write, 112.61 MB for 442,368 atoms of the
-    # same workload family, profiles/k_eam_mixed_eam_cu_442k.md), scaled to this launch by atoms
-    traffic = 112.61e6 / 442368 * n
-    roof = {"bound": "hbm", "kernel": "k_eam_mixed (EAM force, mixed)", "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum on 442,368 atoms, scaled by atoms",
+    prof = profile_figures(FORCE_PROFILE)
+    roof = {"bound": "hbm", "kernel": "k_eam_mixed (EAM force, mixed, with the second half-kick)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": (prof["bytes"] / prof["atoms"] * n) if prof else None,
             "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
             "bytes_per_atom": bytes_atom, "launch_ms": force_launch_ms}
+    if prof:
+        roof["traffic_source"] = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on "
+                                  f"{prof['atoms']:,} atoms ({prof['file']}), scaled to {n:,} atoms")
+        roof["limiter"] = {"l1tex_throughput_pct": prof["l1tex_pct"], "dram_throughput_pct": prof["dram_pct"],
+                           "source": prof["file"]}
 
     serving = None
     if not args.no_serve:
@@ -386,6 +456,7 @@ def run_mdg(args, rank, world, local):
                        "parallelism": f"replicas x{world}", "neighbours_per_atom": L},
             "fp64_form": {"value": fp64_rate, "unit": METRIC, "mixed_speedup": value / world / fp64_rate},
             "force_error": {"l2_rel": err_l2, "max_over_rms": err_max, "bar": 1e-5},
+            "energy_error": energy_error,
             "rebuilds": rebuilds,
             "stage_ms_per_launch": {"drift": drms / max(drn, 1), "density": dms / max(dn, 1),
                                     "forces_and_kick": force_launch_ms, "rebuild": rms_ / max(rn, 1)},

@@ -1,4 +1,6 @@
-"""Measurements of the benchmark configurations other than the headline one.
+"""Measurements of the benchmark configurations other than the headline one
+(bench.py --config NAME). A measurement harness beside bench.py, not part of
+the library: its CPU leg and checks call the oracle.
 
 Each function runs one configuration on the GPU through the public API and
 returns a dict (one JSON line of bench.py --config NAME):
@@ -22,9 +24,9 @@ import time
 
 import numpy as np
 
-from . import EAM, Context, Domain, LJsCut, Multi, Single, System, Verlet, VerletList
-from . import tune
-from . import workloads as W
+from mdcraft_gb300 import EAM, Context, Domain, LJsCut, Multi, Single, System, Verlet, VerletList
+from mdcraft_gb300 import tune
+from mdcraft_gb300 import workloads as W
 
 
 def _domain(box):
@@ -75,6 +77,33 @@ def _energy(sol, sysg):
     sol.prepare(sysg)
     sol.virials(sysg)
     return sysg.measure()
+
+
+def _state_energy(sol, sysg):
+    """(Ep + Em, Etot) after prepare, stages and virials (recompute_state,
+    test/cxx/support/md_test_utils.h:241-253)."""
+    sol.prepare(sysg)
+    sol.stages(sysg)
+    sol.virials(sysg)
+    m = sysg.measure()
+    return m["Ep"] + m["Em"], m["Etot"]
+
+
+def _energy_error(sysg, nl, atoms, s64, smx, dt, steps):
+    """Energy error of the mixed form against the FP64 form: both run `steps`
+    steps from the same start; energies are evaluated in FP64 in both forms,
+    so the difference is that of the trajectories."""
+    out = {}
+    for prec, sol in (("fp64", s64), ("mixed", smx)):
+        sysg.upload(atoms)
+        nl.update(-1.0)
+        e0 = _state_energy(sol, sysg)
+        Verlet(sol).run(sysg, dt, steps)
+        out[prec] = (e0, _state_energy(sol, sysg))
+    (p0, _), (p1, t1) = out["fp64"]
+    (q0, _), (q1, u1) = out["mixed"]
+    return {"at_start_potential_rel": abs(q0 - p0) / abs(p0), "after_steps": steps,
+            "potential_rel": abs(q1 - p1) / abs(p1), "total_rel": abs(u1 - t1) / abs(t1)}
 
 
 def _oracle_rate(atoms, box, params, steps, threads=None):
@@ -139,9 +168,13 @@ def lj_argon(device=0, steps=1000, cpu=True):
         sec = _timed_run(ctx, sysg, st, p["dt"], steps)
         e1 = _energy(sol, sysg)["Etot"]
         final[prec] = sysg.download()
+        final[prec + "_energy"] = _state_energy(sol, sysg)
         out[prec] = {"value": len(atoms) * steps / sec, "unit": "atom-steps/s", "ms_per_step": 1e3 * sec / steps,
                      "rebuilds": nl.rebuilds() - rb0, "energy_drift_rel": (e1 - e0) / abs(e0)}
         sysg.close()
+    (p1, t1), (q1, u1) = final["fp64_energy"], final["mixed_energy"]
+    out["energy_error_vs_fp64"] = {"after_steps": steps, "potential_rel": abs(q1 - p1) / abs(p1),
+                                   "total_rel": abs(u1 - t1) / abs(t1)}
     if cpu:
         rate, sec, rebuilds, ao, threads = _oracle_rate(atoms, box, p, steps)
         dr = np.abs(final["fp64"]["r"] - ao["r"]).max()
@@ -193,6 +226,7 @@ def nial(device=0, steps=500, ncell=80, cpu_steps=4):
     smx.prepare(sysg)
     smx.stages(sysg)
     err_run = _force_error(sysg.forces(), f64b)
+    eerr = _energy_error(sysg, nl, atoms, s64, smx, p["dt"], 20)
     n = len(atoms)
     out = {"config": f"NiAl B2 {ncell}^3 cells, 0.5% vacancies ({n} atoms), Multi with 3 EAM pair tables, "
                      "rc 6 A, skin 0.5 A, 600 K, dt 1 fs, mixed",
@@ -200,7 +234,8 @@ def nial(device=0, steps=500, ncell=80, cpu_steps=4):
            "mixed": {"value": n * steps / sec, "unit": "atom-steps/s", "ms_per_step": 1e3 * sec / steps,
                      "rebuilds": rebuilds},
            "fp64_form": {"value": n * 5 / sec64, "unit": "atom-steps/s", "steps": 5},
-           "force_error_vs_fp64": err, "force_error_vs_fp64_after_run": err_run, "shapes": shapes}
+           "force_error_vs_fp64": err, "force_error_vs_fp64_after_run": err_run, "energy_error_vs_fp64": eerr,
+           "shapes": shapes}
     out["mixed_speedup"] = out["mixed"]["value"] / out["fp64_form"]["value"]
     if cpu_steps:
         rate, secc, rebuilds, _, threads = _oracle_rate(atoms, box, p, cpu_steps)
@@ -237,12 +272,14 @@ def lj_liquid(device=0, steps=200, dims=(128, 128, 256), cpu_steps=1):
     st.run(sysg, p["dt"], 3)
     rb0 = nl.rebuilds()
     sec = _timed_run(ctx, sysg, st, p["dt"], steps)
+    rebuilds = nl.rebuilds() - rb0
+    eerr = _energy_error(sysg, nl, atoms, s64, smx, p["dt"], 10)
     n = len(atoms)
     out = {"config": f"LJ liquid rho*=0.8442 T*=0.72, fcc melt start, {n} atoms, rc 2.5 sigma, skin 0.3 sigma, "
                      f"dt*=0.005, mixed", "atoms": n, "steps": steps,
            "mixed": {"value": n * steps / sec, "unit": "atom-steps/s", "ms_per_step": 1e3 * sec / steps,
-                     "rebuilds": nl.rebuilds() - rb0},
-           "force_error_vs_fp64": err, "shapes": shapes}
+                     "rebuilds": rebuilds},
+           "force_error_vs_fp64": err, "energy_error_vs_fp64": eerr, "shapes": shapes}
     sysg.close()
     if cpu_steps:
         rate, secc, rebuilds, _, threads = _oracle_rate(atoms, box, p, cpu_steps)

@@ -310,8 +310,11 @@ int mdg_system_measure(mdg_system* sys, mdg_state* out);
  * synchronise. Scratch is a static device array of 256 KB held by every GPU
  * that loads the library: at most 8,388,608 atoms per call (larger n fails
  * with MDG_ERR_INVALID); calls whose kernels overlap on the GPU race on it.
- * The first call on a device looks the array up (cudaGetSymbolAddress); make
- * it before any stream capture. */
+ * The first call on a device looks the array up (cudaGetSymbolAddress),
+ * which with lazy module loading (the CUDA default) also loads the module
+ * and can synchronise: make that first call at set-up, as a warm-up, before
+ * any stream capture. An error already pending from an earlier CUDA call is
+ * returned without launching anything. */
 int mdg_measure_static(const double* d_m, const double* d_v, const double* d_Ep, const double* d_Em,
                        const double* d_V, size_t n, double* d_out, void* stream);
 /* Error/diagnostic flags accumulated on the device since the last call

@@ -268,7 +268,8 @@ static void for_each_buffer(mdg_system* sys, F&& f) {
         f((void**)&sys->r0[a], np * sizeof(double));
     }
     f((void**)&sys->cellp, np * sizeof(uint32_t));
-    f((void**)&sys->pos32, 2 * np * sizeof(float4));
+    f((void**)&sys->pos32, 2 * np * sizeof(int4));
+    f((void**)&sys->q0, np * sizeof(int4));
     f((void**)&sys->o0, np * sizeof(float4));
     f((void**)&sys->saved_rcut, np * sizeof(double));
     f((void**)&sys->saved_rns, np * sizeof(double));
@@ -277,7 +278,7 @@ static void for_each_buffer(mdg_system* sys, F&& f) {
     f((void**)&sys->bc, np * sizeof(uint8_t));
     f((void**)&sys->Fp64, (size_t)kMaxKinds * np * sizeof(double));
     f((void**)&sys->Fp32, (size_t)kMaxKinds * np * sizeof(float));
-    f((void**)&sys->trig32, np * sizeof(float));
+    f((void**)&sys->trig32, np * sizeof(float2));
     f((void**)&sys->key, np * sizeof(uint32_t));
     f((void**)&sys->rank, np * sizeof(uint32_t));
     f((void**)&sys->src, np * sizeof(uint32_t));
@@ -315,7 +316,7 @@ int system_alloc(mdg_system* sys) {
     MDG_CUDA(cudaMemsetAsync(sys->ncnt, 0, np * sizeof(uint32_t), st));
     MDG_CUDA(cudaMemsetAsync(sys->bc, 0, np, st));
     MDG_CUDA(cudaMemsetAsync(sys->Fp64, 0, (size_t)kMaxKinds * np * sizeof(double), st));
-    MDG_CUDA(cudaMemsetAsync(sys->trig32, 0, np * sizeof(float), st));
+    MDG_CUDA(cudaMemsetAsync(sys->trig32, 0, np * sizeof(float2), st));
     for (int a = 0; a < 3; ++a) MDG_CUDA(cudaMemsetAsync(sys->Rc[a], 0, np * sizeof(double), st));
     if (sys->n) {
         k_iota<<<nblk(sys->n), kBlock, 0, st>>>((int)sys->n, sys->u32[ORIG][0], sys->slot_of);

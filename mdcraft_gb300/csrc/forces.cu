@@ -523,7 +523,7 @@ FArgs force_args(mdg_system* sys) {
     for (int a = 0; a < 3; ++a) {
         A.L[a] = sys->dom.bmax[a] - sys->dom.bmin[a];
         A.periodic[a] = sys->dom.periodic[a] ? 1 : 0;
-        A.csf[a] = sys->grid.csf[a];
+        A.uf[a] = (float)(sys->grid.cs[a] / kOffUnits);
     }
     A.fx = sys->f64[FX][c];
     A.fy = sys->f64[FY][c];
@@ -535,7 +535,7 @@ FArgs force_args(mdg_system* sys) {
     A.Fp64 = sys->Fp64;
     A.Fp32 = sys->Fp32;
     A.pos32 = sys->pos32;
-    A.pos32b = reinterpret_cast<float4*>(sys->pos32 + sys->np);
+    A.pos32b = sys->pos32 + sys->np;
     A.Ep = sys->f64[EP][c];
     A.Em = sys->f64[EM][c];
     for (int k = 0; k < 9; ++k) A.V[k] = sys->f64[V0 + k][c];

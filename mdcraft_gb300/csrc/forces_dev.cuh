@@ -3,8 +3,9 @@
 // (solo.cu), so both give the same forces bit for bit.
 //
 // LJsCut::compute / EAM::charge and forces (mdcraft/solver/potential/
-// LJs-cut.cxx:22-131, EAM.cxx:141-601) in FP32 pair arithmetic on cell-centred
-// offsets, with compensated per-atom sums.
+// LJs-cut.cxx:22-131, EAM.cxx:141-601) in FP32 pair arithmetic on pair
+// vectors taken exactly from fixed-point cell-centred offsets, with
+// compensated per-atom sums.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -21,15 +22,15 @@ struct FArgs {
     const uint8_t* bc;
     double L[3];
     int periodic[3];
-    float csf[3];
+    float uf[3];  // length of one fixed-point offset unit per axis, cs / 2^29 in FP32
     // outputs / intermediate
     double *fx, *fy, *fz;
     float *gx, *gy, *gz;  // mixed forces
     double* nc;
     double* Fp64;
     float* Fp32;
-    const float4* pos32;
-    float4* pos32b;
+    const int4* pos32;  // fixed-point offsets (mdg_internal.cuh)
+    int4* pos32b;       // the same offsets with w = bits of the FP32 F'(rho) (EAM)
     double *Ep, *Em;
     double* V[9];
     DevStatus* st;
@@ -76,12 +77,14 @@ __device__ __forceinline__ float ksum_add(float& s, float& c, float v) {
     return s;
 }
 
-// Pair vector r_j - r_i of a list entry, from cell-centred offsets.
-__device__ __forceinline__ void pair_vec32(uint32_t e, const float4& pi, const float4& pj,
-                                           const float csf[3], float& dx, float& dy, float& dz) {
-    dx = (pj.x - pi.x) + image_shift(e, 0, csf[0]);
-    dy = (pj.y - pi.y) + image_shift(e, 1, csf[1]);
-    dz = (pj.z - pi.z) + image_shift(e, 2, csf[2]);
+// Pair vector r_j - r_i of a list entry from the fixed-point cell-centred
+// offsets: an exact integer difference (modulo 2^32; the true value is
+// within +-2^31 units), one rounding to FP32, one scaling by the unit.
+__device__ __forceinline__ void pair_vec32(uint32_t e, const int4& pi, const int4& pj, const float uf[3],
+                                           float& dx, float& dy, float& dz) {
+    dx = __int2float_rn((int)((uint32_t)pj.x - (uint32_t)pi.x + image_units(e, 0))) * uf[0];
+    dy = __int2float_rn((int)((uint32_t)pj.y - (uint32_t)pi.y + image_units(e, 1))) * uf[1];
+    dz = __int2float_rn((int)((uint32_t)pj.z - (uint32_t)pi.z + image_units(e, 2))) * uf[2];
 }
 
 // 1/sqrt(x) for x > 0: the hardware estimate refined by one Newton step, so
@@ -147,11 +150,11 @@ __device__ __forceinline__ bool pair_in(const FArgs& A, int i, uint32_t e, float
 template <bool MULTI, bool KICK = false>
 __device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
     if (A.tag[i] == 0) return;
-    const float4 pi = A.pos32[i];
+    const int4 pi = A.pos32[i];
     const int ng = A.ncnt[i] >> 2;
     const int ki = MULTI ? (A.kind[i] & 3) : 0;
     const bool per = ps->periodic;
-    const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
+    const float uf[3] = {A.uf[0], A.uf[1], A.uf[2]};
     const PotParams& P0 = ps->p[ki][0];
     float r2c = P0.r2cut_f, l1 = P0.lj1_f, l2 = P0.lj2_f, mh = P0.mhf_f;
     double R2c = P0.R2cut;
@@ -163,7 +166,7 @@ __device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __res
         const uint4 e4 = e4n;
         if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
         const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
-        float4 pj[4];
+        int4 pj[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32 + (e[q] & kJMask));
         float fx = 0.f, fy = 0.f, fz = 0.f;
@@ -174,7 +177,7 @@ __device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __res
                 r2c = P.r2cut_f; l1 = P.lj1_f; l2 = P.lj2_f; mh = P.mhf_f; R2c = P.R2cut;
             }
             float dx, dy, dz;
-            pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+            pair_vec32(e[q], pi, pj[q], uf, dx, dy, dz);
             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             bool in = pair_in(A, i, e[q], r2, r2c, R2c, per);
             float r2inv = __fdividef(1.0f, fmaxf(r2, 1e-12f));
@@ -232,11 +235,11 @@ __device__ __forceinline__ float analytic_ff32(const PotParams& P, float r2) {
 template <bool MULTI, int FORM, bool KICK = false>
 __device__ __forceinline__ void pair_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
     if (A.tag[i] == 0) return;
-    const float4 pi = A.pos32[i];
+    const int4 pi = A.pos32[i];
     const int ng = A.ncnt[i] >> 2;
     const int ki = MULTI ? (A.kind[i] & 3) : 0;
     const bool per = ps->periodic;
-    const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
+    const float uf[3] = {A.uf[0], A.uf[1], A.uf[2]};
     Kahan3 acc;
     const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
     uint4 e4n = ng > 0 ? __ldg(row) : make_uint4(0, 0, 0, 0);
@@ -244,7 +247,7 @@ __device__ __forceinline__ void pair_mixed_one(const FArgs& A, const PotSet* __r
         const uint4 e4 = e4n;
         if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
         const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
-        float4 pj[4];
+        int4 pj[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32 + (e[q] & kJMask));
         float fx = 0.f, fy = 0.f, fz = 0.f;
@@ -252,7 +255,7 @@ __device__ __forceinline__ void pair_mixed_one(const FArgs& A, const PotSet* __r
         for (int q = 0; q < 4; ++q) {
             const PotParams& P = ps->p[ki][MULTI ? (A.kind[e[q] & kJMask] & 3) : 0];
             float dx, dy, dz;
-            pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+            pair_vec32(e[q], pi, pj[q], uf, dx, dy, dz);
             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             bool in = pair_in(A, i, e[q], r2, P.r2cut_f, P.R2cut, per);
             float FF;
@@ -292,9 +295,9 @@ __device__ __forceinline__ void embed32(const PotParams& P, float rho, float* F,
 
 template <bool MULTI>
 __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
-    const float4 pi = A.pos32[i];
+    const int4 pi = A.pos32[i];
     const int ki = MULTI ? (A.kind[i] & 3) : 0;
-    const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
+    const float uf[3] = {A.uf[0], A.uf[1], A.uf[2]};
     const bool per = ps->periodic;
     float s = 0.f, c = 0.f;
     if (A.tag[i] != 0) {
@@ -311,7 +314,7 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
             const uint4 e4 = e4n;
             if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
             const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
-            float4 pj[4];
+            int4 pj[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32 + (e[q] & kJMask));
             float part = 0.f;
@@ -324,7 +327,7 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
                     eam = P->type == 2;
                 }
                 float dx, dy, dz;
-                pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+                pair_vec32(e[q], pi, pj[q], uf, dx, dy, dz);
                 float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                 bool in = eam && pair_in(A, i, e[q], r2, r2c, R2c, per);
                 float t = r2 * rsqrt_nr(fmaxf(r2, 1e-12f)) * idr;
@@ -349,16 +352,16 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
         if (b == 0) Fp0 = dF;
         if (MULTI) A.Fp32[(size_t)b * A.np + i] = dF;
     }
-    A.pos32b[i] = make_float4(pi.x, pi.y, pi.z, Fp0);
+    A.pos32b[i] = make_int4(pi.x, pi.y, pi.z, __float_as_int(Fp0));
 }
 
 template <bool MULTI, bool KICK = false>
 __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
     if (A.tag[i] == 0) return;
-    const float4 pi = A.pos32b[i];
+    const int4 pi = A.pos32b[i];
     const int ng = A.ncnt[i] >> 2;
     const int ki = MULTI ? (A.kind[i] & 3) : 0;
-    const float csf[3] = {A.csf[0], A.csf[1], A.csf[2]};
+    const float uf[3] = {A.uf[0], A.uf[1], A.uf[2]};
     const bool per = ps->periodic;
     const PotParams* P = &ps->p[ki][0];
     float r2c = P->r2cut_f, idr = P->inv_dr_f;
@@ -373,13 +376,13 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
         const uint4 e4 = e4n;
         if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
         const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
-        float4 pj[4];
+        int4 pj[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) pj[q] = __ldg(A.pos32b + (e[q] & kJMask));
         float fx = 0.f, fy = 0.f, fz = 0.f;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            float Fpi = pi.w, Fpj = pj[q].w;
+            float Fpi = __int_as_float(pi.w), Fpj = __int_as_float(pj[q].w);
             bool eam = true, lj = false;
             if (MULTI) {
                 uint32_t j = e[q] & kJMask;
@@ -394,7 +397,7 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
                 Fpi = A.Fp32[(size_t)kj * A.np + i];
             }
             float dx, dy, dz;
-            pair_vec32(e[q], pi, pj[q], csf, dx, dy, dz);
+            pair_vec32(e[q], pi, pj[q], uf, dx, dy, dz);
             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             bool in = (eam || lj) && pair_in(A, i, e[q], r2, r2c, R2c, per);
             // one reciprocal square root gives both r and 1/r

@@ -11,8 +11,8 @@
 //
 // Mixed form: FP64 positions and velocities, velocity increments computed in
 // FP32 from the FP32 forces, FP64 accumulation; the same pass refreshes the
-// FP32 cell-centred offsets used by the pair kernels and tests the half-skin
-// displacement on them.
+// fixed-point cell-centred offsets used by the pair kernels and runs the
+// half-skin test in FP64 on the new positions.
 #include <cuda_runtime.h>
 
 #include "mdg_host.h"
@@ -66,18 +66,19 @@ __global__ void k_kick_mixed(IArgs A) {
 
 // Half-skin threshold per atom for the mixed test (trig_one).
 __global__ void k_trig(int n, const double* __restrict__ saved_rns, const double* __restrict__ saved_rcut,
-                       float* __restrict__ trig) {
+                       const GridParams* __restrict__ gp, float2* __restrict__ trig) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) trig_one(i, saved_rns, saved_rcut, trig);
+    if (i < n) trig_one(i, saved_rns, saved_rcut, *gp, trig);
 }
 
-// Refresh of the FP32 offsets from FP64 positions (after uploads).
+// Refresh of the fixed-point offsets from FP64 positions (after uploads).
 __global__ void k_offsets(int n, const double* __restrict__ rx, const double* __restrict__ ry,
                           const double* __restrict__ rz, const double* __restrict__ Rx,
-                          const double* __restrict__ Ry, const double* __restrict__ Rz, float4* __restrict__ pos32) {
+                          const double* __restrict__ Ry, const double* __restrict__ Rz, double ux, double uy,
+                          double uz, int4* __restrict__ pos32) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    pos32[i] = make_float4((float)(rx[i] - Rx[i]), (float)(ry[i] - Ry[i]), (float)(rz[i] - Rz[i]), 0.0f);
+    pos32[i] = make_int4(off_encode(rx[i] - Rx[i], ux), off_encode(ry[i] - Ry[i], uy), off_encode(rz[i] - Rz[i], uz), 0);
 }
 
 // FP32 -> FP64 force copy after a mixed stage, so downloads and a later
@@ -223,7 +224,11 @@ IArgs integrator_args(mdg_system* sys, double dt) {
     }
     A.Rx = sys->Rc[0]; A.Ry = sys->Rc[1]; A.Rz = sys->Rc[2];
     A.pos32 = sys->pos32;
-    A.o0 = sys->o0;
+    A.q0 = sys->q0;
+    for (int a = 0; a < 3; ++a) {
+        A.inv_u[a] = sys->grid.inv_u[a];
+        A.uf[a] = (float)(sys->grid.cs[a] / kOffUnits);
+    }
     A.trig = sys->trig32;
     A.st = sys->dstat;
     return A;
@@ -263,7 +268,7 @@ int launch_kick(mdg_system* sys, double dt, int precision) {
 int launch_trig(mdg_system* sys) {
     if (sys->n == 0) return MDG_OK;
     k_trig<<<nblk(sys->n), kBlock, 0, sys->ctx->stream>>>((int)sys->n, sys->saved_rns, sys->saved_rcut,
-                                                          sys->trig32);
+                                                          sys->dgrid, sys->trig32);
     MDG_LAUNCHED(sys->ctx);
     return MDG_OK;
 }
@@ -273,7 +278,8 @@ int launch_offsets(mdg_system* sys) {
     int c = sys->cur;
     k_offsets<<<nblk(sys->n), kBlock, 0, sys->ctx->stream>>>((int)sys->n, sys->f64[RX][c], sys->f64[RY][c],
                                                              sys->f64[RZ][c], sys->Rc[0], sys->Rc[1], sys->Rc[2],
-                                                             sys->pos32);
+                                                             sys->grid.inv_u[0], sys->grid.inv_u[1],
+                                                             sys->grid.inv_u[2], sys->pos32);
     MDG_LAUNCHED(sys->ctx);
     return MDG_OK;
 }

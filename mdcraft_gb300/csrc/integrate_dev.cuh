@@ -33,9 +33,11 @@ struct IArgs {
     int periodic[3];
     // mixed
     const double *Rx, *Ry, *Rz;
-    float4* pos32;
-    const float4* o0;
-    const float* trig;
+    int4* pos32;
+    const int4* q0;      // fixed-point offsets at the last rebuild
+    double inv_u[3];     // fixed-point offset units per axis (GridParams::inv_u)
+    float uf[3];         // their lengths in FP32 (cs / 2^29)
+    const float2* trig;  // (skin/2)^2 of the last rebuild (-1 when skin <= 0) and its band (trig_one)
     DevStatus* st;
 };
 
@@ -91,30 +93,45 @@ __device__ __forceinline__ bool drift64_one(const IArgs& A, int i, int drift, in
     return need;
 }
 
-// Mixed form: kick + drift, cell-offset refresh, half-skin test.
+// Mixed form: kick + drift, cell-offset refresh, and the half-skin test of
+// VerletList::decide (verlet-list.cxx:135-154) with the FP64 result: the
+// displacement since the rebuild is first taken from the fixed-point offsets
+// (q - q0, exact up to one offset unit per axis) in FP32; only an atom whose
+// estimate lies within the proven error band around (skin/2)^2 (trig_one;
+// about 1e-5 of it) is tested again with the reference's FP64 arithmetic, so
+// every decision equals decide_one's on the same positions. (The size, uid,
+// rcut and rns comparisons of decide cannot change inside the step loop: the
+// drift does not touch those fields, and a host-side change marks the list
+// stale.)
 __device__ __forceinline__ bool drift_mixed_one(const IArgs& A, int i) {
-    bool need = false;
-    {
-        double r[3] = {A.rx[i], A.ry[i], A.rz[i]};
-        if (A.tag[i] != 0) {
-            float hm = (0.5f * (float)A.dt) * __frcp_rn((float)A.m[i]);
-            float g[3] = {A.gx[i], A.gy[i], A.gz[i]};
-            double* v[3] = {A.vx, A.vy, A.vz};
-            for (int k = 0; k < 3; ++k) {
-                double vk = v[k][i] + (double)(g[k] * hm);
-                v[k][i] = vk;
-                r[k] = fma(vk, A.dt, r[k]);
-            }
-            A.rx[i] = r[0]; A.ry[i] = r[1]; A.rz[i] = r[2];
+    double r[3] = {A.rx[i], A.ry[i], A.rz[i]};
+    if (A.tag[i] != 0) {
+        float hm = (0.5f * (float)A.dt) * __frcp_rn((float)A.m[i]);
+        float g[3] = {A.gx[i], A.gy[i], A.gz[i]};
+        double* v[3] = {A.vx, A.vy, A.vz};
+        for (int k = 0; k < 3; ++k) {
+            double vk = v[k][i] + (double)(g[k] * hm);
+            v[k][i] = vk;
+            r[k] = fma(vk, A.dt, r[k]);
         }
-        float o[3] = {(float)(r[0] - A.Rx[i]), (float)(r[1] - A.Ry[i]), (float)(r[2] - A.Rz[i])};
-        A.pos32[i] = make_float4(o[0], o[1], o[2], 0.0f);
-        float4 q = A.o0[i];
-        float dx = o[0] - q.x, dy = o[1] - q.y, dz = o[2] - q.z;
-        float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        need = d2 > A.trig[i];
+        A.rx[i] = r[0]; A.ry[i] = r[1]; A.rz[i] = r[2];
     }
-    return need;
+    const int4 q = make_int4(off_encode(r[0] - A.Rx[i], A.inv_u[0]), off_encode(r[1] - A.Ry[i], A.inv_u[1]),
+                             off_encode(r[2] - A.Rz[i], A.inv_u[2]), 0);
+    A.pos32[i] = q;
+    const int4 p = A.q0[i];
+    const float dx = __int2float_rn((int)((uint32_t)q.x - (uint32_t)p.x)) * A.uf[0];
+    const float dy = __int2float_rn((int)((uint32_t)q.y - (uint32_t)p.y)) * A.uf[1];
+    const float dz = __int2float_rn((int)((uint32_t)q.z - (uint32_t)p.z)) * A.uf[2];
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float2 tb = A.trig[i];
+    if (d2 > tb.x + tb.y) return true;
+    if (d2 < tb.x - tb.y) return false;
+    double skin = dsub(A.saved_rns[i], A.saved_rcut[i]);
+    double ex = shortest1(dsub(r[0], A.r0x[i]), A.L[0], A.periodic[0]);
+    double ey = shortest1(dsub(r[1], A.r0y[i]), A.L[1], A.periodic[1]);
+    double ez = shortest1(dsub(r[2], A.r0z[i]), A.L[2], A.periodic[2]);
+    return skin <= 0.0 || sq3_exact(ex, ey, ez) > dmul(dmul(0.25, skin), skin);
 }
 
 __device__ __forceinline__ void kick_mixed_one(const IArgs& A, int i) {
@@ -125,12 +142,24 @@ __device__ __forceinline__ void kick_mixed_one(const IArgs& A, int i) {
     A.vz[i] += (double)(A.gz[i] * hm);
 }
 
-// Half-skin threshold per atom for the mixed test: (skin/2)^2 shrunk by
-// 1e-6 so that FP32 rounding can only trigger a rebuild early.
+// Half-skin threshold per atom for the mixed form's test: (0.25 skin) skin
+// as decide_one computes it (-1, always rebuild, when skin <= 0), and the
+// band within which the FP32 estimate of drift_mixed_one cannot decide. Its
+// error is at most sqrt(3) u per axis from the offset quantisation (u the
+// largest offset unit), i.e. 2 sqrt(3) |d| u + 3 u^2 in d^2, plus ~1e-6
+// relative from the FP32 arithmetic; the band, 1e-5 of the threshold +
+// 4 sqrt(threshold) u + 4 u^2, covers both.
 __device__ __forceinline__ void trig_one(int i, const double* __restrict__ saved_rns,
-                                         const double* __restrict__ saved_rcut, float* __restrict__ trig) {
-    double skin = saved_rns[i] - saved_rcut[i];
-    trig[i] = skin <= 0.0 ? -1.0f : (float)(0.25 * skin * skin * (1.0 - 1e-6));
+                                         const double* __restrict__ saved_rcut, const GridParams& g,
+                                         float2* __restrict__ trig) {
+    double skin = dsub(saved_rns[i], saved_rcut[i]);
+    if (skin <= 0.0) {
+        trig[i] = make_float2(-1.0f, 0.0f);
+        return;
+    }
+    double t = dmul(dmul(0.25, skin), skin);
+    double u = fmax(g.cs[0], fmax(g.cs[1], g.cs[2])) / kOffUnits;
+    trig[i] = make_float2((float)t, (float)(1e-5 * t + 4.0 * sqrt(t) * u + 4.0 * u * u));
 }
 
 }  // namespace mdg

@@ -119,8 +119,9 @@ struct mdg_system {
     // rebuilt per list build (slot order)
     double* Rc[3] = {};        // cell centres
     uint32_t* cellp = nullptr; // packed local cell coordinates
-    float4* pos32 = nullptr;   // offsets from the cell centre + w (EAM F')
-    float4* o0 = nullptr;      // offsets at the rebuild (skin test, mixed form)
+    int4* pos32 = nullptr;     // fixed-point offsets from the cell centre + w (EAM F' bits); 2 x np
+    int4* q0 = nullptr;        // fixed-point offsets at the rebuild (mixed rebuild test)
+    float4* o0 = nullptr;      // FP32 offsets at the rebuild (list build prefilter)
     double* r0[3] = {};        // positions at the rebuild (skin test, FP64 form)
     double* saved_rcut = nullptr;
     double* saved_rns = nullptr;
@@ -129,7 +130,7 @@ struct mdg_system {
     uint8_t* bc = nullptr;        // Periodic boundary flag
     double* Fp64 = nullptr;       // F'(nc) per kind column [nk][np] (FP64 form)
     float* Fp32 = nullptr;        // F'(rho) per kind column [nk][np] (mixed Multi)
-    float* trig32 = nullptr;      // (skin/2)^2 per atom for the mixed half-skin test
+    float2* trig32 = nullptr;     // (skin/2)^2 per atom (-1: skin <= 0) and its exactness band (mixed rebuild test)
     int force_prec = MDG_PREC_FP64;  // arithmetic of the forces last computed
     int fp_ok = 0;                   // Fp64 = F'(nc) of the current nc (set by the FP64 density pass)
     // Measurement outputs a step's prepare clears (Pair::prepare_one) and

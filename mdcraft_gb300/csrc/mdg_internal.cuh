@@ -4,8 +4,10 @@
 //   FP64 SoA  rx ry rz | vx vy vz | fx fy fz (FP64 forces) | m rcut rns
 //             Rx Ry Rz (FP64 centre of the atom's cell at the last rebuild)
 //             Ep Em nc, V[9][n] (per-atom measurement outputs)
-//   FP32      f32[3][n] (mixed forces), pos32 float4 {x,y,z offset from the
-//             cell centre, w = EAM F'(rho)}, o0 float4 (offsets at rebuild)
+//   FP32      f32[3][n] (mixed forces), o0 float4 (FP32 offsets from the
+//             cell centre at the rebuild, read by the list build)
+//   fixed     pos32 int4 {x,y,z offset from the cell centre in units of
+//             cs / 2^29 per axis, w = bits of the FP32 EAM F'(rho)}
 //   ints      orig (slot -> caller index), uid, kind (u16), tag (u16),
 //             cell (packed local cell coordinates)
 //   list      ELL: nbr[k * np + i] (k < K), ncnt[i]; entry = j | image << 25
@@ -55,7 +57,21 @@ struct GridParams {
     double max_rns;
     float csf[3];
     float Lf[3];
+    double inv_u[3];   // 2^29 / cs: FP64 offset -> fixed-point units (pos32)
 };
+
+// Fixed-point cell offsets of the mixed form. An offset from the atom's cell
+// centre is stored as an integer number of units u = cs / 2^29 per axis
+// (range +-4 cells), so the pair vector r_j - r_i = (o_j - o_i) + image
+// cells * 2^29 is an exact integer: the only rounding is its conversion to
+// FP32, and pairs related by inversion symmetry get exactly opposite vectors.
+// (Differences of independently rounded FP32 offsets break that symmetry:
+// on a perfect lattice they left forces that should cancel at ~1e-5 of the
+// RMS force.)
+constexpr int kOffBits = 29;
+constexpr double kOffUnits = 536870912.0;  // 2^29
+
+__device__ __forceinline__ int off_encode(double d, double inv_u) { return __double2int_rn(d * inv_u); }
 
 // Bricked-Morton bin key of a local cell: 4x4x4 bricks in x-fastest order,
 // Morton order inside a brick.
@@ -86,10 +102,11 @@ __host__ __device__ inline size_t nidx(int k, size_t i, size_t np) {
 }
 constexpr uint32_t kSelfCode = 0x15u << kJBits;  // image (0,0,0)
 
-// Image offset encoded in a list entry (2 bits per axis, value+1).
-__device__ inline float image_shift(uint32_t e, int axis, float cs) {
-    int b = (int)((e >> (kJBits + 2 * axis)) & 3u);  // 0, 1, 2 for -1, 0, +1 cells
-    return __int2float_rn(b - 1) * cs;
+// Image offset encoded in a list entry (2 bits per axis, value+1), in
+// fixed-point offset units (-2^29, 0, 2^29; modulo 2^32).
+__device__ inline uint32_t image_units(uint32_t e, int axis) {
+    uint32_t b = (e >> (kJBits + 2 * axis)) & 3u;  // 0, 1, 2 for -1, 0, +1 cells
+    return (b - 1u) << kOffBits;
 }
 
 // Potential types: LJsCut and the tabulated Pair are the reference's

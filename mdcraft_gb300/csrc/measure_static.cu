@@ -19,8 +19,14 @@
 //    order such calls on one stream. Each call writes every partial it reads,
 //    so nothing has to be cleared between calls.
 //  - The first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current) and caches it; make
-//    that first call before any stream capture.
+//    cudaGetSymbolAddress (with that device current) and caches it. With
+//    lazy module loading (the CUDA default) that lookup also loads this
+//    module on the device, which creates the array and can synchronise:
+//    make the first call on each device at set-up, as a warm-up, before any
+//    stream capture and outside any loop that must not wait.
+//  - An error already pending on the calling thread (from an earlier CUDA
+//    call) is reported as such before anything is launched; errors of this
+//    call's own launches are reported after them.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -38,6 +44,7 @@ constexpr size_t kStaticBytes = ((size_t)kStaticParts * kStaticSlots + 16) * siz
 
 // partials [kStaticParts][8], then 16 doubles: totals and the COM velocity
 static __device__ __align__(256) double g_measure_scratch[(size_t)kStaticParts * kStaticSlots + 16];
+static_assert(sizeof(g_measure_scratch) == kStaticBytes, "static scratch size (262,272 bytes per device)");
 
 struct StaticMeasureArgs {
     size_t n;
@@ -165,6 +172,8 @@ extern "C" int mdg_measure_static(const double* d_m, const double* d_v, const do
     double* scratch = static_scratch_ptr(device, &rc);
     if (!scratch) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    e = cudaPeekAtLastError();
+    if (e != cudaSuccess) return cuda_status(e, "mdg_measure_static: error pending from an earlier CUDA call");
     StaticMeasureArgs A;
     A.n = n;
     A.m = d_m;

@@ -217,12 +217,12 @@ __global__ void k_copy(int n, GatherSet<NF, T> gs, const GridParams* __restrict_
 __global__ void k_cells(int n, const double* __restrict__ rx, const double* __restrict__ ry,
                         const double* __restrict__ rz, const GridParams* __restrict__ gp,
                         uint32_t* __restrict__ cellp, double* __restrict__ Rx, double* __restrict__ Ry,
-                        double* __restrict__ Rz, float4* __restrict__ pos32, float4* __restrict__ o0,
+                        double* __restrict__ Rz, int4* __restrict__ pos32, int4* __restrict__ q0, float4* __restrict__ o0,
                         const uint32_t* __restrict__ orig, uint32_t* __restrict__ slot_of) {
     const GridParams g = *gp;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || g.empty) return;
-    cells_one(g, i, rx, ry, rz, cellp, Rx, Ry, Rz, pos32, o0, orig, slot_of);
+    cells_one(g, i, rx, ry, rz, cellp, Rx, Ry, Rz, pos32, q0, o0, orig, slot_of);
 }
 
 // ---------------------------------------------------------------------------
@@ -637,7 +637,7 @@ int nlist_enqueue(mdg_system* sys) {
     if (n == 0) return MDG_OK;
     int nparts = nparts_of(sys);
     DomainDev d = domain_dev(sys);
-    const int c = sys->cur, alt = c ^ 1;
+    const int c = sys->cur;
     MDG_CUDA(cudaMemsetAsync(&sys->dstat->max_count, 0, 3 * sizeof(uint32_t), st));  // max_count, nonuniform, build_flags
     k_wrap_bounds<<<nparts, kBlock, 0, st>>>(n, sys->f64[RX][c], sys->f64[RY][c], sys->f64[RZ][c],
                                              sys->f64[RNS][c], d, sys->part);
@@ -692,7 +692,7 @@ int nlist_enqueue(mdg_system* sys) {
         MDG_LAUNCHED(ctx);
     }
     k_cells<<<nblk(n), kBlock, 0, st>>>(n, sys->f64[RX][c], sys->f64[RY][c], sys->f64[RZ][c], sys->dgrid,
-                                        sys->cellp, sys->Rc[0], sys->Rc[1], sys->Rc[2], sys->pos32, sys->o0,
+                                        sys->cellp, sys->Rc[0], sys->Rc[1], sys->Rc[2], sys->pos32, sys->q0, sys->o0,
                                         sys->u32[ORIG][c], sys->slot_of);
     MDG_LAUNCHED(ctx);
     NbArgs A = nb_args(sys);
@@ -851,12 +851,6 @@ int nlist_export_entries(mdg_system* sys, const std::vector<uint64_t>& off, uint
 }
 
 int launch_trig(mdg_system* sys);
-
-// VerletList::updateint launch_trig(mdg_system* sys);
-
-// VerletList::updateint launch_trig(mdg_system* sys);
-
-// VerletList::updateint launch_trig(mdg_system* sys);
 
 // VerletList::update (verlet-list.cxx:41-55) for the API: enqueue, wait,
 // and rebuild again with larger capacities when the grid or a list outgrew

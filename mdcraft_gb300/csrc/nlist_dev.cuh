@@ -71,6 +71,7 @@ __host__ __device__ inline void grid_from_bounds(const DomainDev& d, const doubl
         g.bricks[i] = (g.num[i] + 3) / 4;
         g.csf[i] = (float)g.cs[i];
         g.Lf[i] = (float)d.size[i];
+        g.inv_u[i] = g.cs[i] > 0.0 ? kOffUnits / g.cs[i] : 0.0;
         if (d.periodic[i] && i < d.dim &&
             (g.dom_n[i] <= 3 || g.offset[i] != 0 || g.num[i] != g.dom_n[i]))
             g.small_box = 1;
@@ -177,7 +178,8 @@ __device__ __forceinline__ void bin_sort_one(int b, const uint32_t* start, uint3
 // Cell centre, cell-relative FP32 offsets and packed cell of atom i.
 __device__ __forceinline__ void cells_one(const GridParams& g, int i, const double* rx, const double* ry,
                                           const double* rz, uint32_t* cellp, double* Rx, double* Ry, double* Rz,
-                                          float4* pos32, float4* o0, const uint32_t* orig, uint32_t* slot_of) {
+                                          int4* pos32, int4* q0, float4* o0, const uint32_t* orig,
+                                          uint32_t* slot_of) {
     double r[3] = {rx[i], ry[i], rz[i]};
     int c[3];
     bool cl;
@@ -185,18 +187,20 @@ __device__ __forceinline__ void cells_one(const GridParams& g, int i, const doub
     cellp[i] = pack_cell(c[0], c[1], c[2]);
     double R[3];
     float o[3];
+    int q[3];
     bool outlier = cl;
     for (int a = 0; a < 3; ++a) {
         R[a] = g.gmin[a] + ((double)c[a] + 0.5) * g.cs[a];
         if (a >= g.dim) R[a] = r[a];
         o[a] = (float)(r[a] - R[a]);
+        q[a] = off_encode(r[a] - R[a], g.inv_u[a]);
         if (fabsf(o[a]) > 0.75f * g.csf[a] && a < g.dim) outlier = true;
     }
     Rx[i] = R[0];
     Ry[i] = R[1];
     Rz[i] = R[2];
-    float4 p = make_float4(o[0], o[1], o[2], 0.0f);
-    pos32[i] = p;
+    pos32[i] = make_int4(q[0], q[1], q[2], 0);
+    q0[i] = make_int4(q[0], q[1], q[2], 0);
     o0[i] = make_float4(o[0], o[1], o[2], outlier ? 1.0f : 0.0f);
     slot_of[orig[i]] = (uint32_t)i;
 }
@@ -443,7 +447,6 @@ __device__ __forceinline__ void nbuild_cell_warp(const NbArgs& A, const GridPara
     if (lane == 0) S.cpre[nc] = T;
     __syncwarp();
 
-    const unsigned lt = (1u << lane) - 1u;
     for (uint32_t base = s0; base < s1; base += 32) {
         const uint32_t ni = s1 - base < 32u ? s1 - base : 32u;
         const bool act = (uint32_t)lane < ni;

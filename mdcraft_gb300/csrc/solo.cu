@@ -48,10 +48,11 @@ struct alignas(16) SoloArgs {
     const uint32_t* orig;
     uint32_t* cellp;
     double *Rx, *Ry, *Rz;
-    float4 *pos32, *o0;
+    int4 *pos32, *q0;
+    float4* o0;
     uint32_t* slot_of;
     const double *saved_rns, *saved_rcut;
-    float* trig;
+    float2* trig;
     GridParams* dgrid;
     long long bin_cap;
     DevStatus* st;
@@ -189,7 +190,7 @@ __device__ __noinline__ bool solo_rebuild(const SoloArgs& S, GridParams& g, doub
     copy_back_block<NT>(S.G, n);
     __syncthreads();
     for (int i = t; i < n; i += NT)
-        cells_one(g, i, S.rx, S.ry, S.rz, S.cellp, S.Rx, S.Ry, S.Rz, S.pos32, S.o0, S.orig, S.slot_of);
+        cells_one(g, i, S.rx, S.ry, S.rz, S.cellp, S.Rx, S.Ry, S.Rz, S.pos32, S.q0, S.o0, S.orig, S.slot_of);
     __syncthreads();
     {
         const bool uniform = S.st->nonuniform == 0;
@@ -207,7 +208,7 @@ __device__ __noinline__ bool solo_rebuild(const SoloArgs& S, GridParams& g, doub
         }
     }
     __syncthreads();
-    for (int i = t; i < n; i += NT) trig_one(i, S.saved_rns, S.saved_rcut, S.trig);
+    for (int i = t; i < n; i += NT) trig_one(i, S.saved_rns, S.saved_rcut, g, S.trig);
     __syncthreads();
     bool ok = !(S.st->build_flags & FLAG_OVERFLOW);
     __syncthreads();
@@ -281,7 +282,7 @@ __device__ __noinline__ bool solo_setup(const SoloArgs& S, GridParams& g, double
         S.slot_of[k] = (uint32_t)k;
         S.N.ncnt[k] = 0;
         S.bc[k] = 0;
-        S.trig[k] = 0.0f;
+        S.trig[k] = make_float2(0.0f, 0.0f);
         S.Rx[k] = 0.0;
         S.Ry[k] = 0.0;
         S.Rz[k] = 0.0;
@@ -295,8 +296,8 @@ __device__ __noinline__ bool solo_setup(const SoloArgs& S, GridParams& g, double
     __syncthreads();
     if (!solo_rebuild<NT>(S, g, red, scan_sh)) return false;
     for (int i = t; i < n; i += NT)
-        S.pos32[i] = make_float4((float)(S.rx[i] - S.Rx[i]), (float)(S.ry[i] - S.Ry[i]),
-                                 (float)(S.rz[i] - S.Rz[i]), 0.0f);
+        S.pos32[i] = make_int4(off_encode(S.rx[i] - S.Rx[i], g.inv_u[0]), off_encode(S.ry[i] - S.Ry[i], g.inv_u[1]),
+                               off_encode(S.rz[i] - S.Rz[i], g.inv_u[2]), 0);
     for (int i = t; i < n; i += NT) solo_zero_one(S, i);
     __syncthreads();
     for (int i = t; i < n; i += NT) drift64_one(S.I, i, 0, 0);
@@ -475,6 +476,7 @@ void solo_fill(void* args, mdg_system* sys, const PotSet* dps, int any_eam, doub
     S.Ry = sys->Rc[1];
     S.Rz = sys->Rc[2];
     S.pos32 = sys->pos32;
+    S.q0 = sys->q0;
     S.o0 = sys->o0;
     S.slot_of = sys->slot_of;
     S.saved_rns = sys->saved_rns;

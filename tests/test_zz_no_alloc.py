@@ -51,14 +51,61 @@ def test_measure_static_matches_measure_on_two_calls():
     stream = torch.cuda.current_stream(dev).cuda_stream
     fn = _entry()
     want = [ref["Ep"], ref["Em"], ref["KE"], ref["Etot"], ref["virial"]]
-    for _ in range(2):
+    free0 = None
+    for call in range(2):
         out.fill_(float("nan"))
+        torch.cuda.synchronize(dev)
+        if call == 1:
+            free0 = torch.cuda.mem_get_info(dev)[0]
         rc = fn(m.data_ptr(), v.data_ptr(), Ep.data_ptr(), Em.data_ptr(), V.data_ptr(), n, out.data_ptr(), stream)
         assert rc == 0
         torch.cuda.synchronize(dev)
+        if call == 1:
+            # nothing was allocated on the device by the second call
+            assert torch.cuda.mem_get_info(dev)[0] >= free0
         o = out.cpu().numpy()
         assert o[:5] == pytest.approx(want, rel=REL)
         assert np.abs(o[5:8] - ref["vcom"]).max() <= 1e-12
+
+
+def _reference(m, v, Ep, Em, V):
+    """The same totals in numpy FP64."""
+    tm = m.sum()
+    vcom = (m[:, None] * v).sum(axis=0) / tm if tm > 0 else np.zeros(3)
+    ke = 0.5 * (m * ((v - vcom) ** 2).sum(axis=1)).sum()
+    return np.array([Ep.sum(), Em.sum(), ke, Ep.sum() + Em.sum() + ke, (V[:, 0] + V[:, 4] + V[:, 8]).sum(),
+                     *vcom])
+
+
+@pytest.mark.parametrize("n", [0, 8_388_608], ids=["empty", "max_atoms"])
+def test_measure_static_edge_sizes(n):
+    """No atoms (all totals zero) and the largest accepted input (every one
+    of the 4096 partials in use), against a numpy FP64 reduction."""
+    import torch
+
+    rng = np.random.default_rng(17)
+    m = rng.uniform(1.0, 60.0, n)
+    v = rng.standard_normal((n, 3))
+    Ep = rng.standard_normal(n)
+    Em = -rng.uniform(0.5, 2.0, n)
+    V = rng.standard_normal((n, 9))
+    dev = torch.device("cuda", 0)
+    td = lambda x: torch.tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa: E731
+    tm, tv, tEp, tEm, tV = td(m), td(v.T), td(Ep), td(Em), td(V.T)
+    out = torch.full((8,), float("nan"), dtype=torch.float64, device=dev)
+    fn = _entry()
+    rc = fn(tm.data_ptr(), tv.data_ptr(), tEp.data_ptr(), tEm.data_ptr(), tV.data_ptr(), n, out.data_ptr(),
+            torch.cuda.current_stream(dev).cuda_stream)
+    assert rc == 0
+    torch.cuda.synchronize(dev)
+    o = out.cpu().numpy()
+    want = _reference(m, v, Ep, Em, V)
+    if n == 0:
+        assert np.array_equal(o, np.zeros(8))
+    else:
+        scale = np.array([np.abs(Ep).sum(), np.abs(Em).sum(), want[2], np.abs(want[3]) + want[2],
+                          np.abs(V).sum(), 1.0, 1.0, 1.0])
+        assert np.all(np.abs(o - want) <= REL * scale)
 
 
 def test_measure_static_rejects_oversize():
