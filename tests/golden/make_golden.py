@@ -12,7 +12,7 @@ The files are byte-identical copies, xz-compressed, so the tests parse them
 exactly as the reference's loaders do. The golden VALUES the tests check are
 the constants asserted in those reference test files (cited in the tests).
 
-usage: python tests/golden/make_golden.py [/path/to/reference]
+usage: python tests/golden/make_golden.py /path/to/reference
 """
 import lzma
 import os
@@ -35,4 +35,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/reference")
+    main(sys.argv[1])
