@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--serve-block-threads", type=int, default=0,
                     help="threads of the fused per-system block (256, 512, 1024; 0: chosen by the autotuner "
                          "on a sample of the stream; -1: a graph loop per request)")
+    ap.add_argument("--serve-order", default="fifo", choices=["fifo", "largest"],
+                    help="admission order of waiting requests in the serving stream")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="only the serving stream (prints its summary)")
     ap.add_argument("--config", default="", choices=["", "lj_argon", "nial", "lj_liquid", "nve_drift"],
@@ -241,7 +243,8 @@ def run_serving(args, device):
         from mdcraft_gb300 import tune
         threads, tuning = tune.tune_serving(specs, solv, device=device, slots=args.serve_slots)
     reqs = SV.prepare(specs)
-    srv = mdg.Server(device=device, slots=args.serve_slots, max_atoms=32768, block_threads=threads)
+    srv = mdg.Server(device=device, slots=args.serve_slots, max_atoms=32768, block_threads=threads,
+                     order=args.serve_order)
     # warm-up: one request of each kind (pool pages, potential tables)
     for kind in ("lj", "eam"):
         s = next(x for x in specs if x["kind"] == kind)
@@ -257,6 +260,7 @@ def run_serving(args, device):
     st = srv.stats()
     srv.close()
     summary.update({"workload": SERVE_WORKLOAD, "slots": args.serve_slots, "steps_per_request": args.serve_steps,
+                    "order": args.serve_order,
                     "block_threads": threads,
                     "tuning": ({str(k): v for k, v in tuning.items()} if tuning else "given"),
                     "arrival_rate_per_s": 2000.0, "budget_bytes": st["budget"], "peak_bytes": st["peak"],

@@ -344,7 +344,13 @@ typedef struct mdg_server_config {
     int block_threads;  /* fused one-block loop per system (mixed precision, one kind,
                            <= 65536 atoms): its threads (256, 512, 1024), 0 = the default
                            (1024), -1 = off (a graph loop per request instead) */
+    int order;          /* admission order of waiting requests: MDG_ORDER_FIFO (0, the
+                           default) or MDG_ORDER_LARGEST (most atom-steps first, which
+                           shortens the tail of a backlog at the cost of small requests'
+                           latency) */
 } mdg_server_config;
+#define MDG_ORDER_FIFO 0
+#define MDG_ORDER_LARGEST 1
 
 typedef struct mdg_request_info {
     int status;         /* MDG_OK or the error that ended the request */
@@ -354,6 +360,10 @@ typedef struct mdg_request_info {
     double t_done;
     uint64_t rebuilds;  /* list rebuilds during the run */
     size_t footprint;   /* device bytes the request held */
+    double service_s;   /* time the request ran, without its queueing: for a fused
+                           one-block run, from the block's start on it to its
+                           completion record (GPU clock); for a graph loop, from
+                           its admission to completion (server clock) */
 } mdg_request_info;
 
 typedef struct mdg_server_stats {
@@ -366,6 +376,12 @@ typedef struct mdg_server_stats {
     double host_retire_s; /* host seconds spent retiring (result copy, release) */
     uint64_t rechecked;   /* requests repeated on the checked path (first list outgrew its sizing) */
     double host_detail_s[4]; /* of retiring: run bookkeeping, result gather, graph release, memory release */
+    size_t live_blocks;   /* blocks of the fused loop's kernel alive now, over all its launches in
+                             flight (running, waiting for a request, or launched and not yet resident) */
+    size_t busy_blocks;   /* of which running a request */
+    size_t block_slots;   /* requests published to the fused loop and not yet finished */
+    size_t alloc_slots;   /* requests admitted whose buffers are still being allocated */
+    uint64_t kernel_launches; /* launches of the fused loop's kernel so far */
 } mdg_server_stats;
 
 int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out);

@@ -635,19 +635,22 @@ class Verlet:
 
 class _ServerConfig(C.Structure):
     _fields_ = [("slots", C.c_int), ("hbm_budget", C.c_size_t), ("max_atoms", C.c_size_t),
-                ("block_threads", C.c_int)]
+                ("block_threads", C.c_int), ("order", C.c_int)]
 
 
 class _RequestInfo(C.Structure):
     _fields_ = [("status", C.c_int), ("done", C.c_int), ("t_submit", C.c_double), ("t_admit", C.c_double),
-                ("t_done", C.c_double), ("rebuilds", C.c_uint64), ("footprint", C.c_size_t)]
+                ("t_done", C.c_double), ("rebuilds", C.c_uint64), ("footprint", C.c_size_t),
+                ("service_s", C.c_double)]
 
 
 class _ServerStats(C.Structure):
     _fields_ = [("budget", C.c_size_t), ("used", C.c_size_t), ("peak", C.c_size_t), ("queued", C.c_size_t),
                 ("running", C.c_size_t), ("finished", C.c_size_t), ("admitted", C.c_uint64),
                 ("launches", C.c_uint64), ("host_admit_s", C.c_double), ("host_graph_s", C.c_double),
-                ("host_retire_s", C.c_double), ("rechecked", C.c_uint64), ("host_detail_s", C.c_double * 4)]
+                ("host_retire_s", C.c_double), ("rechecked", C.c_uint64), ("host_detail_s", C.c_double * 4),
+                ("live_blocks", C.c_size_t), ("busy_blocks", C.c_size_t), ("block_slots", C.c_size_t),
+                ("alloc_slots", C.c_size_t), ("kernel_launches", C.c_uint64)]
 
 
 class Server:
@@ -656,14 +659,19 @@ class Server:
     Each request is a whole driver loop (``steps`` velocity-Verlet steps with
     the list rebuilt on decide()) over its own atoms, domain and solver. Up to
     ``slots`` requests run at once, each on its own stream, admitted in FIFO
-    order as slots and device memory (``hbm_budget`` bytes) free up.
+    order (or largest first) as slots and device memory (``hbm_budget``
+    bytes) free up.
     """
 
+    ORDERS = {"fifo": 0, "largest": 1}
+
     def __init__(self, device: int = 0, slots: int = 16, hbm_budget: int = 0, max_atoms: int = 1 << 16,
-                 block_threads: int = 0):
+                 block_threads: int = 0, order: str = "fifo"):
         """block_threads: threads of the fused per-request block (256, 512, 1024; 0 = 1024);
-        -1 runs every request as a graph loop on its slot's stream instead."""
-        cfg = _ServerConfig(slots, hbm_budget, max_atoms, block_threads)
+        -1 runs every request as a graph loop on its slot's stream instead. order: "fifo"
+        admits waiting requests in arrival order, "largest" the one with the most
+        atom-steps first."""
+        cfg = _ServerConfig(slots, hbm_budget, max_atoms, block_threads, self.ORDERS[order])
         h = C.c_void_p()
         _check(lib().mdg_server_create(device, C.byref(cfg), C.byref(h)))
         self.h = h

@@ -255,12 +255,19 @@ int nlist_capacity_host(mdg_system* sys, const mdg_atom* atoms, size_t n, int ha
 // one request per block of a persistent kernel fed through a queue.
 constexpr int kSoloRing = 4096;
 constexpr int kSoloMaxBlocks = 4096;
+// Launches of the persistent kernel that may be in flight at once: a new
+// launch tops the kernel up when blocks have exited while others still run
+// requests, so its slot must be one whose earlier launch has ended.
+constexpr int kSoloGens = 4;
 struct SoloQueue {              // host-mapped
     volatile uint32_t tail;     // entries published
     volatile uint32_t stop;     // 1: blocks exit when they find no entry
     uint32_t pad[14];
     int ring[kSoloRing];        // argument-record index of each entry
-    volatile uint32_t live[2][kSoloMaxBlocks];  // per launch generation: block running
+    // per launch slot and block: 0 exited (or not launched), 1 launched and
+    // waiting for an entry (set by the host before the launch, so blocks not
+    // yet resident count), 2 running a request
+    volatile uint32_t live[kSoloGens][kSoloMaxBlocks];
 };
 int solo_eligible(const mdg_solver* s, const mdg_system* sys);
 size_t solo_args_bytes();
@@ -273,7 +280,8 @@ size_t solo_out_bytes();
 // memory; in and out may be the same buffer).
 void solo_fill(void* args, mdg_system* sys, const PotSet* dps, int any_eam, double pot_rcut, int periodic,
                double dt, long steps, const void* atoms_in_dev, void* out_dev, void* atoms_out_dev, uint32_t seq);
-int solo_out_read(const void* out_host, uint32_t* done, unsigned long long* left, DevStatus* st);
+int solo_out_read(const void* out_host, uint32_t* done, unsigned long long* left, DevStatus* st,
+                  double* service_s = nullptr);
 int solo_persistent_launch(cudaStream_t stream, int threads, int blocks, const void* desc_dev, SoloQueue* q_dev,
                            uint32_t* head, int idle_limit, int gen);
 int solo_blocks_per_sm(int threads, int* blocks);

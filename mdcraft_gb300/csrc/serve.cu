@@ -18,8 +18,9 @@
 // that arrive while others run start as soon as a block is free. Each
 // block writes its result atoms and a completion record into host-mapped
 // memory; the host polls those and never waits for the device. Idle blocks
-// exit after a bounded wait; the host relaunches the kernel when work is
-// queued and no block is left.
+// exit after a bounded wait; the host tops the kernel up with a further
+// launch (up to kSoloGens in flight) whenever fewer blocks are alive than
+// the GPU holds and requests wait.
 //
 // Graph mode (everything else, or when block mode is off): the request's
 // system gets the slot's own stream; set-up and the loop (one graph launch)
@@ -58,6 +59,7 @@ struct Request {
     int precision = MDG_PREC_FP64;
     size_t footprint = 0;  // bytes charged while it runs
     mdg_request_info info{};
+    double t_graph_start = 0.0;  // server clock at the latest admission to a graph loop
 };
 
 // IDLE -> ALLOC (buffers requested) -> BLOCK (queued or running in a block)
@@ -96,7 +98,7 @@ constexpr size_t kMaxSpentGraphs = 16384;
 
 // Polls (about a microsecond apart) after which an idle block of the
 // persistent kernel exits.
-constexpr int kIdlePolls = 20000;
+constexpr int kIdlePolls = 100000;
 
 }  // namespace
 
@@ -106,12 +108,12 @@ struct mdg_server {
     size_t budget = 0, used = 0, peak = 0;
     size_t max_atoms = 0;
     int block_threads = 0;
+    int order = MDG_ORDER_FIFO;
     std::vector<Slot> slots;
     mdg_ctx* alloc_ctx = nullptr;  // block-mode systems: allocations and releases
-    mdg_ctx* feed_ctx[2] = {nullptr, nullptr};  // the persistent kernel, two launch generations
-    cudaEvent_t feed_ev[2] = {nullptr, nullptr};  // recorded after each launch
-    int feed_launched[2] = {0, 0};
-    int feed_cur = 0;
+    mdg_ctx* feed_ctx[kSoloGens] = {};     // the persistent kernel: one stream per launch slot
+    cudaEvent_t feed_ev[kSoloGens] = {};   // recorded after each launch
+    int feed_launched[kSoloGens] = {};
     int threads = 512, blocks = 0; // persistent kernel shape
     SoloQueue* q = nullptr;        // host-mapped request queue
     SoloQueue* q_dev = nullptr;
@@ -196,6 +198,9 @@ void finish(mdg_server* sv, Request* r, int status) {
     r->info.status = status;
     r->info.done = 1;
     r->info.t_done = sv->now();
+    // graph mode: from admission to completion (host clock); a repeat on the
+    // checked path adds its own span
+    if (r->t_graph_start > 0.0) r->info.service_s += r->info.t_done - r->t_graph_start;
     sv->finished.push_back(r->id);
     sv->nfinished++;
 }
@@ -268,6 +273,7 @@ int ensure_slot_ctx(mdg_server* sv, Slot& sl) {
 // driver's calls one by one, each list build verified and grown).
 void admit_graph(mdg_server* sv, Slot& sl, Request* r, int checked) {
     double t0 = sv->now();
+    r->t_graph_start = t0;
     sl.checked = checked;
     size_t n = r->atoms.size();
     int rc = ensure_slot_ctx(sv, sl);
@@ -427,8 +433,12 @@ int progress(mdg_server* sv) {
             uint32_t done = 0;
             unsigned long long left = 0;
             DevStatus st;
-            solo_out_read((char*)sv->outs + k * sv->out_stride, &done, &left, &st);
-            if (done == sl.seq) advance_block(sv, sl, left, st);
+            double service = 0.0;
+            solo_out_read((char*)sv->outs + k * sv->out_stride, &done, &left, &st, &service);
+            if (done == sl.seq) {
+                sl.req->info.service_s += service;
+                advance_block(sv, sl, left, st);
+            }
             continue;
         }
         cudaError_t e = cudaEventQuery(sl.ev);
@@ -461,14 +471,21 @@ int progress(mdg_server* sv) {
     if (!sv->spent_execs.empty() &&
         ((sv->queue.empty() && running_of(sv) == 0) || sv->spent_execs.size() >= kMaxSpentGraphs))
         destroy_spent(sv);
-    // FIFO admission: the head waits for memory rather than being overtaken
+    // Admission in FIFO order (or, with MDG_ORDER_LARGEST, the largest
+    // waiting request first); the chosen request waits for memory rather
+    // than being overtaken
     AllocGroup group;
     for (Slot& sl : sv->slots) {
         if (sv->queue.empty()) break;
         if (sl.req) continue;
-        Request* r = sv->queue.front();
+        auto pick = sv->queue.begin();
+        if (sv->order == MDG_ORDER_LARGEST)
+            for (auto it = sv->queue.begin(); it != sv->queue.end(); ++it)
+                if ((*it)->atoms.size() * (size_t)(*it)->steps > (*pick)->atoms.size() * (size_t)(*pick)->steps)
+                    pick = it;
+        Request* r = *pick;
         if (sv->used + r->footprint > sv->budget && sv->used > 0) break;
-        sv->queue.pop_front();
+        sv->queue.erase(pick);
         charge(sv, sl, r);
         if (!block_mode(sv, r)) {
             admit_graph(sv, sl, r, 0);
@@ -487,35 +504,44 @@ int progress(mdg_server* sv) {
         MDG_CUDA(cudaEventRecord(group.ev, sv->alloc_ctx->stream));
         sv->alloc_groups.push_back(std::move(group));
     }
-    // the persistent kernel: launched when requests wait and it has fewer
-    // live blocks than it could have (its idle blocks exit after a bounded
-    // wait); the new launch is the other generation, whose previous launch
-    // must have ended, so at most two are in flight
+    // the persistent kernel: topped up when requests wait and fewer of its
+    // blocks are alive (running a request, waiting for one, or launched and
+    // not yet resident) than the smaller of the blocks the GPU holds and the
+    // requests published. Idle blocks exit after a bounded wait, so blocks of
+    // one launch can be gone while others of it still run long requests; a
+    // top-up launches the missing blocks in a launch slot whose previous
+    // launch has ended, with their flags set before the launch so that
+    // blocks not yet resident are counted.
     size_t waiting = 0;
     for (const Slot& sl : sv->slots) waiting += (sl.req && sl.state == BLOCK) ? 1 : 0;
     if (waiting > 0) {
-        auto ended = [&](int gen) -> int {
-            if (!sv->feed_launched[gen]) return 1;
-            cudaError_t e = cudaEventQuery(sv->feed_ev[gen]);
-            if (e == cudaErrorNotReady) return 0;
-            return e == cudaSuccess ? 1 : -1;
-        };
-        const int cur = sv->feed_cur;
-        int live = 0;
-        int cur_end = ended(cur);
-        if (cur_end < 0) return cuda_status(cudaGetLastError(), "persistent kernel");
-        if (!cur_end)
-            for (int b = 0; b < sv->blocks; ++b) live += sv->q->live[cur][b] ? 1 : 0;
-        int gen = -1;
-        if (cur_end) gen = cur;
-        else if ((size_t)live < std::min<size_t>((size_t)sv->blocks, waiting) && ended(cur ^ 1) == 1) gen = cur ^ 1;
-        if (gen >= 0) {
-            int rc = solo_persistent_launch(sv->feed_ctx[gen]->stream, sv->threads, sv->blocks, sv->desc_dev,
-                                            sv->q_dev, sv->head, kIdlePolls, gen);
-            if (rc) return rc;
-            MDG_CUDA(cudaEventRecord(sv->feed_ev[gen], sv->feed_ctx[gen]->stream));
-            sv->feed_launched[gen] = 1;
-            sv->feed_cur = gen;
+        int alive = 0, free_gen = -1;
+        for (int gen = 0; gen < kSoloGens; ++gen) {
+            bool ended = true;
+            if (sv->feed_launched[gen]) {
+                cudaError_t e = cudaEventQuery(sv->feed_ev[gen]);
+                if (e == cudaErrorNotReady) ended = false;
+                else if (e != cudaSuccess) return cuda_status(e, "persistent kernel");
+            }
+            if (ended) {
+                if (free_gen < 0) free_gen = gen;
+                continue;
+            }
+            for (int b = 0; b < sv->blocks; ++b) alive += sv->q->live[gen][b] ? 1 : 0;
+        }
+        if ((size_t)alive < std::min<size_t>((size_t)sv->blocks, waiting) && free_gen >= 0) {
+            const int k = sv->blocks - alive;
+            // an ended launch left every flag of its slot at 0
+            for (int b = 0; b < k; ++b) sv->q->live[free_gen][b] = 1u;
+            std::atomic_thread_fence(std::memory_order_seq_cst);
+            int rc = solo_persistent_launch(sv->feed_ctx[free_gen]->stream, sv->threads, k, sv->desc_dev,
+                                            sv->q_dev, sv->head, kIdlePolls, free_gen);
+            if (rc) {
+                for (int b = 0; b < k; ++b) sv->q->live[free_gen][b] = 0u;
+                return rc;
+            }
+            MDG_CUDA(cudaEventRecord(sv->feed_ev[free_gen], sv->feed_ctx[free_gen]->stream));
+            sv->feed_launched[free_gen] = 1;
             sv->kernel_launches++;
         }
     }
@@ -541,7 +567,7 @@ void server_free(mdg_server* sv) {
     }
     for (AllocGroup& ag : sv->alloc_groups) sv->free_events.push_back(ag.ev);
     for (cudaEvent_t e : sv->free_events) cudaEventDestroy(e);
-    for (int g = 0; g < 2; ++g) {
+    for (int g = 0; g < kSoloGens; ++g) {
         if (sv->feed_ev[g]) cudaEventDestroy(sv->feed_ev[g]);
         if (sv->feed_ctx[g]) mdg_ctx_destroy(sv->feed_ctx[g]);
     }
@@ -568,6 +594,7 @@ int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out
     if (cfg->block_threads > 0 && cfg->block_threads != 256 && cfg->block_threads != 512 &&
         cfg->block_threads != 1024)
         return MDG_ERR_INVALID;
+    if (cfg->order != MDG_ORDER_FIFO && cfg->order != MDG_ORDER_LARGEST) return MDG_ERR_INVALID;
     *out = nullptr;
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
@@ -581,6 +608,7 @@ int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out
     sv->t0 = Clock::now();
     sv->max_atoms = cfg->max_atoms;
     sv->block_threads = cfg->block_threads;
+    sv->order = cfg->order;
     size_t free_b = 0, total_b = 0;
     cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
     if (e != cudaSuccess) {
@@ -623,10 +651,11 @@ int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out
     }
     {
         int rc = mdg_ctx_create(device, &sv->alloc_ctx);
-        for (int g = 0; g < 2 && rc == MDG_OK; ++g) rc = mdg_ctx_create(device, &sv->feed_ctx[g]);
+        for (int g = 0; g < kSoloGens && rc == MDG_OK; ++g) rc = mdg_ctx_create(device, &sv->feed_ctx[g]);
         if (rc == MDG_OK) {
-            e = cudaEventCreateWithFlags(&sv->feed_ev[0], cudaEventDisableTiming);
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sv->feed_ev[1], cudaEventDisableTiming);
+            e = cudaSuccess;
+            for (int g = 0; g < kSoloGens && e == cudaSuccess; ++g)
+                e = cudaEventCreateWithFlags(&sv->feed_ev[g], cudaEventDisableTiming);
             if (e == cudaSuccess) e = cudaHostAlloc((void**)&sv->q, sizeof(SoloQueue), cudaHostAllocMapped);
             if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&sv->q_dev, sv->q, 0);
             if (e == cudaSuccess) memset((void*)sv->q, 0, sizeof(SoloQueue));
@@ -778,7 +807,9 @@ int mdg_server_stats_get(mdg_server* srv, mdg_server_stats* out) {
         if (sl.ctx) mdg_ctx_launch_count(sl.ctx, &l);
         total += l;
     }
-    for (mdg_ctx* c : {srv->alloc_ctx, srv->feed_ctx[0], srv->feed_ctx[1]}) {
+    std::vector<mdg_ctx*> ctxs(srv->feed_ctx, srv->feed_ctx + kSoloGens);
+    ctxs.push_back(srv->alloc_ctx);
+    for (mdg_ctx* c : ctxs) {
         uint64_t l = 0;
         if (c) mdg_ctx_launch_count(c, &l);
         total += l;
@@ -792,6 +823,21 @@ int mdg_server_stats_get(mdg_server* srv, mdg_server_stats* out) {
     out->host_detail_s[1] = srv->download_s;
     out->host_detail_s[2] = srv->graph_destroy_s;
     out->host_detail_s[3] = srv->release_s;
+    // the fused kernel's blocks (host-mapped flags) and the slots feeding it
+    out->live_blocks = out->busy_blocks = 0;
+    if (srv->q)
+        for (int gen = 0; gen < kSoloGens; ++gen)
+            for (int b = 0; b < srv->blocks; ++b) {
+                const uint32_t f = srv->q->live[gen][b];
+                out->live_blocks += f ? 1 : 0;
+                out->busy_blocks += f == 2u ? 1 : 0;
+            }
+    out->block_slots = out->alloc_slots = 0;
+    for (const Slot& sl : srv->slots) {
+        out->block_slots += (sl.req && sl.state == BLOCK) ? 1 : 0;
+        out->alloc_slots += (sl.req && sl.state == ALLOC) ? 1 : 0;
+    }
+    out->kernel_launches = srv->kernel_launches;
     return MDG_OK;
 }
 

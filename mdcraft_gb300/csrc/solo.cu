@@ -32,7 +32,16 @@ struct SoloOut {
     DevStatus st;
     volatile uint32_t done;
     uint32_t pad;
+    // GPU clock (%globaltimer, ns): the block starts on the request / has
+    // written the result records (service time = end - start)
+    unsigned long long t_start, t_end;
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 struct alignas(16) SoloArgs {
     IArgs I;
@@ -345,6 +354,8 @@ __device__ void solo_run(SoloArgs& S, GridParams& g, double (*red)[NT / 32], uin
     long long left = S.steps;
     uint32_t rebuilds = 0;
     bool ok = true;
+    unsigned long long t_start = 0;
+    if (t == 0) t_start = global_ns();
     if (S.setup) ok = solo_setup<EAM, NT>(S, g, red, scan_sh);
     if (t == 0) {
         S.st->need_rebuild = 0;
@@ -370,6 +381,8 @@ __device__ void solo_run(SoloArgs& S, GridParams& g, double (*red)[NT / 32], uin
         S.st->pad[1] = ok ? 0u : 1u;  // 1: a list outgrew its capacities; the run is void
         S.out->left = (unsigned long long)left;
         S.out->st = *S.st;
+        S.out->t_start = t_start;
+        S.out->t_end = global_ns();
         __threadfence_system();
         S.out->done = S.seq;
     }
@@ -394,8 +407,9 @@ __global__ void __launch_bounds__(NT, 1) k_solo_persistent(const SoloArgs* __res
     __shared__ double red[7][NT / 32];
     __shared__ uint32_t scan_sh[32];
     __shared__ int s_rec;
-    // liveness for the host, which tops up the kernel's width with a second
-    // launch when blocks have gone idle and exited while requests wait
+    // liveness for the host (which set 1 before the launch), so that it tops
+    // up the kernel with a further launch when blocks have gone idle and
+    // exited while requests wait
     if (threadIdx.x == 0) q->live[gen][blockIdx.x] = 1u;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -418,6 +432,7 @@ __global__ void __launch_bounds__(NT, 1) k_solo_persistent(const SoloArgs* __res
         __syncthreads();
         const int rec = s_rec;
         if (rec < 0) break;
+        if (threadIdx.x == 0) q->live[gen][blockIdx.x] = 2u;  // 2: running a request
         {
             const int4* src = reinterpret_cast<const int4*>(desc + rec);
             int4* dst = reinterpret_cast<int4*>(&S);
@@ -426,6 +441,7 @@ __global__ void __launch_bounds__(NT, 1) k_solo_persistent(const SoloArgs* __res
         __syncthreads();
         if (S.any_eam) solo_run<true, NT>(S, g, red, scan_sh);
         else solo_run<false, NT>(S, g, red, scan_sh);
+        if (threadIdx.x == 0) q->live[gen][blockIdx.x] = 1u;  // 1: waiting for the next entry
     }
     if (threadIdx.x == 0) {
         __threadfence_system();
@@ -495,11 +511,13 @@ size_t solo_args_bytes() { return sizeof(SoloArgs); }
 static_assert(sizeof(SoloArgs) % 16 == 0, "argument records are copied as 16-byte words");
 size_t solo_out_bytes() { return sizeof(SoloOut); }
 
-int solo_out_read(const void* out_host, uint32_t* done, unsigned long long* left, DevStatus* st) {
+int solo_out_read(const void* out_host, uint32_t* done, unsigned long long* left, DevStatus* st,
+                  double* service_s) {
     const SoloOut* o = reinterpret_cast<const SoloOut*>(out_host);
     *done = __atomic_load_n(const_cast<const uint32_t*>(&o->done), __ATOMIC_ACQUIRE);
     if (left) *left = o->left;
     if (st) *st = o->st;
+    if (service_s) *service_s = o->t_end > o->t_start ? (double)(o->t_end - o->t_start) * 1e-9 : 0.0;
     return MDG_OK;
 }
 
@@ -526,7 +544,7 @@ int solo_persistent_launch(cudaStream_t stream, int threads, int blocks, const v
                            uint32_t* head, int idle_limit, int gen) {
     const SoloArgs* d = reinterpret_cast<const SoloArgs*>(desc_dev);
     if (blocks <= 0) return MDG_OK;
-    if (blocks > kSoloMaxBlocks || gen < 0 || gen > 1) return MDG_ERR_INVALID;
+    if (blocks > kSoloMaxBlocks || gen < 0 || gen >= kSoloGens) return MDG_ERR_INVALID;
     const size_t dyn = solo_dyn_bytes(threads);
     if (threads == 256) {
         MDG_CUDA(solo_prepare_attr<256>());

@@ -246,3 +246,34 @@ def test_autotuner_picks_a_measured_candidate():
     assert best in (256, 1024)
     assert set(rates) == {256, 1024} and all(r > 0 for r in rates.values())
     assert rates[best] == max(rates.values())
+
+
+@pytest.mark.parametrize("block_threads", [0, -1], ids=["fused_block", "graph_loop"])
+def test_largest_first_order_and_service_time(block_threads):
+    """Admission by most atom-steps first: requests queued together start
+    largest first and each result is still the single-system driver loop's,
+    bit for bit; every record carries a service time that excludes the
+    request's queueing."""
+    _ensure_built()
+    solv = SV.solvers("mixed")
+    specs = _specs(8, 40, seed=23)
+    reqs = SV.prepare(specs)
+    srv = mdg.Server(slots=1, max_atoms=8192, block_threads=block_threads, order="largest")
+    ids = [srv.submit(solv[s["kind"]], dom, atoms, s["dt"], s["steps"]) for s, atoms, dom in reqs]
+    infos = {}
+    for k, rid in enumerate(ids):
+        srv.wait(rid, 300.0)
+        out, infos[k] = srv.result(rid)
+        assert infos[k]["status"] == 0
+        if k in (0, 5):
+            assert _same(out, _direct(specs[k], solv)), f"request {k}"
+    srv.close()
+    # one slot: the admissions are sequential, so their order is visible
+    order = sorted(range(len(specs)), key=lambda k: infos[k]["t_admit"])
+    work = [specs[k]["n"] * specs[k]["steps"] for k in order]
+    # the first admission may go to the first request before the rest are
+    # queued; every later one takes the largest waiting request
+    assert work[1:] == sorted(work[1:], reverse=True)
+    for k in range(len(specs)):
+        svc = infos[k]["service_s"]
+        assert 0.0 < svc <= infos[k]["t_done"] - infos[k]["t_submit"] + 1e-3
