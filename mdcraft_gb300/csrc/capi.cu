@@ -417,6 +417,34 @@ static void cubic_coeffs(const std::vector<double>& y, const std::vector<double>
     }
 }
 
+// Per-interval polynomials of the force pass, in u on [x_n, x_n + h] with
+// x_n = n h, from the FP64 pieces of the rho and r*phi (Vpar) splines:
+//   W(u)  = V'(r) r - V(r)  (cubic: the V piece's derivative times r = (n + u) h,
+//           minus the piece itself), row .x..w = W0..W3;
+//   D(u)  = rho'(r)         (quadratic: the rho piece's derivative), row .x..z;
+// so that the EAM pair force over r is ((F'_i + F'_j) D + W / r^2) / r
+// (EAM.cxx:417-463) with every coefficient rounded once from FP64.
+static void force_rows(const std::vector<double>& ry, const std::vector<double>& rz, const std::vector<double>& vy,
+                       const std::vector<double>& vz, double h, int N, std::vector<float4>& out) {
+    out.resize(2 * (size_t)N);
+    const double h1 = 1.0 / h;
+    for (int n = 0; n < N; ++n) {
+        // V piece: v0 + v1 u + v2 u^2 + v3 u^3 (the reference's a, b form)
+        double m = (vy[n + 1] - vy[n]) * h1;
+        double aa = (vz[n + 1] - m) - (m - vz[n]);
+        double bb = aa - (m - vz[n]);
+        const double v0 = vy[n], v1 = h * vz[n], v2 = -h * bb, v3 = h * aa;
+        const double k = (double)n;
+        out[2 * (size_t)n] = make_float4((float)(v1 * k - v0), (float)(2.0 * v2 * k), (float)(v2 + 3.0 * v3 * k),
+                                         (float)(2.0 * v3));
+        // rho piece's derivative in r: (c1 + 2 c2 u + 3 c3 u^2) / h
+        m = (ry[n + 1] - ry[n]) * h1;
+        aa = (rz[n + 1] - m) - (m - rz[n]);
+        bb = aa - (m - rz[n]);
+        out[2 * (size_t)n + 1] = make_float4((float)rz[n], (float)(-2.0 * bb), (float)(3.0 * aa), 0.f);
+    }
+}
+
 int pot_upload(mdg_potential* p, int device) {
     if ((p->type != POT_EAM && p->type != POT_TAB) || p->device == device) return MDG_OK;
     if (p->d_tab64) cudaFree(p->d_tab64);
@@ -435,13 +463,12 @@ int pot_upload(mdg_potential* p, int device) {
     h32.insert(h32.end(), rc.begin(), rc.end());
     h32.insert(h32.end(), vc.begin(), vc.end());
     h32.insert(h32.end(), fc.begin(), fc.end());
-    // rho and V rows interleaved (32 bytes per interval) for the force pass,
-    // which reads both rows of one interval with one load
+    // the force pass's W and D rows of each interval (32 bytes), read with
+    // one load, 32-byte aligned
     if (h32.size() & 1) h32.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
-    for (int k = 0; k < p->Nr1; ++k) {
-        h32.push_back(rc[k]);
-        h32.push_back(vc[k]);
-    }
+    std::vector<float4> fr;
+    force_rows(p->Rho, p->dRho, p->Vpar, p->dVpar, p->dr, p->Nr1, fr);
+    h32.insert(h32.end(), fr.begin(), fr.end());
     MDG_CUDA(cudaSetDevice(device));
     MDG_CUDA(cudaMalloc(&p->d_tab64, h64.size() * sizeof(double)));
     MDG_CUDA(cudaMalloc(&p->d_tab32, h32.size() * sizeof(float4)));

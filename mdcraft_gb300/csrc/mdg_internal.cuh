@@ -140,7 +140,7 @@ struct PotParams {
     const float4* rho_c;
     const float4* v_c;
     const float4* f_c;
-    const float4* rv_c;  // rho_c[k], v_c[k] interleaved, 32-byte aligned rows
+    const float4* rv_c;  // force rows: W(u) = V'r - V, then D(u) = rho' (2 float4 per interval)
     float inv_dr_f, inv_drh_f, dr1_f, drh_f;
 };
 
