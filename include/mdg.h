@@ -161,6 +161,14 @@ int mdg_nlist_list_for(mdg_system* sys, const double x[3], uint64_t* out,
  * ints = {domain_num_cells[3], grid_offset[3], num_cells[3]},
  * dbls = {cell_sizes[3]}. */
 int mdg_nlist_grid(mdg_system* sys, int32_t ints[9], double dbls[3]);
+/* Grid::build (grid.cxx:43-95, find_bounds grid.cxx:209-243) over the
+ * system's atoms, without a list: the same geometry as mdg_nlist_grid,
+ * from a bounds pass on the device (positions are wrapped into the period
+ * as by a rebuild), which replaces the grid mdg_nlist_grid and
+ * mdg_nlist_list_for report until the next rebuild. ints/dbls as for
+ * mdg_nlist_grid; no atoms give the reference's empty grid (grid.cxx:26-34:
+ * one domain cell per axis, offset 1, no local cells). */
+int mdg_grid_build(mdg_system* sys, int32_t ints[9], double dbls[3]);
 /* Rebuilds performed by mdg_run / mdg_nlist_update since creation. */
 int mdg_nlist_rebuilds(mdg_system* sys, uint64_t* count);
 
@@ -206,6 +214,23 @@ int mdg_pot_values(mdg_ctx* ctx, mdg_potential* pot, const double* r2, size_t n,
  * potential without an embedding table (LJsCut, LJs, Pair). */
 int mdg_pot_embedding(mdg_ctx* ctx, mdg_potential* pot, const double* rho, size_t n, double* F,
                       double* dF);
+/* The per-atom overloads of Potential (potential/base.h:44-56):
+ * force(atom, neibs, nlist) (LJs-cut.cxx:22-68, EAM.cxx:465-497),
+ * virial(atom, neibs, nlist) (LJs-cut.cxx:70-131, EAM.cxx:306-354) and
+ * density(atom, neibs, nlist) (EAM.cxx:541-560) of one atom over an explicit
+ * list of indices into neibs[0..nneibs), in the list's order with the
+ * reference's FP64 arithmetic, on ctx's device. Pairs use raw differences
+ * r_j - r_i (no periodic images), as the reference's per-atom calls do.
+ * `atom` may point into neibs. With half != 0, LJsCut also pushes each
+ * pair's force (force) and energy and virial (virial) onto the neighbour;
+ * EAM ignores it, as the reference does. The records are updated in place:
+ * f (force), V, Ep and, for EAM, Em (virial), nc (density). LJs and Pair
+ * are not supported here (MDG_ERR_INVALID), nor is density for LJsCut. */
+#define MDG_ATOM_FORCE 0
+#define MDG_ATOM_VIRIAL 1
+#define MDG_ATOM_DENSITY 2
+int mdg_pot_atom(mdg_ctx* ctx, mdg_potential* pot, int what, mdg_atom* atom, mdg_atom* neibs, size_t nneibs,
+                 const uint64_t* list, size_t count, int half);
 
 /* ---- solvers ------------------------------------------------------------------- */
 /* Single(pot, boundary) (mdcraft/solver/single.h:37-42). periodic != 0
@@ -221,7 +246,8 @@ int mdg_solver_destroy(mdg_solver* s);
 int mdg_solver_num_stages(mdg_solver* s, int* n);
 int mdg_solver_set_precision(mdg_solver* s, int precision);
 /* Pair::prepare / charge / forces / virials (mdcraft/solver/pair.cxx:16-114)
- * on a system whose list is built. */
+ * on a system whose list is built (prepare, which reads no list, also runs
+ * on a system without one). */
 int mdg_solver_prepare(mdg_solver* s, mdg_system* sys);
 int mdg_solver_charge(mdg_solver* s, mdg_system* sys);
 int mdg_solver_forces(mdg_solver* s, mdg_system* sys);

@@ -15,6 +15,7 @@
 #include <fstream>
 #include <sstream>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "mdg_host.h"
@@ -1297,6 +1298,91 @@ int mdg_pot_embedding(mdg_ctx* ctx, mdg_potential* p, const double* rho, size_t 
     return pot_eval(P, 1, rho, n, F, dF, ctx->stream);
 }
 
+int mdg_pot_atom(mdg_ctx* ctx, mdg_potential* p, int what, mdg_atom* atom, mdg_atom* neibs, size_t nneibs,
+                 const uint64_t* list, size_t count, int half) {
+    if (!ctx || !p || !atom || (count && (!list || !neibs))) return MDG_ERR_INVALID;
+    if (what < MDG_ATOM_FORCE || what > MDG_ATOM_DENSITY) return MDG_ERR_INVALID;
+    if (p->type != POT_LJCUT && p->type != POT_EAM) {
+        set_error("per-atom evaluation covers LJsCut and EAM");
+        return MDG_ERR_INVALID;
+    }
+    if (p->type == POT_LJCUT && what == MDG_ATOM_DENSITY) {
+        set_error("LJsCut has no density");
+        return MDG_ERR_INVALID;
+    }
+    if (count == 0) return MDG_OK;  // the reference returns on an empty list
+    if (count > (size_t)INT32_MAX) {
+        set_error("list too long");
+        return MDG_ERR_INVALID;
+    }
+    // records: the atom, then each distinct neighbour once (the atom itself
+    // when it is listed and lies in neibs)
+    const bool inside = atom >= neibs && atom < neibs + nneibs;
+    const size_t self = inside ? (size_t)(atom - neibs) : (size_t)-1;
+    std::vector<mdg_atom> recs(1, *atom);
+    std::vector<uint32_t> slots(count);
+    std::unordered_map<uint64_t, uint32_t> slot_of;
+    std::vector<uint64_t> owner(1, self);
+    for (size_t k = 0; k < count; ++k) {
+        const uint64_t j = list[k];
+        if (j >= nneibs) {
+            set_error("list entry beyond the neighbour array");
+            return MDG_ERR_INVALID;
+        }
+        if (j == self) {
+            slots[k] = 0;
+            continue;
+        }
+        auto it = slot_of.find(j);
+        if (it == slot_of.end()) {
+            it = slot_of.emplace(j, (uint32_t)recs.size()).first;
+            recs.push_back(neibs[j]);
+            owner.push_back(j);
+        }
+        slots[k] = it->second;
+    }
+    MDG_CUDA(cudaSetDevice(ctx->device));
+    int rc = pot_upload(p, ctx->device);
+    if (rc) return rc;
+    PotParams P;
+    fill_params(p, P, nullptr, nullptr);
+    uint32_t flags = 0;
+    rc = pot_atom(P, what, recs.data(), recs.size(), slots.data(), count, half ? 1 : 0, ctx->stream, &flags);
+    if (rc) return rc;
+    *atom = recs[0];
+    for (size_t s = 1; s < recs.size(); ++s) neibs[owner[s]] = recs[s];
+    if (flags & FLAG_TABLE) {
+        set_error("EAM embedding density outside the table (the reference's extrapolation was used)");
+        return MDG_ERR_RANGE;
+    }
+    return MDG_OK;
+}
+
+int mdg_grid_build(mdg_system* sys, int32_t ints[9], double dbls[3]) {
+    if (!sys || !ints || !dbls) return MDG_ERR_INVALID;
+    if (sys->n == 0) {
+        // Grid::initialize_empty (grid.cxx:26-34)
+        for (int a = 0; a < 3; ++a) {
+            ints[a] = 1;
+            ints[3 + a] = 1;
+            ints[6 + a] = 0;
+            dbls[a] = sys->dom.bmax[a] - sys->dom.bmin[a];
+        }
+        return MDG_OK;
+    }
+    MDG_CUDA(cudaSetDevice(sys->ctx->device));
+    GridParams g;
+    int rc = grid_build_only(sys, &g);
+    if (rc) return rc;
+    for (int a = 0; a < 3; ++a) {
+        ints[a] = g.dom_n[a];
+        ints[3 + a] = g.offset[a];
+        ints[6 + a] = g.num[a];
+        dbls[a] = g.cs[a];
+    }
+    return MDG_OK;
+}
+
 // ---- solvers ----------------------------------------------------------------
 static void set_stages(mdg_solver* s, int type, bool first) {
     if (type == POT_TAB || type == POT_LJS) type = POT_LJCUT;  // all potential::type::pair
@@ -1547,7 +1633,7 @@ static int step_stages(mdg_solver* s, mdg_system* sys, const PotSet& ps, int pre
     return rc;
 }
 
-static int check_ready(mdg_solver* s, mdg_system* sys, PotSet* ps) {
+static int check_ready(mdg_solver* s, mdg_system* sys, PotSet* ps, bool need_list = true) {
     if (!s || !sys) return MDG_ERR_INVALID;
     if (s->nstages == 0) {
         set_error("solver has no potential");
@@ -1557,7 +1643,7 @@ static int check_ready(mdg_solver* s, mdg_system* sys, PotSet* ps) {
         set_error("the mixed form needs a full Verlet list (half lists run in the FP64 form)");
         return MDG_ERR_STATE;
     }
-    if (!sys->have_list && sys->n) {
+    if (need_list && !sys->have_list && sys->n) {
         set_error("no Verlet list: call mdg_nlist_update first");
         return MDG_ERR_STATE;
     }
@@ -1578,8 +1664,9 @@ static int check_ready(mdg_solver* s, mdg_system* sys, PotSet* ps) {
 static double pot_rcut_of(mdg_solver* s) { return s->multi ? -1.0 : s->pot[0][0]->rcut; }
 
 int mdg_solver_prepare(mdg_solver* s, mdg_system* sys) {
+    // Pair::prepare reads no list (pair.cxx:16-29)
     PotSet ps;
-    int rc = check_ready(s, sys, &ps);
+    int rc = check_ready(s, sys, &ps, false);
     if (rc) return rc;
     rc = launch_zero(sys, ps.any_eam || s->multi);
     if (rc) return rc;

@@ -17,6 +17,9 @@
 // so the per-atom sums need no atomics and are deterministic.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstring>
+
 #include "mdg_host.h"
 #include "forces_dev.cuh"
 
@@ -692,6 +695,139 @@ __global__ void k_pot_embedding(PotParams P, int n, const double* __restrict__ r
     eam_embed64(P, rho[i], &EF, &d, st);
     F[i] = EF;
     dF[i] = d;
+}
+
+// ---- Potential::force / virial / density of one atom over an explicit list
+// (the per-atom overloads of potential/base.h: LJs-cut.cxx:22-131,
+// EAM.cxx:306-354, 465-497, 541-560). One thread walks the list in the
+// reference's order with its FP64 arithmetic; recs[0] is the atom and
+// slots[k] the record of list entry k. LJsCut with a half list pushes each
+// pair's force, energy and virial onto the neighbour too; EAM ignores the
+// half flag, as the reference does.
+__global__ void k_pot_atom(PotParams P, int what, mdg_atom* recs, const uint32_t* __restrict__ slots, int count,
+                           int half, DevStatus* st) {
+    if (threadIdx.x != 0 || blockIdx.x != 0 || count == 0) return;
+    mdg_atom& a = recs[0];
+    const double x = a.r[0], y = a.r[1], z = a.r[2];
+    if (P.type == POT_LJCUT) {
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        double Vxx = 0.0, Vyy = 0.0, Vzz = 0.0, Vxy = 0.0, Vxz = 0.0, Vyz = 0.0;
+        for (int k = 0; k < count; ++k) {
+            mdg_atom& nb = recs[slots[k]];
+            const double dx = nb.r[0] - x, dy = nb.r[1] - y, dz = nb.r[2] - z;
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 > P.R2cut || r2 < 1e-15) continue;
+            const double pref = lj_pref64(P, r2);
+            if (what == MDG_ATOM_FORCE) {
+                fx += dx * pref;
+                fy += dy * pref;
+                fz += dz * pref;
+                if (half) {
+                    nb.f[0] -= dx * pref;
+                    nb.f[1] -= dy * pref;
+                    nb.f[2] -= dz * pref;
+                }
+            } else if (what == MDG_ATOM_VIRIAL) {
+                const double ff[3] = {pref * dx, pref * dy, pref * dz}, d[3] = {dx, dy, dz};
+                Vxx += ff[0] * dx;
+                Vyy += ff[1] * dy;
+                Vzz += ff[2] * dz;
+                Vxy += ff[0] * dy;
+                Vxz += ff[0] * dz;
+                Vyz += ff[1] * dz;
+                const double r2inv = 1.0 / r2;
+                const double tmp = P.s6 * (r2inv * r2inv * r2inv);
+                const double e = 0.5 * 4 * P.a * tmp * (tmp - 1);
+                a.Ep += e;
+                if (half) {
+                    for (int c = 0; c < 3; ++c)
+                        for (int r = 0; r < 3; ++r) nb.V[r + 3 * c] += 0.5 * (ff[r] * d[c]);
+                    nb.Ep += e;
+                }
+            }
+        }
+        if (what == MDG_ATOM_FORCE) {
+            a.f[0] += fx;
+            a.f[1] += fy;
+            a.f[2] += fz;
+        } else if (what == MDG_ATOM_VIRIAL) {
+            const double M[9] = {Vxx, Vxy, Vxz, Vxy, Vyy, Vyz, Vxz, Vyz, Vzz};
+            for (int q = 0; q < 9; ++q) a.V[q] += 0.5 * M[q];
+        }
+        return;
+    }
+    if (P.type != POT_EAM) return;
+    if (what == MDG_ATOM_DENSITY) {
+        double sd = 0.0;
+        for (int k = 0; k < count; ++k) {
+            const mdg_atom& nb = recs[slots[k]];
+            const double dx = nb.r[0] - x, dy = nb.r[1] - y, dz = nb.r[2] - z;
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 > P.R2cut || r2 < 1e-15) continue;
+            sd = sd + eam_rho64(P, sqrt(r2));
+        }
+        a.nc += sd;
+        return;
+    }
+    // force and virial: F' of every listed neighbour's density and the atom's own
+    double EFs = 0.0, dFs = 0.0;
+    eam_embed64(P, a.nc, &EFs, &dFs, st);
+    double F[3] = {0.0, 0.0, 0.0}, M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Ep = 0.0;
+    for (int k = 0; k < count; ++k) {
+        const mdg_atom& nb = recs[slots[k]];
+        double EFj = 0.0, dFj = 0.0;
+        eam_embed64(P, nb.nc, &EFj, &dFj, st);
+        const double d[3] = {nb.r[0] - x, nb.r[1] - y, nb.r[2] - z};
+        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (r2 > P.R2cut || r2 < 1e-15) continue;
+        double e = 0.0;
+        const double FF = eam_ff64(P, r2, dFj + dFs, &e);
+        if (what == MDG_ATOM_FORCE) {
+            for (int q = 0; q < 3; ++q) F[q] += FF * d[q];
+        } else {
+            const double h = 0.5 * FF;
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 3; ++r) M[r + 3 * c] += h * d[r] * d[c];
+            Ep += e;
+        }
+    }
+    if (what == MDG_ATOM_FORCE) {
+        for (int q = 0; q < 3; ++q) a.f[q] += F[q];
+    } else {
+        a.Em = EFs;
+        for (int q = 0; q < 9; ++q) a.V[q] += M[q];
+        a.Ep += Ep;
+    }
+}
+
+int pot_atom(const PotParams& P, int what, mdg_atom* recs_host, size_t nrec, const uint32_t* slots_host,
+             size_t count, int half, cudaStream_t st, uint32_t* flags) {
+    mdg_atom* d = nullptr;
+    uint32_t* ds = nullptr;
+    DevStatus* dst = nullptr;
+    int rc = MDG_OK;
+    cudaError_t e = cudaMalloc(&d, nrec * sizeof(mdg_atom));
+    if (e == cudaSuccess) e = cudaMalloc(&ds, std::max<size_t>(count, 1) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&dst, sizeof(DevStatus));
+    if (e == cudaSuccess) e = cudaMemsetAsync(dst, 0, sizeof(DevStatus), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, recs_host, nrec * sizeof(mdg_atom), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && count)
+        e = cudaMemcpyAsync(ds, slots_host, count * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        k_pot_atom<<<1, 32, 0, st>>>(P, what, d, ds, (int)count, half, dst);
+        e = cudaGetLastError();
+    }
+    DevStatus hs;
+    memset(&hs, 0, sizeof(hs));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(recs_host, d, nrec * sizeof(mdg_atom), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_status(e, "per-atom potential evaluation");
+    if (flags) *flags = hs.flags;
+    cudaFree(dst);
+    cudaFree(ds);
+    cudaFree(d);
+    return rc;
 }
 
 // what = 0: u[k] = value(x[k]); what = 1: F, dF of density x[k]. Host arrays

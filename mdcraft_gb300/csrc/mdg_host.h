@@ -290,6 +290,14 @@ int nlist_sort_perm(mdg_system* sys, uint32_t* perm);
 int pot_eval(const PotParams& P, int what, const double* x, size_t n, double* out0, double* out1,
              cudaStream_t st);
 int nlist_list_for(mdg_system* sys, const double x[3], std::vector<uint64_t>& found);
+// One atom's force / virial / density over an explicit list (forces.cu):
+// recs_host[0] is the atom, slots_host[k] the record of list entry k; the
+// records come back updated. Waits on `st`.
+int pot_atom(const PotParams& P, int what, mdg_atom* recs_host, size_t nrec, const uint32_t* slots_host,
+             size_t count, int half, cudaStream_t st, uint32_t* flags);
+// Grid::build alone (nlist.cu): the bounds pass and the grid over the
+// system's atoms, waited for.
+int grid_build_only(mdg_system* sys, GridParams* out);
 int nlist_export_offsets(mdg_system* sys, std::vector<uint64_t>& off);
 int nlist_export_entries(mdg_system* sys, const std::vector<uint64_t>& off, uint64_t* idx);
 int nlist_capacity(mdg_system* sys, int half);

@@ -493,6 +493,33 @@ int nlist_capacity(mdg_system* sys, int half) {
     return size_from_grid(sys, *sys->hgrid, half);
 }
 
+// Grid::build alone: the bounds pass and the grid of the current positions.
+int grid_build_only(mdg_system* sys, GridParams* out) {
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    int rc = ensure_parts(sys);
+    if (rc) return rc;
+    const int nparts = nparts_of(sys);
+    DomainDev d = domain_dev(sys);
+    const int c = sys->cur;
+    k_wrap_bounds<<<nparts, kBlock, 0, st>>>((int)sys->n, sys->f64[RX][c], sys->f64[RY][c], sys->f64[RZ][c],
+                                             sys->f64[RNS][c], d, sys->part);
+    MDG_LAUNCHED(ctx);
+    k_grid_finalize<<<1, kBlock, 0, st>>>(sys->part, nparts, d, sys->dgrid, 1LL << 40, sys->dstat);
+    MDG_LAUNCHED(ctx);
+    MDG_CUDA(cudaMemcpyAsync(out, sys->dgrid, sizeof(GridParams), cudaMemcpyDeviceToHost, st));
+    MDG_CUDA(cudaStreamSynchronize(st));
+    if (out->empty == -1) {
+        set_error("neighbour search radius rns must be positive");
+        return MDG_ERR_INVALID;
+    }
+    if (out->empty == -2) {
+        set_error("cell grid too large (more than 1023 cells on an axis)");
+        return MDG_ERR_INVALID;
+    }
+    return MDG_OK;
+}
+
 // The same sizing from atoms still on the host (before they are uploaded):
 // the bounds pass is repeated on the host with the device's arithmetic, so
 // the grid is the one the first rebuild will compute. Nothing waits for the

@@ -5,6 +5,7 @@
 //   lattice::Domain            mdcraft/lattice/domain.h:77-189
 //   tools::Threads             mdcraft/tools/threads.h:28-60   (no-op pool)
 //   neibs::ListOne / List      mdcraft/neibs/verlet-list.h:9-123
+//   neibs::Grid                mdcraft/neibs/grid.h:14-180
 //   neibs::VerletList          mdcraft/neibs/verlet-list.h:134-470
 //   solver::potential::Base, LJsCut, LJs, EAM, Pair
 //                                          potential/{base,LJs-cut,LJs,EAM,pair}.h
@@ -32,6 +33,7 @@
 #include <random>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include <mdcraft/data/atom.h>
@@ -194,7 +196,117 @@ class VerletList;
 // handed `nlist.get()` find the atoms' device copy.
 class List : public std::vector<ListOne> {
 public:
+    List() = default;
+    explicit List(std::size_t n) : std::vector<ListOne>(n) {}
     VerletList* owner = nullptr;
+};
+
+// Grid (grid.h:14-180): build() runs the bounds pass on the GPU
+// (mdg_grid_build); the index queries are the reference's integer
+// arithmetic on the grid it returns (grid.cxx:107-207).
+using cell_id_t = int;
+using Index3D = std::array<cell_id_t, 3>;
+static constexpr cell_id_t empty_cell = -1;
+using Flag3D = std::array<bool, 3>;
+
+struct element_ids {
+    cell_id_t cell_id = 0;
+    point_id atom_id = 0;
+    bool operator<(const element_ids& rhs) const { return cell_id < rhs.cell_id; }
+    bool operator==(const element_ids& rhs) const { return cell_id == rhs.cell_id; }
+};
+
+class Grid {
+public:
+    explicit Grid(Domain& domain, Threads& threads = tools::dummy_pool) : domain(domain) {
+        (void)threads;
+        // Grid::initialize_full (grid.cxx:18-25)
+        cell_sizes = {domain.xsize(), domain.ysize(), domain.zsize()};
+        domain_num_cells = {1, 1, 1};
+        grid_offset = {0, 0, 0};
+        num_cells = {1, 1, 1};
+    }
+
+    void build(const Atoms& atoms) {
+        mdg_domain d = domain.to_mdg();
+        mdg_system* sys = nullptr;
+        gpu::check(mdg_system_create(gpu::context(), &d, atoms.size(), &sys), "Grid::build");
+        int32_t ints[9];
+        double dbls[3];
+        int rc = atoms.empty() ? MDG_OK : mdg_system_upload_atoms(sys, data::as_mdg(atoms), atoms.size());
+        if (rc == MDG_OK) rc = mdg_grid_build(sys, ints, dbls);
+        mdg_system_destroy(sys);
+        gpu::check(rc, "Grid::build");
+        for (int a = 0; a < 3; ++a) {
+            domain_num_cells[a] = ints[a];
+            grid_offset[a] = ints[3 + a];
+            num_cells[a] = ints[6 + a];
+            cell_sizes[a] = dbls[a];
+        }
+    }
+
+    Index3D local_index3D(const vector& v) const {
+        Index3D c = global_index3D(v);
+        for (int i = 0; i < domain.dim(); ++i) c[i] -= grid_offset[i];
+        return c;
+    }
+
+    cell_id_t cell_index(const Index3D& ijk) const { return ijk[0] + num_cells[0] * (ijk[1] + num_cells[1] * ijk[2]); }
+
+    void set_indices(Atoms& atoms, std::vector<element_ids>& indices) const {
+        indices.resize(atoms.size());
+        for (point_id i = 0; i < atoms.size(); ++i) {
+            indices[i].cell_id = cell_index(local_index3D(atoms[i].r));
+            indices[i].atom_id = i;
+        }
+    }
+
+    // Grid::adjacent_cells (grid.cxx:138-207)
+    std::tuple<std::array<cell_id_t, 27>, Flag3D> adjacent_cells(const vector& r) const {
+        const Index3D cell = global_index3D(r);
+        std::array<cell_id_t, 27> list;
+        int size = 0;
+        const bool per[3] = {domain.xperiodic(), domain.yperiodic(), domain.zperiodic()};
+        for (cell_id_t x : {-1, 0, 1}) {
+            if (per[0] && ((domain_num_cells[0] == 1 && x != 0) || (domain_num_cells[0] == 2 && x == 1))) continue;
+            for (cell_id_t y : {-1, 0, 1}) {
+                if (per[1] && ((domain_num_cells[1] == 1 && y != 0) || (domain_num_cells[1] == 2 && y == 1)))
+                    continue;
+                for (cell_id_t z : {-1, 0, 1}) {
+                    if (per[2] && ((domain_num_cells[2] == 1 && z != 0) || (domain_num_cells[2] == 2 && z == 1)))
+                        continue;
+                    Index3D nb = {cell[0] + x, cell[1] + y, cell[2] + z};
+                    for (int a = 0; a < 3; ++a) {
+                        if (per[a]) nb[a] = (nb[a] + domain_num_cells[a]) % domain_num_cells[a];
+                        nb[a] -= grid_offset[a];
+                    }
+                    if (0 <= nb[0] && nb[0] < num_cells[0] && 0 <= nb[1] && nb[1] < num_cells[1] && 0 <= nb[2] &&
+                        nb[2] < num_cells[2])
+                        list[size++] = cell_index(nb);
+                }
+            }
+        }
+        for (int i = size; i < 27; ++i) list[i] = empty_cell;
+        Flag3D is_edge = {false, false, false};
+        for (int i = 0; i < domain.dim(); ++i) is_edge[i] = cell[i] == 0 || cell[i] == num_cells[i] - 1;
+        return {list, is_edge};
+    }
+
+    double cell_size() const { return std::max(cell_sizes[0], std::max(cell_sizes[1], cell_sizes[2])); }
+    cell_id_t cells_number() const { return num_cells[0] * num_cells[1] * num_cells[2]; }
+
+private:
+    Index3D global_index3D(const vector& v) const {
+        Index3D c = {0, 0, 0};
+        for (int i = 0; i < domain.dim(); ++i) c[i] = (cell_id_t)std::floor((v[i] - domain.bmin(i)) / cell_sizes[i]);
+        return c;
+    }
+
+    Domain& domain;
+    Index3D domain_num_cells{};
+    std::array<double, 3> cell_sizes{};
+    Index3D grid_offset{};
+    Index3D num_cells{};
 };
 
 class VerletList {
@@ -337,7 +449,46 @@ public:
     mdg_potential* handle() const { return m_pot; }
     const unsigned short type;
 
+    // Potential::value over arrays of squared distances (base.h:41-42; the
+    // pair energy term, EAM.cxx:141-174, pair.cxx:81-114, LJs.cxx:61-71;
+    // 0 for LJsCut, base.cxx:19), evaluated on the GPU
+    void value(const double* r2, double* Uout, std::size_t size) {
+        gpu::check(mdg_pot_values(gpu::context(), m_pot, r2, size, Uout), "Potential::value");
+    }
+    double value(const double* r2, std::size_t size) {
+        std::vector<double> u(size);
+        value(r2, u.data(), size);
+        double s = 0.0;
+        for (double x : u) s += x;
+        return s;
+    }
+
+    // The per-atom overloads (base.h:44-56): force, virial and density of
+    // one atom over an explicit list of indices into `neibs`, in the list's
+    // order with the reference's FP64 arithmetic, on the GPU
+    // (mdg_pot_atom; LJsCut: LJs-cut.cxx:22-131, EAM: EAM.cxx:306-354,
+    // 465-497, 541-560).
+    virtual void force(Atoms::iterator atom, Atoms& neibs, NeibsListOne& nlist) {
+        per_atom(MDG_ATOM_FORCE, atom, neibs, nlist);
+    }
+    virtual void virial(Atoms::iterator atom, Atoms& neibs, NeibsListOne& nlist) {
+        per_atom(MDG_ATOM_VIRIAL, atom, neibs, nlist);
+    }
+    virtual void density(Atoms::iterator atom, Atoms& neibs, NeibsListOne& nlist) {
+        per_atom(MDG_ATOM_DENSITY, atom, neibs, nlist);
+    }
+
 protected:
+    void per_atom(int what, Atoms::iterator atom, Atoms& neibs, NeibsListOne& nlist) {
+        if (nlist.empty()) return;
+        std::vector<uint64_t> idx(nlist.begin(), nlist.end());
+        const int rc = mdg_pot_atom(gpu::context(), m_pot, what, reinterpret_cast<mdg_atom*>(&*atom),
+                                    data::as_mdg(neibs), neibs.size(), idx.data(), idx.size(), nlist.half() ? 1 : 0);
+        // a density outside the embedding table keeps the reference's
+        // extrapolated value, as the reference does
+        if (rc != MDG_OK && rc != MDG_ERR_RANGE) gpu::check(rc, "Potential per-atom call");
+    }
+
     double m_rcut;
     mdg_potential* m_pot = nullptr;
 };
@@ -361,6 +512,10 @@ public:
     explicit EAM(std::string filename) : Base(0.0, type::eam) {
         gpu::check(mdg_pot_eam_create_from_file(filename.c_str(), &m_pot), "EAM(file)");
         gpu::check(mdg_pot_rcut(m_pot, &m_rcut), "EAM rcut");
+    }
+    // EAM::embeddingEnergy (EAM.cxx:562-601) on the GPU
+    void embeddingEnergy(const double* nr, double* EF, double* dF, std::size_t size) {
+        gpu::check(mdg_pot_embedding(gpu::context(), m_pot, nr, size, EF, dF), "EAM::embeddingEnergy");
     }
 };
 
@@ -509,7 +664,24 @@ public:
     virtual ~ISolver() {
         if (m_s) mdg_solver_destroy(m_s);
     }
-    virtual void prepare(Atoms& atoms, Atoms& neibs, NeibsList& nlist) { call(mdg_solver_prepare, nlist); }
+    // Pair::prepare (pair.cxx:16-29). The reference's prepare reads no list,
+    // so a list no VerletList owns is accepted: the atoms are then prepared
+    // on a device system of their own over the boundary's domain.
+    virtual void prepare(Atoms& atoms, Atoms& neibs, NeibsList& nlist) {
+        (void)neibs;
+        if (nlist.owner) {
+            call(mdg_solver_prepare, nlist);
+            return;
+        }
+        mdg_domain d = m_domain->to_mdg();
+        mdg_system* sys = nullptr;
+        gpu::check(mdg_system_create(gpu::context(), &d, atoms.size(), &sys), "prepare");
+        int rc = atoms.empty() ? MDG_OK : mdg_system_upload_atoms(sys, data::as_mdg(atoms), atoms.size());
+        if (rc == MDG_OK) rc = mdg_solver_prepare(m_s, sys);
+        if (rc == MDG_OK && !atoms.empty()) rc = mdg_system_download_atoms(sys, data::as_mdg(atoms), atoms.size());
+        mdg_system_destroy(sys);
+        gpu::check(rc, "prepare");
+    }
     void charge(Atoms&, Atoms&, NeibsList& nlist) { call(mdg_solver_charge, nlist); }
     void forces(Atoms&, Atoms&, NeibsList& nlist) { call(mdg_solver_forces, nlist); }
     void virials(Atoms&, Atoms&, NeibsList& nlist) { call(mdg_solver_virials, nlist); }
@@ -535,6 +707,7 @@ protected:
             stages.emplace_back([this](Atoms& a, Atoms& b, NeibsList& l) { forces(a, b, l); });
     }
     mdg_solver* m_s = nullptr;
+    lattice::Domain* m_domain = &lattice::dummy_domain;  // the boundary's domain
 };
 
 using Pair = ISolver;
@@ -545,6 +718,7 @@ public:
     Single(Potential& potential, Boundary& boundary = boundary::dummy_boundary,
            Thermostat& thermostat = thermostat::dummy_thermostat, tools::Threads& threads = tools::dummy_pool) {
         (void)threads;
+        m_domain = &boundary.get_domain();
         gpu::check(mdg_solver_single(potential.handle(), boundary.periodic() ? 1 : 0, &m_s), "Single");
         if (thermostat.handle()) gpu::check(mdg_solver_set_thermostat(m_s, thermostat.handle()), "thermostat");
         make_stages();
@@ -557,6 +731,7 @@ public:
     Multi(Boundary& boundary = boundary::dummy_boundary, Thermostat& thermostat = thermostat::dummy_thermostat,
           std::size_t nkinds = 1, tools::Threads& threads = tools::dummy_pool) {
         (void)threads;
+        m_domain = &boundary.get_domain();
         gpu::check(mdg_solver_multi((int)nkinds, boundary.periodic() ? 1 : 0, &m_s), "Multi");
         if (thermostat.handle()) gpu::check(mdg_solver_set_thermostat(m_s, thermostat.handle()), "thermostat");
     }
