@@ -3,9 +3,9 @@
  *
  * Each function cites the reference routine it restates. Arithmetic follows
  * the reference's FP64 operation order; compile with -ffp-contract=off.
- * Threads: a small dynamic parallel-for over atoms (pthreads), standing in for
- * mdcraft::tools::Threads (mdcraft/tools/threads.h:225-347) so the CPU
- * baseline uses every host core.
+ * Threads: mdcraft::tools::Threads restated (a kept pool of workers and the
+ * reference's cut of each loop into bins, threads.h:214-347), so the timed
+ * CPU baseline runs the reference's threading scheme on every host core.
  */
 #define _GNU_SOURCE
 #include "mdref.h"
@@ -18,59 +18,114 @@
 #include <unistd.h>
 
 /* ------------------------------------------------------------------------ */
-/* parallel-for                                                             */
+/* parallel-for: tools::Threads with its thread pool                        */
 /* ------------------------------------------------------------------------ */
 
 typedef void (*range_fn)(void* ctx, size_t b, size_t e, int tid);
 
+/* tools::Threads (mdcraft/tools/threads.h:214-347, threads.cxx:32-74,
+ * thread-pool.h): `count` workers made once and kept; every parallel loop
+ * is cut into n_tasks = max(1, min(10 * count, n / 500)) bins of n / n_tasks
+ * elements (the last bin takes the remainder), handed to the workers in
+ * order through one queue while the caller waits for all of them; with
+ * count < 2 the loop runs serially on the caller (Threads::disabled). */
 typedef struct {
+    int count;
+    pid_t pid; /* the process whose threads these are (a fork keeps none) */
+    pthread_t th[256];
+    pthread_mutex_t mu;
+    pthread_cond_t work, done;
     range_fn fn;
     void* ctx;
-    size_t n, chunk;
-    atomic_size_t next;
-} pf_job;
+    size_t n, bin;
+    int n_tasks, next_task, done_tasks;
+    int stop;
+} md_pool;
 
 typedef struct {
-    pf_job* job;
+    md_pool* pool;
     int tid;
-} pf_arg;
+} md_worker;
 
-static void* pf_worker(void* p) {
-    pf_arg* a = (pf_arg*)p;
-    pf_job* j = a->job;
+static md_pool* g_pool = NULL;
+static md_worker g_workers[256];
+
+static void* pool_worker(void* p) {
+    md_worker* w = (md_worker*)p;
+    md_pool* q = w->pool;
+    pthread_mutex_lock(&q->mu);
     for (;;) {
-        size_t b = atomic_fetch_add(&j->next, j->chunk);
-        if (b >= j->n) break;
-        size_t e = b + j->chunk < j->n ? b + j->chunk : j->n;
-        j->fn(j->ctx, b, e, a->tid);
+        while (!q->stop && q->next_task >= q->n_tasks) pthread_cond_wait(&q->work, &q->mu);
+        if (q->stop) break;
+        const int t = q->next_task++;
+        const size_t b = (size_t)t * q->bin;
+        const size_t e = t == q->n_tasks - 1 ? q->n : b + q->bin;
+        pthread_mutex_unlock(&q->mu);
+        q->fn(q->ctx, b, e, w->tid);
+        pthread_mutex_lock(&q->mu);
+        if (++q->done_tasks == q->n_tasks) pthread_cond_signal(&q->done);
     }
+    pthread_mutex_unlock(&q->mu);
     return NULL;
+}
+
+static void pool_stop(md_pool* q) {
+    pthread_mutex_lock(&q->mu);
+    q->stop = 1;
+    pthread_cond_broadcast(&q->work);
+    pthread_mutex_unlock(&q->mu);
+    for (int t = 0; t < q->count; ++t) pthread_join(q->th[t], NULL);
+    pthread_mutex_destroy(&q->mu);
+    pthread_cond_destroy(&q->work);
+    pthread_cond_destroy(&q->done);
+    free(q);
+}
+
+/* The pool of `count` workers (Threads::resize makes a new ThreadPool). */
+static md_pool* pool_get(int count) {
+    if (g_pool && g_pool->pid != getpid()) g_pool = NULL; /* inherited by a fork: no threads behind it */
+    if (g_pool && g_pool->count == count) return g_pool;
+    if (g_pool) pool_stop(g_pool);
+    md_pool* q = (md_pool*)calloc(1, sizeof(md_pool));
+    q->count = count;
+    q->pid = getpid();
+    pthread_mutex_init(&q->mu, NULL);
+    pthread_cond_init(&q->work, NULL);
+    pthread_cond_init(&q->done, NULL);
+    for (int t = 0; t < count; ++t) {
+        g_workers[t].pool = q;
+        g_workers[t].tid = t;
+        pthread_create(&q->th[t], NULL, pool_worker, &g_workers[t]);
+    }
+    g_pool = q;
+    return q;
 }
 
 static void parallel_for(int nthreads, size_t n, range_fn fn, void* ctx) {
     if (n == 0) return;
-    if (nthreads <= 1 || n < 256) {
+    if (nthreads > 256) nthreads = 256;
+    if (nthreads < 2) {
         fn(ctx, 0, n, 0);
         return;
     }
-    pf_job job;
-    job.fn = fn;
-    job.ctx = ctx;
-    job.n = n;
-    job.chunk = n / ((size_t)nthreads * 16);
-    if (job.chunk < 64) job.chunk = 64;
-    atomic_init(&job.next, 0);
-    pthread_t th[256];
-    pf_arg args[256];
-    if (nthreads > 256) nthreads = 256;
-    for (int t = 0; t < nthreads; ++t) {
-        args[t].job = &job;
-        args[t].tid = t;
-    }
-    for (int t = 1; t < nthreads; ++t)
-        pthread_create(&th[t], NULL, pf_worker, &args[t]);
-    pf_worker(&args[0]);
-    for (int t = 1; t < nthreads; ++t) pthread_join(th[t], NULL);
+    md_pool* q = pool_get(nthreads);
+    size_t per = n / 500;
+    size_t want = (size_t)10 * (size_t)nthreads;
+    int n_tasks = (int)(per < want ? per : want);
+    if (n_tasks < 1) n_tasks = 1;
+    pthread_mutex_lock(&q->mu);
+    q->fn = fn;
+    q->ctx = ctx;
+    q->n = n;
+    q->bin = n / (size_t)n_tasks;
+    q->done_tasks = 0;
+    q->next_task = 0;
+    q->n_tasks = n_tasks;
+    pthread_cond_broadcast(&q->work);
+    while (q->done_tasks < q->n_tasks) pthread_cond_wait(&q->done, &q->mu);
+    q->n_tasks = 0; /* nothing left to hand out */
+    q->next_task = 0;
+    pthread_mutex_unlock(&q->mu);
 }
 
 int md_hardware_threads(void) {
