@@ -285,6 +285,18 @@ int solo_out_read(const void* out_host, uint32_t* done, unsigned long long* left
 int solo_persistent_launch(cudaStream_t stream, int threads, int blocks, const void* desc_dev, SoloQueue* q_dev,
                            uint32_t* head, int idle_limit, int gen);
 int solo_blocks_per_sm(int threads, int* blocks);
+// The persistent kernel inside a captured graph: one executable graph per
+// launch slot, made by capturing that slot's first launch on its stream;
+// a later launch sets the graph's kernel node to the blocks it wants and
+// launches the graph again.
+struct SoloGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t node = nullptr;
+};
+int solo_graph_launch(SoloGraph& G, cudaStream_t stream, int threads, int blocks, const void* desc_dev,
+                      SoloQueue* q_dev, uint32_t* head, int idle_limit, int gen);
+void solo_graph_destroy(SoloGraph& G);
 int nlist_build(mdg_system* sys, double kbuf, int half);
 int nlist_sort_perm(mdg_system* sys, uint32_t* perm);
 int pot_eval(const PotParams& P, int what, const double* x, size_t n, double* out0, double* out1,

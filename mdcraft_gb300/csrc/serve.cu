@@ -20,7 +20,9 @@
 // memory; the host polls those and never waits for the device. Idle blocks
 // exit after a bounded wait; the host tops the kernel up with a further
 // launch (up to kSoloGens in flight) whenever fewer blocks are alive than
-// the GPU holds and requests wait.
+// the GPU holds and requests wait. Each launch slot's kernel is captured
+// once into a CUDA graph; a top-up sets that graph's grid to the blocks
+// missing and launches it.
 //
 // Graph mode (everything else, or when block mode is off): the request's
 // system gets the slot's own stream; set-up and the loop (one graph launch)
@@ -113,6 +115,7 @@ struct mdg_server {
     mdg_ctx* alloc_ctx = nullptr;  // block-mode systems: allocations and releases
     mdg_ctx* feed_ctx[kSoloGens] = {};     // the persistent kernel: one stream per launch slot
     cudaEvent_t feed_ev[kSoloGens] = {};   // recorded after each launch
+    SoloGraph feed_graph[kSoloGens];       // the kernel captured once per launch slot
     int feed_launched[kSoloGens] = {};
     int threads = 512, blocks = 0; // persistent kernel shape
     SoloQueue* q = nullptr;        // host-mapped request queue
@@ -534,8 +537,8 @@ int progress(mdg_server* sv) {
             // an ended launch left every flag of its slot at 0
             for (int b = 0; b < k; ++b) sv->q->live[free_gen][b] = 1u;
             std::atomic_thread_fence(std::memory_order_seq_cst);
-            int rc = solo_persistent_launch(sv->feed_ctx[free_gen]->stream, sv->threads, k, sv->desc_dev,
-                                            sv->q_dev, sv->head, kIdlePolls, free_gen);
+            int rc = solo_graph_launch(sv->feed_graph[free_gen], sv->feed_ctx[free_gen]->stream, sv->threads, k,
+                                       sv->desc_dev, sv->q_dev, sv->head, kIdlePolls, free_gen);
             if (rc) {
                 for (int b = 0; b < k; ++b) sv->q->live[free_gen][b] = 0u;
                 return rc;
@@ -568,6 +571,7 @@ void server_free(mdg_server* sv) {
     for (AllocGroup& ag : sv->alloc_groups) sv->free_events.push_back(ag.ev);
     for (cudaEvent_t e : sv->free_events) cudaEventDestroy(e);
     for (int g = 0; g < kSoloGens; ++g) {
+        solo_graph_destroy(sv->feed_graph[g]);
         if (sv->feed_ev[g]) cudaEventDestroy(sv->feed_ev[g]);
         if (sv->feed_ctx[g]) mdg_ctx_destroy(sv->feed_ctx[g]);
     }

@@ -560,6 +560,56 @@ int solo_persistent_launch(cudaStream_t stream, int threads, int blocks, const v
     return MDG_OK;
 }
 
+int solo_graph_launch(SoloGraph& G, cudaStream_t stream, int threads, int blocks, const void* desc_dev,
+                      SoloQueue* q_dev, uint32_t* head, int idle_limit, int gen) {
+    if (blocks <= 0) return MDG_OK;
+    if (blocks > kSoloMaxBlocks || gen < 0 || gen >= kSoloGens) return MDG_ERR_INVALID;
+    if (!G.exec) {
+        // the kernel's shared-memory attribute is set before the capture (it
+        // is not a stream operation)
+        int per_sm = 0;
+        int rc = solo_blocks_per_sm(threads, &per_sm);
+        if (rc) return rc;
+        MDG_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        rc = solo_persistent_launch(stream, threads, blocks, desc_dev, q_dev, head, idle_limit, gen);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(stream, &g);
+        if (rc != MDG_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return rc != MDG_OK ? rc : cuda_status(e, "persistent kernel capture");
+        }
+        cudaGraphNode_t node = nullptr;
+        size_t nn = 1;
+        e = cudaGraphGetNodes(g, &node, &nn);
+        if (e == cudaSuccess && nn != 1) {
+            cudaGraphDestroy(g);
+            set_error("persistent kernel capture: expected one kernel node");
+            return MDG_ERR_CUDA;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&G.exec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            G.exec = nullptr;
+            return cuda_status(e, "persistent kernel graph");
+        }
+        G.graph = g;
+        G.node = node;
+    } else {
+        cudaKernelNodeParams p;
+        MDG_CUDA(cudaGraphKernelNodeGetParams(G.node, &p));
+        p.gridDim = dim3((unsigned)blocks, 1, 1);
+        MDG_CUDA(cudaGraphExecKernelNodeSetParams(G.exec, G.node, &p));
+    }
+    MDG_CUDA(cudaGraphLaunch(G.exec, stream));
+    return MDG_OK;
+}
+
+void solo_graph_destroy(SoloGraph& G) {
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    if (G.graph) cudaGraphDestroy(G.graph);
+    G = SoloGraph();
+}
+
 int solo_blocks_per_sm(int threads, int* blocks) {
     cudaError_t e;
     const size_t dyn = solo_dyn_bytes(threads);
