@@ -39,6 +39,11 @@ int launch_virials(mdg_system* sys, const PotSet* dps, const PotSet& ps);
 int launch_drift(mdg_system* sys, double dt, int precision, double pot_rcut, int periodic_boundary, int drift,
                  int check);
 int launch_kick(mdg_system* sys, double dt, int precision);
+int launch_forces_step(mdg_system* sys, const PotSet* dps, const PotSet& ps, double dt,
+                       const unsigned long long* left);
+int launch_drift_guarded(mdg_system* sys, double dt, const unsigned long long* left, unsigned long long min_left);
+int ensure_cutbits(mdg_system* sys);
+int launch_density_rec(mdg_system* sys, const PotSet* dps, const PotSet& ps);
 int launch_decide(mdg_system* sys);
 int launch_trig(mdg_system* sys);
 int launch_offsets(mdg_system* sys);
@@ -343,6 +348,9 @@ void system_free(mdg_system* sys) {
     sys_free(sys, sys->scan_tmp, sys->scan_cap * sizeof(uint32_t));
     sys_free(sys, sys->part, sys->part_cap * 8 * sizeof(double));
     sys_free(sys, sys->nbr, (size_t)sys->K * sys->np * sizeof(uint32_t));
+    sys_free(sys, sys->cutbits, (size_t)sys->cut_words * sys->np * sizeof(uint32_t));
+    sys->cutbits = nullptr;
+    sys->cut_words = 0;
     sys_free(sys, sys->xfer, sys->xfer_bytes);
     sys_free(sys, sys->step_io, sys->step_io_bytes);
     sys->step_io = nullptr;
@@ -1609,6 +1617,33 @@ static double fused_kick(mdg_solver* s, int prec, double dt) {
     return prec == MDG_PREC_MIXED && !s->thermo ? dt : 0.0;
 }
 
+// Whether a mixed step loop starts each next step inside the force pass
+// (k_force_step): the mixed EAM form without a thermostat, whose second
+// half-kick already runs there (the EAM force pass reads its neighbours only
+// through the density pass's copies, so it can move atoms).
+static bool starts_next_step(mdg_solver* s, const PotSet& ps, int prec) {
+    return prec == MDG_PREC_MIXED && !s->thermo && ps.any_eam;
+}
+
+// The stages of a loop step whose force pass may start the next step
+// (launch_forces_step; sys->dcounter holds the steps left, this one
+// included): the density pass where the solver has one, then the force pass.
+static int step_stages_next(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt) {
+    for (int q = 0; q < s->nstages - 1; ++q) {
+        cudaEvent_t t0 = timer_begin(sys->ctx);
+        int rc = s->stages[q] == 0 ? launch_density_rec(sys, ext(s)->d.dev, ps)
+                                   : launch_stage(sys, ext(s)->d.dev, ps, MDG_PREC_MIXED, s->stages[q], nullptr, 0.0);
+        timer_end(sys->ctx, s->stages[q] == 0 ? MDG_TIME_DENSITY : MDG_TIME_FORCES, t0);
+        if (rc) return rc;
+    }
+    cudaEvent_t t0 = timer_begin(sys->ctx);
+    int rc = launch_forces_step(sys, ext(s)->d.dev, ps, dt, sys->dcounter);
+    timer_end(sys->ctx, MDG_TIME_FORCES, t0);
+    if (rc) return rc;
+    sys->force_prec = MDG_PREC_MIXED;
+    return MDG_OK;
+}
+
 // The step's stages, the last one carrying the fused kick where it applies,
 // then the kick pass where it does not.
 static int step_stages(mdg_solver* s, mdg_system* sys, const PotSet& ps, int prec, double dt) {
@@ -1782,10 +1817,14 @@ int mdg_verlet_make_step(mdg_solver* s, mdg_system* sys, double dt) {
 // ---------------------------------------------------------------------------
 namespace mdg {
 
+// After a step's force pass: the rebuild test of this step's positions
+// chooses the rebuild; the test of the next step's positions, when the force
+// pass already ran that step's drift, becomes the current one.
 __global__ void k_rebuild_cond(cudaGraphConditionalHandle h, DevStatus* st) {
     if (threadIdx.x != 0) return;
     unsigned need = st->need_rebuild;
-    st->need_rebuild = 0;
+    st->need_rebuild = st->need_next;
+    st->need_next = 0;
     if (need) st->pad[0] += 1;  // rebuilds done inside graphs
     cudaGraphSetConditional(h, need ? 1u : 0u);
 }
@@ -1812,6 +1851,7 @@ __global__ void k_set_counter(unsigned long long* counter, unsigned long long v,
     if (threadIdx.x == 0) {
         *counter = v;
         st->need_rebuild = 0;
+        st->need_next = 0;
         st->build_flags = 0;
         st->pad[0] = 0;
     }
@@ -1832,6 +1872,10 @@ static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, dou
     int prec = s->precision;
     if (!sys->dcounter) {
         int rc = sys_malloc(sys, (void**)&sys->dcounter, sizeof(unsigned long long));
+        if (rc) return rc;
+    }
+    if (starts_next_step(s, ps, prec)) {
+        int rc = ensure_cutbits(sys);
         if (rc) return rc;
     }
     cudaGraph_t g = nullptr;
@@ -1881,6 +1925,10 @@ static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, dou
                 e = add_cond(pp);
             }
             if (rc0 == 0 && e == cudaSuccess) rc0 = launch_offsets(sys);
+            // the first step's half-kick and drift (later steps start in the
+            // force pass before them)
+            if (rc0 == 0 && e == cudaSuccess && starts_next_step(s, ps, prec))
+                rc0 = launch_drift_guarded(sys, dt, sys->dcounter, 1);
         }
         if (rc0 == 0 && e == cudaSuccess) {
             k_loop_start<<<1, 32, 0, st>>>(hloop, sys->dcounter, sys->dstat);
@@ -1913,8 +1961,14 @@ static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, dou
 
     l0 = ctx->launches;
     MDG_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    int rc = launch_drift(sys, dt, prec, s->multi ? -1.0 : s->pot[0][0]->rcut, s->periodic, 1, 1);
-    if (rc == 0) rc = step_stages(s, sys, ps, prec, dt);
+    const bool next = starts_next_step(s, ps, prec);
+    int rc = MDG_OK;
+    if (next) {
+        rc = step_stages_next(s, sys, ps, dt);
+    } else {
+        rc = launch_drift(sys, dt, prec, s->multi ? -1.0 : s->pot[0][0]->rcut, s->periodic, 1, 1);
+        if (rc == 0) rc = step_stages(s, sys, ps, prec, dt);
+    }
     if (rc == 0) {
         k_rebuild_cond<<<1, 32, 0, st>>>(hrb, sys->dstat);
         ctx->launches++;
@@ -1953,6 +2007,9 @@ static int build_run_graph(mdg_solver* s, mdg_system* sys, const PotSet& ps, dou
                                            cudaStreamCaptureModeThreadLocal));
     rc = nlist_enqueue(sys);
     if (rc == 0) rc = launch_trig(sys);
+    // the next step's half-kick and drift, which the force pass left to
+    // after the rebuild (none after the last step)
+    if (rc == 0 && next) rc = launch_drift_guarded(sys, dt, sys->dcounter, 2);
     e2 = cudaStreamEndCapture(st, &out);
     if (rc) return rc;
     if (e2 != cudaSuccess) return cuda_status(e2, "rebuild capture");
@@ -2310,6 +2367,77 @@ static bool page_locked(const void* p) {
 
 extern "C" {
 
+namespace mdg {
+// The host-driven step loop's bookkeeping where the force pass starts the
+// next step: the flags and counter as the graph's k_rebuild_cond and
+// k_loop_ctrl leave them.
+__global__ void k_need_swap(DevStatus* st) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        st->need_rebuild = st->need_next;
+        st->need_next = 0;
+    }
+}
+__global__ void k_counter_dec(unsigned long long* c) {
+    if (threadIdx.x == 0 && blockIdx.x == 0 && *c > 0) *c -= 1;
+}
+}  // namespace mdg
+
+// The step loop of mdg_run driven from the host (timing on), for a mixed
+// solver whose force pass starts the next step: the same passes in the same
+// order as the graph (first drift; per step density, force + next drift, and
+// after a rebuild the next drift as its own pass), each timed.
+static int run_loop_next(mdg_solver* s, mdg_system* sys, const PotSet& ps, double dt, long steps, cudaEvent_t ev) {
+    mdg_ctx* ctx = sys->ctx;
+    cudaStream_t st = ctx->stream;
+    if (!sys->dcounter) {
+        int rc = sys_malloc(sys, (void**)&sys->dcounter, sizeof(unsigned long long));
+        if (rc) return rc;
+    }
+    {
+        int rc = ensure_cutbits(sys);
+        if (rc) return rc;
+    }
+    k_set_counter<<<1, 32, 0, st>>>(sys->dcounter, (unsigned long long)steps, sys->dstat);
+    MDG_LAUNCHED(ctx);
+    if (sys->force_prec != MDG_PREC_MIXED) {
+        int rc = launch_force_copy(sys, 0);
+        if (rc) return rc;
+        sys->force_prec = MDG_PREC_MIXED;
+    }
+    {
+        cudaEvent_t t0 = timer_begin(ctx);
+        int rc = launch_drift_guarded(sys, dt, sys->dcounter, 1);
+        timer_end(ctx, MDG_TIME_DRIFT, t0);
+        if (rc) return rc;
+    }
+    for (long k = 0; k < steps; ++k) {
+        // this step's rebuild test is final before its stages run
+        MDG_CUDA(cudaMemcpyAsync(&sys->hstat->need_rebuild, &sys->dstat->need_rebuild, sizeof(uint32_t),
+                                 cudaMemcpyDeviceToHost, st));
+        MDG_CUDA(cudaEventRecord(ev, st));
+        int rc = step_stages_next(s, sys, ps, dt);
+        if (rc) return rc;
+        k_need_swap<<<1, 32, 0, st>>>(sys->dstat);
+        MDG_LAUNCHED(ctx);
+        MDG_CUDA(cudaEventSynchronize(ev));
+        if (sys->hstat->need_rebuild) {
+            cudaEvent_t t0 = timer_begin(ctx);
+            rc = nlist_build(sys, -1.0, sys->half);
+            timer_end(ctx, MDG_TIME_REBUILD, t0);
+            if (rc && rc != MDG_ERR_RANGE) return rc;
+            rc = launch_trig(sys);
+            if (rc) return rc;
+            t0 = timer_begin(ctx);
+            rc = launch_drift_guarded(sys, dt, sys->dcounter, 2);
+            timer_end(ctx, MDG_TIME_DRIFT, t0);
+            if (rc) return rc;
+        }
+        k_counter_dec<<<1, 32, 0, st>>>(sys->dcounter);
+        MDG_LAUNCHED(ctx);
+    }
+    return MDG_OK;
+}
+
 int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
     PotSet ps;
     int rc = check_ready(s, sys, &ps);
@@ -2339,6 +2467,11 @@ int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
         }
         rc = launch_offsets(sys);
         if (rc) goto done;
+    }
+    if (starts_next_step(s, ps, prec) && sys->n > 0) {
+        rc = run_loop_next(s, sys, ps, dt, steps, ev);
+        if (rc) goto done;
+        steps = 0;  // done above
     }
     for (long k = 0; k < steps; ++k) {
         cudaError_t ce = cudaMemsetAsync(&sys->dstat->need_rebuild, 0, sizeof(uint32_t), st);

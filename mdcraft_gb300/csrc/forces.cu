@@ -22,6 +22,7 @@
 
 #include "mdg_host.h"
 #include "forces_dev.cuh"
+#include "integrate_dev.cuh"
 
 namespace mdg {
 
@@ -374,6 +375,12 @@ __global__ void __launch_bounds__(kBlock, MB) k_lj_mixed(FArgs A, const PotSet* 
 }
 
 template <bool MULTI, int MB>
+__global__ void __launch_bounds__(kBlock, MB) k_density_rec(FArgs A, const PotSet* __restrict__ ps) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < A.n) density_mixed_one<MULTI, true>(A, ps, i);
+}
+
+template <bool MULTI, int MB>
 __global__ void __launch_bounds__(kBlock, MB) k_density_mixed(FArgs A, const PotSet* __restrict__ ps) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < A.n) density_mixed_one<MULTI>(A, ps, i);
@@ -539,6 +546,7 @@ FArgs force_args(mdg_system* sys) {
     A.Fp32 = sys->Fp32;
     A.pos32 = sys->pos32;
     A.pos32b = sys->pos32 + sys->np;
+    A.cutbits = nullptr;  // set by the passes of a step loop whose force pass moves atoms
     A.Ep = sys->f64[EP][c];
     A.Em = sys->f64[EM][c];
     for (int k = 0; k < 9; ++k) A.V[k] = sys->f64[V0 + k][c];
@@ -600,6 +608,109 @@ static void launch_forces_mixed(const mdg_system* sys, const FArgs& A, const Pot
         if (multi) launch_eam_lj<true, KICK>(false, mb, A, dps, nb, st);
         else launch_eam_lj<false, KICK>(false, mb, A, dps, nb, st);
     }
+}
+
+// ---- the force pass that starts the next step -----------------------------
+// The step loop's EAM force pass (mixed form, no thermostat) with the step's
+// second half-kick. When the next step can start in it — steps remain after
+// this one (*left > 1) and no rebuild is due at this step's positions
+// (need_rebuild, from the drift that made them) — every atom then also runs
+// the next step's first half-kick, drift, offsets refresh and rebuild test
+// (kick_drift_mixed; atoms with tag 0 only the last two), the test's result
+// into need_next; otherwise the next drift runs as its own pass after the
+// rebuild. The decision is the same for every thread. Moving atoms while
+// others still read them is safe here because this pass reads its
+// neighbours only through the density pass's copies (pos32b, Fp32) and takes
+// each pair's cut decision from the density pass (cutbits), where the
+// unfused pass would settle pairs near the cutoff on the FP64 positions.
+template <bool MULTI, int MB>
+__global__ void __launch_bounds__(kBlock, MB)
+    k_force_step(FArgs A, IArgs D, const PotSet* __restrict__ ps, const unsigned long long* __restrict__ left) {
+    const bool next = *left > 1ull && A.st->need_rebuild == 0u;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool need = false;
+    if (i < A.n) {
+        float fx, fy, fz;
+        const bool moved = eam_mixed_force<MULTI, true>(A, ps, i, fx, fy, fz);
+        if (!next) {
+            if (moved) store_force<true>(A, i, fx, fy, fz);
+        } else if (moved) {
+            need = kick_drift_mixed(D, A.gx, A.gy, A.gz, i, fx, fy, fz);
+        } else {
+            const double r[3] = {D.rx[i], D.ry[i], D.rz[i]};
+            need = offsets_check_mixed(D, i, r);
+        }
+    }
+    if (next) flag_need_next(need, A.st);
+}
+
+int launch_forces_step(mdg_system* sys, const PotSet* dps, const PotSet& ps, double dt,
+                       const unsigned long long* left) {
+    if (sys->n == 0) return MDG_OK;
+    mdg_ctx* ctx = sys->ctx;
+    FArgs A = force_args(sys);
+    if (!ps.any_eam || !sys->cutbits || sys->cut_words * 32 < sys->K) {
+        set_error("the step-starting force pass needs an EAM solver and the density pass's cut bits");
+        return MDG_ERR_STATE;
+    }
+    A.cutbits = sys->cutbits;
+    A.kick_hdt = 0.5f * (float)dt;
+    const IArgs D = integrator_args(sys, dt);
+    const int nb = nblk(sys->n);
+    cudaStream_t st = ctx->stream;
+    const bool multi = ps.multi != 0;
+    const int mb = force_blocks(sys, multi);
+    if (multi) {
+        if (mb == 3) k_force_step<true, 3><<<nb, kBlock, 0, st>>>(A, D, dps, left);
+        else k_force_step<true, 4><<<nb, kBlock, 0, st>>>(A, D, dps, left);
+    } else {
+        if (mb == 3) k_force_step<false, 3><<<nb, kBlock, 0, st>>>(A, D, dps, left);
+        else k_force_step<false, 4><<<nb, kBlock, 0, st>>>(A, D, dps, left);
+    }
+    MDG_LAUNCHED(ctx);
+    return MDG_OK;
+}
+
+// The density pass of a step whose force pass moves atoms (k_force_step):
+// as the charge stage, recording the band pairs' FP64 decisions.
+int launch_density_rec(mdg_system* sys, const PotSet* dps, const PotSet& ps) {
+    if (sys->n == 0) return MDG_OK;
+    FArgs A = force_args(sys);
+    if (!sys->cutbits || sys->cut_words * 32 < sys->K) {
+        set_error("the density pass's cut bits are not allocated");
+        return MDG_ERR_STATE;
+    }
+    A.cutbits = sys->cutbits;
+    const int nb = nblk(sys->n);
+    cudaStream_t st = sys->ctx->stream;
+    const bool multi = ps.multi != 0;
+    const int mb = density_blocks(sys, multi);
+    if (multi) {
+        if (mb == 3) k_density_rec<true, 3><<<nb, kBlock, 0, st>>>(A, dps);
+        else if (mb == 5) k_density_rec<true, 5><<<nb, kBlock, 0, st>>>(A, dps);
+        else k_density_rec<true, 4><<<nb, kBlock, 0, st>>>(A, dps);
+    } else {
+        if (mb == 3) k_density_rec<false, 3><<<nb, kBlock, 0, st>>>(A, dps);
+        else if (mb == 5) k_density_rec<false, 5><<<nb, kBlock, 0, st>>>(A, dps);
+        else k_density_rec<false, 4><<<nb, kBlock, 0, st>>>(A, dps);
+    }
+    MDG_LAUNCHED(sys->ctx);
+    sys->fp_ok = 0;  // nc rewritten (FP32 sums); Fp64 no longer matches it
+    return MDG_OK;
+}
+
+// The density pass's cut bits of a system (mdg_system::cutbits), sized for
+// its list capacity; the force pass that starts the next step reads them.
+int ensure_cutbits(mdg_system* sys) {
+    const int words = (sys->K + 31) / 32;
+    if (sys->cutbits && sys->cut_words >= words) return MDG_OK;
+    sys_free(sys, sys->cutbits, (size_t)sys->cut_words * sys->np * sizeof(uint32_t));
+    sys->cutbits = nullptr;
+    sys->cut_words = 0;
+    int rc = sys_malloc(sys, (void**)&sys->cutbits, (size_t)std::max(words, 1) * sys->np * sizeof(uint32_t));
+    if (rc) return rc;
+    sys->cut_words = std::max(words, 1);
+    return MDG_OK;
 }
 
 // stage: 0 = charge (density), 1 = forces (then the thermostat, if any).

@@ -31,6 +31,7 @@ struct FArgs {
     float* Fp32;
     const int4* pos32;  // fixed-point offsets (mdg_internal.cuh)
     int4* pos32b;       // the same offsets with w = bits of the FP32 F'(rho) (EAM)
+    uint32_t* cutbits;  // null, or the density pass's FP64 decisions of band pairs (mdg_system::cutbits)
     double *Ep, *Em;
     double* V[9];
     DevStatus* st;
@@ -143,13 +144,38 @@ __device__ __forceinline__ bool pair_in(const FArgs& A, int i, uint32_t e, float
     return in && (per || !(e & kWrapBit));
 }
 
+// pair_in for the density pass of a step whose force pass moves atoms: the
+// FP64 decisions of the band pairs (entry k of atom i) are also collected in
+// *bits, one bit per entry, and *band notes that the word has one.
+__device__ __forceinline__ bool pair_in_rec(const FArgs& A, int i, uint32_t e, float r2, float r2c, double R2c,
+                                            bool per, int k, uint32_t* bits, bool* band) {
+    bool in = r2 >= 1e-15f && r2 <= r2c;
+    if (fabsf(r2 - r2c) <= 1e-5f * r2c) {
+        in = cut_in(A, i, e & kJMask, r2, r2c, R2c);
+        *bits |= (uint32_t)in << (k & 31);
+        *band = true;
+    }
+    return in && (per || !(e & kWrapBit));
+}
+
+// pair_in for such a force pass: a band pair takes the density pass's FP64
+// decision (the same FP32 r^2 puts it in the band there), so the pass reads
+// no neighbour's FP64 position.
+__device__ __forceinline__ bool pair_in_bits(const FArgs& A, int i, uint32_t e, float r2, float r2c, bool per,
+                                             int k) {
+    bool in = r2 >= 1e-15f && r2 <= r2c;
+    if (fabsf(r2 - r2c) <= 1e-5f * r2c) in = (__ldg(A.cutbits + (size_t)(k >> 5) * A.np + i) >> (k & 31)) & 1u;
+    return in && (per || !(e & kWrapBit));
+}
+
 // The pair loops below read four list entries with one 16-byte load, then
 // the four neighbour records, so the loads of a group overlap; the four
 // contributions are summed in FP32 and the group sum enters a Kahan sum.
 
-template <bool MULTI, bool KICK = false>
-__device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
-    if (A.tag[i] == 0) return;
+template <bool MULTI>
+__device__ __forceinline__ bool lj_mixed_force(const FArgs& A, const PotSet* __restrict__ ps, int i, float& out_x,
+                                             float& out_y, float& out_z) {
+    if (A.tag[i] == 0) return false;
     const int4 pi = A.pos32[i];
     const int ng = A.ncnt[i] >> 2;
     const int ki = MULTI ? (A.kind[i] & 3) : 0;
@@ -191,7 +217,16 @@ __device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __res
         acc.add(1, fy);
         acc.add(2, fz);
     }
-    store_force<KICK>(A, i, acc.s[0], acc.s[1], acc.s[2]);
+    out_x = acc.s[0];
+    out_y = acc.s[1];
+    out_z = acc.s[2];
+    return true;
+}
+
+template <bool MULTI, bool KICK = false>
+__device__ __forceinline__ void lj_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
+    float fx, fy, fz;
+    if (lj_mixed_force<MULTI>(A, ps, i, fx, fy, fz)) store_force<KICK>(A, i, fx, fy, fz);
 }
 
 // Force / r of a tabulated Pair term (pair.cxx:316-346) in FP32 from the
@@ -232,9 +267,10 @@ __device__ __forceinline__ float analytic_ff32(const PotParams& P, float r2) {
 // Pair-type forces (no EAM term) beyond the plain LJsCut kernel: FORM 3 =
 // every pair a tabulated Pair, 4 = every pair LJs, 0 = chosen per kind pair
 // among LJsCut, Pair and LJs.
-template <bool MULTI, int FORM, bool KICK = false>
-__device__ __forceinline__ void pair_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
-    if (A.tag[i] == 0) return;
+template <bool MULTI, int FORM>
+__device__ __forceinline__ bool pair_mixed_force(const FArgs& A, const PotSet* __restrict__ ps, int i, float& out_x,
+                                             float& out_y, float& out_z) {
+    if (A.tag[i] == 0) return false;
     const int4 pi = A.pos32[i];
     const int ng = A.ncnt[i] >> 2;
     const int ki = MULTI ? (A.kind[i] & 3) : 0;
@@ -276,7 +312,16 @@ __device__ __forceinline__ void pair_mixed_one(const FArgs& A, const PotSet* __r
         acc.add(1, fy);
         acc.add(2, fz);
     }
-    store_force<KICK>(A, i, acc.s[0], acc.s[1], acc.s[2]);
+    out_x = acc.s[0];
+    out_y = acc.s[1];
+    out_z = acc.s[2];
+    return true;
+}
+
+template <bool MULTI, int FORM, bool KICK = false>
+__device__ __forceinline__ void pair_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
+    float fx, fy, fz;
+    if (pair_mixed_force<MULTI, FORM>(A, ps, i, fx, fy, fz)) store_force<KICK>(A, i, fx, fy, fz);
 }
 
 __device__ __forceinline__ void embed32(const PotParams& P, float rho, float* F, float* dF,
@@ -293,7 +338,9 @@ __device__ __forceinline__ void embed32(const PotParams& P, float rho, float* F,
     *dF = dcubic(c, u) * P.inv_drh_f;
 }
 
-template <bool MULTI>
+// REC: also record the FP64 decisions of the band pairs in A.cutbits, for a
+// force pass that moves atoms (pair_in_rec).
+template <bool MULTI, bool REC = false>
 __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
     const int4 pi = A.pos32[i];
     const int ki = MULTI ? (A.kind[i] & 3) : 0;
@@ -309,6 +356,8 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
         const float4* tab = P->rho_c;
         const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
         uint4 e4n = ng > 0 ? __ldg(row) : make_uint4(0, 0, 0, 0);
+        uint32_t bits = 0;   // FP64 cut decisions of this word's band entries, for A.cutbits
+        bool band = false;  // the word has a band entry
         for (int g = 0; g < ng; ++g) {
             // the next group's entries are requested before this group's work
             const uint4 e4 = e4n;
@@ -329,7 +378,11 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
                 float dx, dy, dz;
                 pair_vec32(e[q], pi, pj[q], uf, dx, dy, dz);
                 float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                bool in = eam && pair_in(A, i, e[q], r2, r2c, R2c, per);
+                bool in;
+                if (REC)  // every pair's band decision, whatever its potential
+                    in = pair_in_rec(A, i, e[q], r2, r2c, R2c, per, 4 * g + q, &bits, &band) && eam;
+                else
+                    in = eam && pair_in(A, i, e[q], r2, r2c, R2c, per);
                 float t = r2 * rsqrt_nr(fmaxf(r2, 1e-12f)) * idr;
                 int nn = (int)t;
                 in = in && nn < Nr1;
@@ -339,6 +392,11 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
                 part += v;
             }
             ksum_add(s, c, part);
+            if (REC && ((g & 7) == 7 || g + 1 == ng)) {
+                if (band) A.cutbits[(size_t)(g >> 3) * A.np + i] = bits;
+                bits = 0;
+                band = false;
+            }
         }
     }
     float rho = s;
@@ -355,9 +413,14 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
     A.pos32b[i] = make_int4(pi.x, pi.y, pi.z, __float_as_int(Fp0));
 }
 
-template <bool MULTI, bool KICK = false>
-__device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
-    if (A.tag[i] == 0) return;
+// BITS: a pair in the 1e-5 band around the cutoff takes the density pass's
+// FP64 decision (A.cutbits) rather than testing the FP64 positions itself;
+// the force pass then reads no FP64 position of a neighbour (what a force
+// pass that moves its atoms needs).
+template <bool MULTI, bool BITS = false>
+__device__ __forceinline__ bool eam_mixed_force(const FArgs& A, const PotSet* __restrict__ ps, int i, float& out_x,
+                                             float& out_y, float& out_z) {
+    if (A.tag[i] == 0) return false;
     const int4 pi = A.pos32b[i];
     const int ng = A.ncnt[i] >> 2;
     const int ki = MULTI ? (A.kind[i] & 3) : 0;
@@ -399,7 +462,9 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
             float dx, dy, dz;
             pair_vec32(e[q], pi, pj[q], uf, dx, dy, dz);
             float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            bool in = (eam || lj) && pair_in(A, i, e[q], r2, r2c, R2c, per);
+            bool in;
+            if (BITS) in = (eam || lj) && pair_in_bits(A, i, e[q], r2, r2c, per, 4 * g + q);
+            else in = (eam || lj) && pair_in(A, i, e[q], r2, r2c, R2c, per);
             // one reciprocal square root gives both r and 1/r
             float rinv = rsqrt_nr(fmaxf(r2, 1e-12f));
             float r = r2 * rinv;
@@ -424,7 +489,16 @@ __device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __re
         acc.add(1, fy);
         acc.add(2, fz);
     }
-    store_force<KICK>(A, i, acc.s[0], acc.s[1], acc.s[2]);
+    out_x = acc.s[0];
+    out_y = acc.s[1];
+    out_z = acc.s[2];
+    return true;
+}
+
+template <bool MULTI, bool KICK = false>
+__device__ __forceinline__ void eam_mixed_one(const FArgs& A, const PotSet* __restrict__ ps, int i) {
+    float fx, fy, fz;
+    if (eam_mixed_force<MULTI>(A, ps, i, fx, fy, fz)) store_force<KICK>(A, i, fx, fy, fz);
 }
 
 }  // namespace mdg

@@ -59,6 +59,18 @@ __global__ void k_drift_mixed(IArgs A) {
     flag_need(need, A.st);
 }
 
+// The mixed drift as its own pass inside the step loop's graph, where the
+// force pass could not start the step (the first step, after a rebuild):
+// skipped on the device when fewer than min_left steps remain or the
+// rebuild before it outgrew its capacities.
+__global__ void k_drift_mixed_guarded(IArgs A, const unsigned long long* __restrict__ left,
+                                      unsigned long long min_left) {
+    if (*left < min_left || (A.st->build_flags & FLAG_OVERFLOW)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool need = i < A.n ? drift_mixed_one(A, i) : false;
+    flag_need(need, A.st);
+}
+
 __global__ void k_kick_mixed(IArgs A) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < A.n) kick_mixed_one(A, i);
@@ -244,6 +256,14 @@ int launch_drift(mdg_system* sys, double dt, int precision, double pot_rcut, int
     if (precision == MDG_PREC_MIXED && drift) k_drift_mixed<<<nblk(sys->n), kBlock, 0, ctx->stream>>>(A);
     else k_drift64<<<nblk(sys->n), kBlock, 0, ctx->stream>>>(A, drift, check);
     MDG_LAUNCHED(ctx);
+    return MDG_OK;
+}
+
+int launch_drift_guarded(mdg_system* sys, double dt, const unsigned long long* left, unsigned long long min_left) {
+    if (sys->n == 0) return MDG_OK;
+    IArgs A = integrator_args(sys, dt);
+    k_drift_mixed_guarded<<<nblk(sys->n), kBlock, 0, sys->ctx->stream>>>(A, left, min_left);
+    MDG_LAUNCHED(sys->ctx);
     return MDG_OK;
 }
 

@@ -46,6 +46,11 @@ __device__ __forceinline__ void flag_need(bool need, DevStatus* st) {
     if (b && (threadIdx.x & 31) == (__ffs(b) - 1)) atomicOr(&st->need_rebuild, 1u);
 }
 
+__device__ __forceinline__ void flag_need_next(bool need, DevStatus* st) {
+    unsigned b = __ballot_sync(__activemask(), need);
+    if (b && (threadIdx.x & 31) == (__ffs(b) - 1)) atomicOr(&st->need_next, 1u);
+}
+
 // VerletList::decide per atom (verlet-list.cxx:135-154), exact FP64.
 __device__ __forceinline__ bool decide_one(const IArgs& A, int i, double x, double y, double z) {
     if (A.uid[i] != A.saved_uid[i] || A.rcut[i] != A.saved_rcut[i] || A.rns[i] != A.saved_rns[i]) return true;
@@ -103,19 +108,9 @@ __device__ __forceinline__ bool drift64_one(const IArgs& A, int i, int drift, in
 // rcut and rns comparisons of decide cannot change inside the step loop: the
 // drift does not touch those fields, and a host-side change marks the list
 // stale.)
-__device__ __forceinline__ bool drift_mixed_one(const IArgs& A, int i) {
-    double r[3] = {A.rx[i], A.ry[i], A.rz[i]};
-    if (A.tag[i] != 0) {
-        float hm = (0.5f * (float)A.dt) * __frcp_rn((float)A.m[i]);
-        float g[3] = {A.gx[i], A.gy[i], A.gz[i]};
-        double* v[3] = {A.vx, A.vy, A.vz};
-        for (int k = 0; k < 3; ++k) {
-            double vk = v[k][i] + (double)(g[k] * hm);
-            v[k][i] = vk;
-            r[k] = fma(vk, A.dt, r[k]);
-        }
-        A.rx[i] = r[0]; A.ry[i] = r[1]; A.rz[i] = r[2];
-    }
+// The offsets refresh and the rebuild test of drift_mixed_one, for the
+// atom's position r after its drift.
+__device__ __forceinline__ bool offsets_check_mixed(const IArgs& A, int i, const double r[3]) {
     const int4 q = make_int4(off_encode(r[0] - A.Rx[i], A.inv_u[0]), off_encode(r[1] - A.Ry[i], A.inv_u[1]),
                              off_encode(r[2] - A.Rz[i], A.inv_u[2]), 0);
     A.pos32[i] = q;
@@ -132,6 +127,47 @@ __device__ __forceinline__ bool drift_mixed_one(const IArgs& A, int i) {
     double ey = shortest1(dsub(r[1], A.r0y[i]), A.L[1], A.periodic[1]);
     double ez = shortest1(dsub(r[2], A.r0z[i]), A.L[2], A.periodic[2]);
     return skin <= 0.0 || sq3_exact(ex, ey, ez) > dmul(dmul(0.25, skin), skin);
+}
+
+__device__ __forceinline__ bool drift_mixed_one(const IArgs& A, int i) {
+    double r[3] = {A.rx[i], A.ry[i], A.rz[i]};
+    if (A.tag[i] != 0) {
+        float hm = (0.5f * (float)A.dt) * __frcp_rn((float)A.m[i]);
+        float g[3] = {A.gx[i], A.gy[i], A.gz[i]};
+        double* v[3] = {A.vx, A.vy, A.vz};
+        for (int k = 0; k < 3; ++k) {
+            double vk = v[k][i] + (double)(g[k] * hm);
+            v[k][i] = vk;
+            r[k] = fma(vk, A.dt, r[k]);
+        }
+        A.rx[i] = r[0]; A.ry[i] = r[1]; A.rz[i] = r[2];
+    }
+    return offsets_check_mixed(A, i, r);
+}
+
+// The end of a mixed step's force pass when the next step starts in it:
+// the FP32 force stored, this step's second half-kick, then the next
+// step's first half-kick and drift, offsets refresh and rebuild test —
+// kick_mixed_one followed by drift_mixed_one, operation for operation
+// (the same FP32 increment added to v twice, r advanced by fma(v, dt, r)).
+// Returns the rebuild test of the new position.
+__device__ __forceinline__ bool kick_drift_mixed(const IArgs& A, float* gx, float* gy, float* gz, int i, float fx,
+                                                 float fy, float fz) {
+    gx[i] = fx;
+    gy[i] = fy;
+    gz[i] = fz;
+    const float hm = (0.5f * (float)A.dt) * __frcp_rn((float)A.m[i]);
+    const float g[3] = {fx, fy, fz};
+    double* v[3] = {A.vx, A.vy, A.vz};
+    double r[3] = {A.rx[i], A.ry[i], A.rz[i]};
+    for (int k = 0; k < 3; ++k) {
+        double vk = v[k][i] + (double)(g[k] * hm);  // second half-kick of this step
+        vk = vk + (double)(g[k] * hm);               // first half-kick of the next
+        v[k][i] = vk;
+        r[k] = fma(vk, A.dt, r[k]);
+    }
+    A.rx[i] = r[0]; A.ry[i] = r[1]; A.rz[i] = r[2];
+    return offsets_check_mixed(A, i, r);
 }
 
 __device__ __forceinline__ void kick_mixed_one(const IArgs& A, int i) {

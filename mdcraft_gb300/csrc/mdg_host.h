@@ -156,6 +156,14 @@ struct mdg_system {
     uint32_t* nbr = nullptr;
     uint32_t* ncnt = nullptr;
     int K = 0;        // capacity per atom (self excluded)
+    // the mixed density pass's FP64 cut decisions of the pairs in the band
+    // around the cutoff, one bit per list entry (word w of atom i at
+    // cutbits[w * np + i], written when the word holds such a pair), for a
+    // force pass that starts the next step and so must not read positions it
+    // moves; cut_words words per atom, allocated by the step loop that uses
+    // them
+    uint32_t* cutbits = nullptr;
+    int cut_words = 0;
     int half = 0;
     int have_list = 0;
     uint64_t rebuilds = 0;

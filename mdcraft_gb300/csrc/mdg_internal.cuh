@@ -200,6 +200,8 @@ struct DevStatus {
     uint32_t build_flags;   // FLAG_* raised by the current rebuild
     uint32_t pad[2];
     uint32_t therm_calls;   // thermostat applications so far (Philox counter word)
+    uint32_t need_next;     // rebuild test of the next step's positions, from a force pass
+                            // that ran the next step's first half-kick and drift
 };
 
 }  // namespace mdg

@@ -130,3 +130,38 @@ def test_graph_prologue_rebuilds_after_upload(make):
     assert ra == rb and ra >= 1
     for k in ("r", "v", "f"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def _tagged(make):
+    def f():
+        atoms, box, per, p = make()
+        atoms["tag"][::17] = 0  # held in place: no kick, no drift (verlet.cxx:36-85)
+        return atoms, box, per, p
+    return f
+
+
+@pytest.mark.parametrize("make", [_tagged(lambda: W.eam_cu_fcc(ncell=8, T=3000.0)),
+                                  _tagged(lambda: W.lj_argon_fcc(ncell=6, T=600.0, jitter=0.01)),
+                                  lambda: W.eam_nial_b2(ncell=8, T=3000.0)],
+                         ids=["eam_hot_tagged", "lj_hot_tagged", "nial_multi_hot"])
+def test_step_loop_equals_stepwise_api(make):
+    """mdg_run's mixed step loop starts each next step inside the force pass
+    (its epilogue runs the next half-kick, drift, offsets refresh and rebuild
+    test); the stepwise API (make_step, decide, update) runs those as passes
+    of their own. Same bits, rebuilds included."""
+    atoms, p, a = _pair(make, "mixed")
+    a["stepper"].run(a["sys"], p["dt"], 40)
+    ref = a["sys"].download()
+    _, _, b = _pair(make, "mixed")
+    for _ in range(40):
+        b["stepper"].make_step(b["sys"], p["dt"])
+        if b["nl"].decide():
+            b["nl"].update(-1.0)
+    got = b["sys"].download()
+    assert b["nl"].rebuilds() == a["nl"].rebuilds() >= 2
+    assert np.array_equal(got["r"], ref["r"])
+    assert np.array_equal(got["v"], ref["v"])
+    assert np.array_equal(got["f"], ref["f"])
+    frozen = np.asarray(atoms["tag"]) == 0
+    if frozen.any():
+        assert np.array_equal(ref["v"][frozen], np.asarray(atoms["v"])[frozen])
