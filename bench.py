@@ -186,7 +186,7 @@ def peaks():
 # ncu summary of the dominant kernel (committed under profiles/): its DRAM
 # bytes of one launch and the atoms that launch processed give the traffic
 # per atom; its L1 figure names what limits the kernel
-FORCE_PROFILE = os.path.join(ROOT, "profiles", "k_eam_mixed_eam_cu_442k.md")
+FORCE_PROFILE = os.path.join(ROOT, "profiles", "k_force_step_eam_cu_442k.md")
 
 
 def profile_figures(path):
@@ -420,21 +420,29 @@ def run_mdg(args, rank, world, local):
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e = dist.sum(float(n) * args.e2e_steps) / e2e_s
 
-    # roofline of the dominant kernel (EAM force, mixed, with the step's second
-    # half-kick fused in): compulsory bytes per atom = own offsets+F' (16) +
-    # list count (4) + list entries (4 L) + FP32 force (12) + kick: mass (8),
-    # velocity read and write (48)
-    bytes_atom = 32.0 + 4.0 * L + 56.0
+    # roofline of the dominant kernel (k_force_step: the EAM force pass, mixed,
+    # with the step's second half-kick and, on every step that needs no
+    # rebuild and is not the last, the next step's first half-kick and drift):
+    # compulsory bytes per atom = own offsets+F' (16) + list count (4) + list
+    # entries (4 L) + FP32 force (12) + kick: mass (8), velocity read and
+    # write (48); + on the steps it starts the next one: position read and
+    # write (48), cell centre (24), rebuild-time offsets (16) and threshold
+    # (8), new offsets (16) = 112. Its launches in the timed stepwise run:
+    # fn, of which all but the rebuild steps and the last started the next.
+    started = max(fn - rn - 1, 0) / max(fn, 1)
+    bytes_atom = 32.0 + 4.0 * L + 56.0 + 112.0 * started
     force_launch_ms = fms / max(fn, 1)
     achieved = bytes_atom * n / (force_launch_ms / 1e3) / 1e9
     pk = peaks()
     peak = pk.get("hbm_gbs", 6800.0)
     prof = profile_figures(FORCE_PROFILE)
-    roof = {"bound": "hbm", "kernel": "k_eam_mixed (EAM force, mixed, with the second half-kick)",
+    roof = {"bound": "hbm",
+            "kernel": "k_force_step (EAM force, mixed, with the second half-kick and the next step's start)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": (prof["bytes"] / prof["atoms"] * n) if prof else None,
             "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
-            "bytes_per_atom": bytes_atom, "launch_ms": force_launch_ms}
+            "bytes_per_atom": bytes_atom, "launch_ms": force_launch_ms,
+            "launches_starting_next_step": started}
     if prof:
         roof["traffic_source"] = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on "
                                   f"{prof['atoms']:,} atoms ({prof['file']}), scaled to {n:,} atoms")
