@@ -81,6 +81,8 @@ def lib():
         "mdg_nlist_list_for": ([vp, vp, vp, sz, C.POINTER(C.c_size_t)], ip),
         "mdg_nlist_sort": ([vp, vp, sz, vp], ip),
         "mdg_nlist_grid": ([vp, vp, vp], ip), "mdg_nlist_rebuilds": ([vp, u64p], ip),
+        "mdg_grid_build": ([vp, vp, vp], ip),
+        "mdg_pot_atom": ([vp, vp, ip, vp, vp, sz, vp, sz, ip], ip),
         "mdg_pot_ljcut_create": ([dp, dp, dp, pp], ip),
         "mdg_pot_eam_create": ([dp, vp, vp, vp, ip, dp, ip, dp, pp], ip),
         "mdg_pot_eam_create_from_file": ([C.c_char_p, pp], ip), "mdg_pot_destroy": ([vp], ip),
@@ -231,6 +233,16 @@ class System:
         out = np.zeros((self.n, 3)) if arr is None else np.ascontiguousarray(arr, dtype=np.float64)
         _check(fn(self.h, _ptr(out)))
         return out
+
+    def grid_build(self) -> dict:
+        """Grid::build (grid.cxx:43-95) over the system's atoms, on the device
+        and without a list (positions are wrapped into the period as by a
+        rebuild)."""
+        ints = np.zeros(9, dtype=np.int32)
+        dbl = np.zeros(3)
+        _check(lib().mdg_grid_build(self.h, _ptr(ints), _ptr(dbl)))
+        return {"domain_num_cells": ints[0:3], "grid_offset": ints[3:6], "num_cells": ints[6:9],
+                "cell_sizes": dbl}
 
     def positions(self):
         return self._vec(lib().mdg_system_get_positions)
