@@ -45,7 +45,8 @@ struct GridParams {
     int bricks[3];     // ceil(num / 4)
     int dim;
     int periodic[3];
-    int small_box;     // some periodic axis has <= 3 cells: exact FP64 neighbour test only
+    int small_box;     // some periodic axis has <= 2 cells, or a local grid short of it: the per-atom
+                       // build with per-pair minimum-image codes and the exact FP64 test only
     int ncells;
     int nbins;         // 64 * bricks product
     int empty;

@@ -72,8 +72,14 @@ __host__ __device__ inline void grid_from_bounds(const DomainDev& d, const doubl
         g.csf[i] = (float)g.cs[i];
         g.Lf[i] = (float)d.size[i];
         g.inv_u[i] = g.cs[i] > 0.0 ? kOffUnits / g.cs[i] : 0.0;
+        // A periodic axis of 3 cells keeps the fast paths: its cells are at
+        // least max rns wide (floor(L / rns) = 3), so every listed pair is
+        // nearer than L / 2 and the image of its neighbour cell is the
+        // minimum image (no per-pair adjustment, the FP32 prefilter holds).
+        // One or two cells per axis (the reference's n = 1, 2 rules), or a
+        // local grid short of the periodic box, take the per-atom body.
         if (d.periodic[i] && i < d.dim &&
-            (g.dom_n[i] <= 3 || g.offset[i] != 0 || g.num[i] != g.dom_n[i]))
+            (g.dom_n[i] <= 2 || g.offset[i] != 0 || g.num[i] != g.dom_n[i]))
             g.small_box = 1;
         if (g.num[i] < 1 || g.num[i] > 1023) g.empty = -2;
     }
@@ -372,8 +378,8 @@ __device__ __forceinline__ void nbuild_bin(const NbArgs& A, const GridParams& g,
 // matrix and appends those candidates in lane order.
 // Entry order per atom is therefore the order of the per-atom loop in
 // nbuild_bin, and the lists are the same, entry for entry. Used when no
-// periodic axis has 3 cells or fewer (no minimum-image adjustment of the
-// image code); otherwise nbuild_bin runs.
+// periodic axis has 2 cells or fewer (no minimum-image adjustment of the
+// image code, GridParams::small_box); otherwise nbuild_bin runs.
 struct NbWarpSmem {
     uint32_t cj0[27];        // first slot of each non-empty neighbour cell
     uint32_t cpre[28];       // candidate prefix over those cells

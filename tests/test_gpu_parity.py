@@ -225,6 +225,11 @@ def _cases():
     cases.append(("nial_b2_2000", atoms, box, (1, 1, 1), p))
     atoms, box, per, p = W.eam_cu_fcc(ncell=4)  # 2 cells per axis: n=2 rules
     cases.append(("eam_cu_small_256", atoms, box, (1, 1, 1), p))
+    # 3 cells per periodic axis (the warp build with cell images)
+    atoms, box, per, p = W.eam_cu_fcc(ncell=6, T=900.0, jitter=0.03)
+    cases.append(("eam_cu_3cells_864", atoms, box, (1, 1, 1), p))
+    atoms, box, per, p = W.eam_nial_b2(ncell=8)
+    cases.append(("nial_b2_3cells_1024", atoms, box, (1, 1, 1), p))
     rng = np.random.default_rng(7)
     g = W.new_atoms(3000)
     g["r"] = rng.random((3000, 3)) * 6.0
@@ -236,6 +241,11 @@ def _cases():
     g2 = g.copy()
     g2["r"][:, 2] = 0.0
     cases.append(("gas_2d_periodic_x", g2, (0.0, 6.0, 0.0, 6.0, 0.0, 0.0), (1, 0, 0), None))
+    # one periodic axis of 3 cells with rns equal to a third of it, open axes
+    g3 = g.copy()
+    g3["r"][:, 0] = rng.random(3000) * 1.5
+    g3["rns"] = 0.5
+    cases.append(("gas_3cells_periodic_x_rns_third", g3, (0.0, 1.5, 0.0, 6.0, 0.0, 6.0), (1, 0, 0), None))
     return cases
 
 

@@ -75,13 +75,16 @@ def test_result_same_alone_and_in_mix():
         assert _same(outs[k], _direct(specs[k], solv)), f"request {k}"
 
 
-def test_small_boxes_two_cells_per_dimension():
+@pytest.mark.parametrize("dims", [(4, 4, 4), (6, 6, 8)], ids=["2_cells", "3_cells"])
+def test_small_boxes_two_cells_per_dimension(dims):
     """The smallest requests (4^3 fcc cells, 2 grid cells per dimension: the
-    reference's n = 2 rule): mixed forces within the bar of the FP64 ones on
-    the same positions, and mixed vs FP64 runs through the server."""
+    reference's n = 2 rule; 6x6x8 cells, 3 grid cells on two axes): mixed
+    forces within the bar of the FP64 ones on the same positions, and mixed
+    vs FP64 runs through the server."""
     _ensure_built()
     from tests import gpu_helpers as H
-    specs = [dict(index=0, kind=k, dims=(4, 4, 4), n=256, t_arrival=0.0, steps=40, dt=p["dt"], seed=77 + j)
+    n = 4 * dims[0] * dims[1] * dims[2]
+    specs = [dict(index=0, kind=k, dims=dims, n=n, t_arrival=0.0, steps=40, dt=p["dt"], seed=77 + j)
              for j, (k, p) in enumerate((("lj", W.SERVE_LJ), ("eam", W.SERVE_EAM)))]
     s64, smx = SV.solvers("fp64"), SV.solvers("mixed")
     for spec in specs:
@@ -99,7 +102,7 @@ def test_small_boxes_two_cells_per_dimension():
         s.close()
     out = {}
     for prec, solv in (("fp64", s64), ("mixed", smx)):
-        srv = mdg.Server(slots=2, max_atoms=1024)
+        srv = mdg.Server(slots=2, max_atoms=max(1024, n))
         reqs = SV.prepare(specs)
         ids = [srv.submit(solv[s["kind"]], d, a, s["dt"], s["steps"]) for s, a, d in reqs]
         for k, rid in enumerate(ids):
