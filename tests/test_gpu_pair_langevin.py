@@ -295,3 +295,38 @@ def test_langevin_mixed_tracks_fp64_and_changes_with_parameters():
     st.run(g["sys"], 0.002, 5)
     assert lg.temperature() == 3000.0
     assert not np.array_equal(r_cold, g["sys"].positions())
+
+
+def test_multi_mixed_step_loop_equals_stepwise():
+    """A mixed Multi with EAM, LJs and Pair terms: mdg_run's graph (whose force
+    pass starts the next step, taking the band pairs' cut decisions of every
+    potential type from the density pass) gives the bits of the stepwise API
+    (make_step, decide, update), rebuilds included."""
+    al = S.al2009()
+    t = S.nialpair()
+    pots = {(0, 0): ("eam", al), (1, 1): ("ljs", LJS), (0, 1): ("pair", t)}
+    atoms, box = _fcc(5, 0.405, 13)
+    atoms["kind"] = (np.arange(len(atoms)) % 3 == 1).astype(np.uint16)
+    atoms["v"] *= 3.0
+    rc = max(al["rcut"], t["rcut"], LJS[2])
+    runs = []
+    for stepwise in (False, True):
+        _, g = _build(atoms, box, pots, rc, precision="mixed")
+        g["nl"].update(-1.0)
+        g["solver"].prepare(g["sys"])
+        g["solver"].stages(g["sys"])
+        st = mdg.Verlet(g["solver"])
+        rb0 = g["nl"].rebuilds()
+        if stepwise:
+            for _ in range(30):
+                st.make_step(g["sys"], 0.002)
+                if g["nl"].decide():
+                    g["nl"].update(-1.0)
+        else:
+            st.run(g["sys"], 0.002, 30)
+        runs.append((g["sys"].download(), g["nl"].rebuilds() - rb0))
+    (a, ra), (b, rb) = runs
+    assert ra == rb and ra >= 1
+    assert np.array_equal(a["r"], b["r"])
+    assert np.array_equal(a["v"], b["v"])
+    assert np.array_equal(a["f"], b["f"])
