@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--serve-block-threads", type=int, default=0,
                     help="threads of the fused per-system block (256, 512, 1024; 0: chosen by the autotuner "
                          "on a sample of the stream; -1: a graph loop per request)")
-    ap.add_argument("--serve-order", default="fifo", choices=["fifo", "largest"],
+    ap.add_argument("--serve-order", default="balanced", choices=["fifo", "largest", "balanced"],
                     help="admission order of waiting requests in the serving stream")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="only the serving stream (prints its summary)")

@@ -371,12 +371,16 @@ typedef struct mdg_server_config {
                            <= 65536 atoms): its threads (256, 512, 1024), 0 = the default
                            (1024), -1 = off (a graph loop per request instead) */
     int order;          /* admission order of waiting requests: MDG_ORDER_FIFO (0, the
-                           default) or MDG_ORDER_LARGEST (most atom-steps first, which
+                           default), MDG_ORDER_LARGEST (most atom-steps first, which
                            shortens the tail of a backlog at the cost of small requests'
-                           latency) */
+                           latency) or MDG_ORDER_BALANCED (arrival order, except that the
+                           largest waiting request goes first once its atom-steps reach
+                           the waiting atom-steps per worker, a block of the fused loop or
+                           else a slot: largest-first for the end of a backlog only) */
 } mdg_server_config;
 #define MDG_ORDER_FIFO 0
 #define MDG_ORDER_LARGEST 1
+#define MDG_ORDER_BALANCED 2
 
 typedef struct mdg_request_info {
     int status;         /* MDG_OK or the error that ended the request */

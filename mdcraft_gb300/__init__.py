@@ -671,18 +671,20 @@ class Server:
     Each request is a whole driver loop (``steps`` velocity-Verlet steps with
     the list rebuilt on decide()) over its own atoms, domain and solver. Up to
     ``slots`` requests run at once, each on its own stream, admitted in FIFO
-    order (or largest first) as slots and device memory (``hbm_budget``
-    bytes) free up.
+    order (or largest first, or largest first on the tail of a backlog) as
+    slots and device memory (``hbm_budget`` bytes) free up.
     """
 
-    ORDERS = {"fifo": 0, "largest": 1}
+    ORDERS = {"fifo": 0, "largest": 1, "balanced": 2}
 
     def __init__(self, device: int = 0, slots: int = 16, hbm_budget: int = 0, max_atoms: int = 1 << 16,
                  block_threads: int = 0, order: str = "fifo"):
         """block_threads: threads of the fused per-request block (256, 512, 1024; 0 = 1024);
         -1 runs every request as a graph loop on its slot's stream instead. order: "fifo"
         admits waiting requests in arrival order, "largest" the one with the most
-        atom-steps first."""
+        atom-steps first, "balanced" in arrival order except that the largest
+        waiting request goes first once its atom-steps reach the waiting
+        atom-steps per block of the fused kernel (per request slot without it)."""
         cfg = _ServerConfig(slots, hbm_budget, max_atoms, block_threads, self.ORDERS[order])
         h = C.c_void_p()
         _check(lib().mdg_server_create(device, C.byref(cfg), C.byref(h)))

@@ -64,6 +64,9 @@ struct Request {
     double t_graph_start = 0.0;  // server clock at the latest admission to a graph loop
 };
 
+// A request's work for the admission order: atoms x steps.
+inline double work_of(const Request* r) { return (double)r->atoms.size() * (double)r->steps; }
+
 // IDLE -> ALLOC (buffers requested) -> BLOCK (queued or running in a block)
 // -> finished, or IDLE -> RUN (graph loop enqueued) -> COPY (result copy
 // enqueued) -> finished.
@@ -125,6 +128,7 @@ struct mdg_server {
     std::deque<AllocGroup> alloc_groups;
     std::vector<cudaEvent_t> free_events;
     std::deque<Request*> queue;
+    double queued_work = 0;        // atom-steps of the requests in `queue`
     std::unordered_map<uint64_t, Request*> reqs;
     std::deque<uint64_t> finished;
     uint64_t next_id = 1;
@@ -474,21 +478,30 @@ int progress(mdg_server* sv) {
     if (!sv->spent_execs.empty() &&
         ((sv->queue.empty() && running_of(sv) == 0) || sv->spent_execs.size() >= kMaxSpentGraphs))
         destroy_spent(sv);
-    // Admission in FIFO order (or, with MDG_ORDER_LARGEST, the largest
-    // waiting request first); the chosen request waits for memory rather
-    // than being overtaken
+    // Admission in FIFO order; with MDG_ORDER_LARGEST the largest waiting
+    // request first; with MDG_ORDER_BALANCED the largest first only while
+    // its atom-steps are at least the waiting atom-steps per worker (the
+    // persistent kernel's blocks, or the request slots without it): once
+    // the backlog is short enough that it would otherwise run on alone at
+    // the end (longest-first on the tail, the rule that bounds a schedule's
+    // makespan). The chosen request waits for memory rather than being
+    // overtaken.
     AllocGroup group;
     for (Slot& sl : sv->slots) {
         if (sv->queue.empty()) break;
         if (sl.req) continue;
         auto pick = sv->queue.begin();
-        if (sv->order == MDG_ORDER_LARGEST)
+        if (sv->order != MDG_ORDER_FIFO) {
+            auto largest = sv->queue.begin();
             for (auto it = sv->queue.begin(); it != sv->queue.end(); ++it)
-                if ((*it)->atoms.size() * (size_t)(*it)->steps > (*pick)->atoms.size() * (size_t)(*pick)->steps)
-                    pick = it;
+                if (work_of(*it) > work_of(*largest)) largest = it;
+            const double per = sv->block_threads >= 0 ? (double)sv->blocks : (double)sv->slots.size();
+            if (sv->order == MDG_ORDER_LARGEST || work_of(*largest) * per >= sv->queued_work) pick = largest;
+        }
         Request* r = *pick;
         if (sv->used + r->footprint > sv->budget && sv->used > 0) break;
         sv->queue.erase(pick);
+        sv->queued_work = sv->queue.empty() ? 0.0 : sv->queued_work - work_of(r);
         charge(sv, sl, r);
         if (!block_mode(sv, r)) {
             admit_graph(sv, sl, r, 0);
@@ -598,7 +611,8 @@ int mdg_server_create(int device, const mdg_server_config* cfg, mdg_server** out
     if (cfg->block_threads > 0 && cfg->block_threads != 256 && cfg->block_threads != 512 &&
         cfg->block_threads != 1024)
         return MDG_ERR_INVALID;
-    if (cfg->order != MDG_ORDER_FIFO && cfg->order != MDG_ORDER_LARGEST) return MDG_ERR_INVALID;
+    if (cfg->order != MDG_ORDER_FIFO && cfg->order != MDG_ORDER_LARGEST && cfg->order != MDG_ORDER_BALANCED)
+        return MDG_ERR_INVALID;
     *out = nullptr;
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
@@ -740,6 +754,7 @@ int mdg_server_submit(mdg_server* srv, mdg_solver* solver, const mdg_domain* dom
         return MDG_OK;
     }
     srv->queue.push_back(r);
+    srv->queued_work += work_of(r);
     return MDG_OK;
 }
 

@@ -280,3 +280,47 @@ def test_largest_first_order_and_service_time(block_threads):
     for k in range(len(specs)):
         svc = infos[k]["service_s"]
         assert 0.0 < svc <= infos[k]["t_done"] - infos[k]["t_submit"] + 1e-3
+
+
+def _balanced_order(works, first, per):
+    """The admission rule of MDG_ORDER_BALANCED restated: after the first
+    admissions, the largest waiting request (the earliest of equals) goes
+    first when its work times `per` (the workers) is at least the waiting
+    work, else the earliest waiting request."""
+    queue = [k for k in range(len(works)) if k not in first]
+    out = list(first)
+    while queue:
+        largest = max(queue, key=lambda k: works[k])
+        pick = largest if works[largest] * per >= sum(works[k] for k in queue) else queue[0]
+        queue.remove(pick)
+        out.append(pick)
+    return out
+
+
+def test_balanced_order_promotes_the_largest_on_the_tail():
+    """MDG_ORDER_BALANCED on two graph-loop slots (no fused kernel, so the
+    workers are the slots): arrival order until the largest waiting request
+    holds at least half the waiting atom-steps, then that one; results stay
+    the single-system driver loop's."""
+    _ensure_built()
+    solv = SV.solvers("mixed")
+    specs = W.serving_stream(count=10, rate=1e9, seed=20, steps=100, n_min=256, n_max=4000)
+    reqs = SV.prepare(specs)
+    srv = mdg.Server(slots=2, max_atoms=8192, block_threads=-1, order="balanced")
+    ids = [srv.submit(solv[s["kind"]], dom, atoms, s["dt"], s["steps"]) for s, atoms, dom in reqs]
+    infos = {}
+    for k, rid in enumerate(ids):
+        srv.wait(rid, 300.0)
+        out, infos[k] = srv.result(rid)
+        assert infos[k]["status"] == 0
+        if k in (1, 7):
+            assert _same(out, _direct(specs[k], solv)), f"request {k}"
+    srv.close()
+    order = sorted(range(len(specs)), key=lambda k: infos[k]["t_admit"])
+    # every request was queued before the third admission
+    assert max(i["t_submit"] for i in infos.values()) < infos[order[2]]["t_admit"]
+    works = [s["n"] * s["steps"] for s in specs]
+    assert order == _balanced_order(works, order[:2], 2)
+    # on this stream the rule is neither arrival order nor largest-first
+    assert order[2:] != sorted(order[2:])
+    assert [works[k] for k in order[2:]] != sorted((works[k] for k in order[2:]), reverse=True)
