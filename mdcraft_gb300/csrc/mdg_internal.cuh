@@ -46,7 +46,8 @@ struct GridParams {
     int dim;
     int periodic[3];
     int small_box;     // some periodic axis has <= 2 cells, or a local grid short of it: the per-atom
-                       // build with per-pair minimum-image codes and the exact FP64 test only
+                       // build with per-pair minimum-image codes (FP32 prefilter on a whole grid,
+                       // the exact FP64 test for every candidate on a local grid short of the box)
     int ncells;
     int nbins;         // 64 * bricks product
     int empty;

@@ -361,7 +361,8 @@ __global__ void __launch_bounds__(kExportWarps * 32)
 
 // Block of NW warps (cells per block: a system's launch shape, default 4),
 // a warp per bin; bins of grids with a periodic axis of 2 cells or fewer
-// (GridParams::small_box) take the per-atom body. 64 registers.
+// (GridParams::small_box) take the per-atom body (FP32 prefilter with a
+// per-pair minimum image). 64 registers.
 template <int NW>
 __global__ void __launch_bounds__(NW * 32, 32 / NW) k_nbuild_warp(NbArgs A, const GridParams* __restrict__ gp) {
     __shared__ GridParams g;

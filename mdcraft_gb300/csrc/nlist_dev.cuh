@@ -77,7 +77,8 @@ __host__ __device__ inline void grid_from_bounds(const DomainDev& d, const doubl
         // nearer than L / 2 and the image of its neighbour cell is the
         // minimum image (no per-pair adjustment, the FP32 prefilter holds).
         // One or two cells per axis (the reference's n = 1, 2 rules), or a
-        // local grid short of the periodic box, take the per-atom body.
+        // local grid short of the periodic box, take the per-atom body,
+        // whose prefilter takes a per-pair minimum image.
         if (d.periodic[i] && i < d.dim &&
             (g.dom_n[i] <= 2 || g.offset[i] != 0 || g.num[i] != g.dom_n[i]))
             g.small_box = 1;
@@ -248,6 +249,16 @@ __device__ __forceinline__ bool are_neibs_exact(const GridParams& g, double xa, 
     return sq3_exact(drx, dry, drz) <= d2;
 }
 
+// The nearest image of a displacement d on a periodic axis of length L,
+// for |d| < 1.5 L (the offsets of binned atoms are within half a cell of
+// their cell centres, so one shift suffices on axes of one or two cells).
+__device__ __forceinline__ float min_image_f(float d, float L) {
+    const float half = 0.5f * L;
+    if (d > half) return d - L;
+    if (d < -half) return d + L;
+    return d;
+}
+
 // The list of every atom of one bin (cell), one lane per atom, `width`
 // lanes per cell (a cell holds ~10-20 atoms, so two cells share a warp): the
 // 27 (or fewer, on small periodic axes) neighbour cells in the reference's
@@ -266,7 +277,19 @@ __device__ __forceinline__ void nbuild_bin(const NbArgs& A, const GridParams& g,
     if (g.dim < 2) gc[1] = 0;
     bool edge[3] = {false, false, false};
     for (int a = 0; a < g.dim; ++a) edge[a] = gc[a] == 0 || gc[a] == g.num[a] - 1;
-    const bool prefilter = uniform_rns && !g.small_box;
+    // The FP32 prefilter also holds on periodic axes of one or two cells
+    // when the grid covers the whole box: every cell there is an edge cell,
+    // so the exact test takes the minimum image, and the FP32 minimum image
+    // of the neighbour cell's displacement is the same distance to ~1e-6 of
+    // r^2, inside the band that goes to FP64. A local grid short of the box
+    // keeps the FP64 test for every candidate.
+    bool mi[3] = {false, false, false};
+    bool whole = true;
+    for (int a = 0; a < g.dim; ++a) {
+        mi[a] = g.periodic[a] && g.dom_n[a] <= 2;
+        if (g.periodic[a] && (g.offset[a] != 0 || g.num[a] != g.dom_n[a])) whole = false;
+    }
+    const bool prefilter = uniform_rns && whole;
 
     for (uint32_t base = s0; base < s1; base += width) {
         uint32_t i = base + lane;
@@ -314,7 +337,10 @@ __device__ __forceinline__ void nbuild_bin(const NbArgs& A, const GridParams& g,
                         float dx = oi.x - oj.x - sh[0];
                         float dy = oi.y - oj.y - sh[1];
                         float dz = oi.z - oj.z - sh[2];
-                        float d2 = dx * dx + dy * dy + dz * dz;
+                        const float ex = mi[0] ? min_image_f(dx, g.Lf[0]) : dx;
+                        const float ey = mi[1] ? min_image_f(dy, g.Lf[1]) : dy;
+                        const float ez = mi[2] ? min_image_f(dz, g.Lf[2]) : dz;
+                        float d2 = ex * ex + ey * ey + ez * ez;
                         bool acc;
                         if (prefilter && oi.w == 0.0f && oj.w == 0.0f && d2 < lo2) {
                             acc = true;
