@@ -360,9 +360,8 @@ __global__ void __launch_bounds__(kExportWarps * 32)
 // ---------------------------------------------------------------------------
 
 // Block of NW warps (cells per block: a system's launch shape, default 4),
-// a warp per bin; bins of grids with a periodic axis of 2 cells or fewer
-// (GridParams::small_box) take the per-atom body (FP32 prefilter with a
-// per-pair minimum image). 64 registers.
+// a warp per bin, on grids without a periodic axis of 2 cells or fewer
+// (GridParams::small_box; those take k_nbuild_atoms). 64 registers.
 template <int NW>
 __global__ void __launch_bounds__(NW * 32, 32 / NW) k_nbuild_warp(NbArgs A, const GridParams* __restrict__ gp) {
     __shared__ GridParams g;
@@ -371,10 +370,20 @@ __global__ void __launch_bounds__(NW * 32, 32 / NW) k_nbuild_warp(NbArgs A, cons
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int bin = blockIdx.x * NW + warp;
-    if (g.empty || bin >= g.nbins) return;
-    const bool uniform = A.st->nonuniform == 0;
-    if (g.small_box) nbuild_bin(A, g, bin, lane, uniform, 32);
-    else nbuild_cell_warp(A, g, bin, lane, uniform, S[warp]);
+    if (g.empty || g.small_box || bin >= g.nbins) return;
+    nbuild_cell_warp(A, g, bin, lane, A.st->nonuniform == 0, S[warp]);
+}
+
+// The list build of grids with a periodic axis of 2 cells or fewer (a few
+// cells of many atoms): a thread per atom. Launched after k_nbuild_warp;
+// each of the two returns at once on the other's grids.
+__global__ void __launch_bounds__(kBlock) k_nbuild_atoms(NbArgs A, const GridParams* __restrict__ gp) {
+    __shared__ GridParams g;
+    if (threadIdx.x == 0) g = *gp;
+    __syncthreads();
+    if (g.empty || !g.small_box) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < (uint32_t)A.n) nbuild_atom(A, g, i, A.st->nonuniform == 0);
 }
 
 // VerletList::optimize_search_radius (verlet-list.cxx:72-92):
@@ -731,6 +740,8 @@ int nlist_enqueue(mdg_system* sys) {
     if (cpb == 2) k_nbuild_warp<2><<<nbw, 2 * 32, 0, st>>>(A, sys->dgrid);
     else if (cpb == 8) k_nbuild_warp<8><<<nbw, 8 * 32, 0, st>>>(A, sys->dgrid);
     else k_nbuild_warp<4><<<nbw, 4 * 32, 0, st>>>(A, sys->dgrid);
+    MDG_LAUNCHED(ctx);
+    k_nbuild_atoms<<<nblk(n), kBlock, 0, st>>>(A, sys->dgrid);
     MDG_LAUNCHED(ctx);
     return MDG_OK;
 }

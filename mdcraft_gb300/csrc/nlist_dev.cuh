@@ -249,6 +249,42 @@ __device__ __forceinline__ bool are_neibs_exact(const GridParams& g, double xa, 
     return sq3_exact(drx, dry, drz) <= d2;
 }
 
+// The grid covers every cell of each periodic axis (no local grid short of
+// the box).
+__device__ __forceinline__ bool grid_whole(const GridParams& g) {
+    for (int a = 0; a < g.dim; ++a)
+        if (g.periodic[a] && (g.offset[a] != 0 || g.num[a] != g.dom_n[a])) return false;
+    return true;
+}
+
+// Image code of a listed pair (list entry bits above kJBits): per axis the
+// cell offset of j's image seen from i's cell (own), from the neighbour
+// cell's offset dl, moved by a period on axes of 3 cells or fewer when the
+// FP32 displacement (dx, dy, dz: i minus the neighbour cell's image of j)
+// says the other image is nearer; bit 6 when the image crossed a periodic
+// face (the offset differs from the local cells' difference lc - own).
+__device__ __forceinline__ uint32_t pair_image_code(const GridParams& g, const int own[3], const int lc[3],
+                                                    const int dl[3], float dx, float dy, float dz,
+                                                    DevStatus* st) {
+    uint32_t code = 0;
+    for (int a = 0; a < 3; ++a) {
+        int dlt = dl[a];
+        if (g.periodic[a] && a < g.dim && g.dom_n[a] <= 3) {
+            float dd = -(a == 0 ? dx : a == 1 ? dy : dz);
+            float half = 0.5f * g.Lf[a];
+            if (dd > half) dlt -= g.dom_n[a];
+            else if (dd < -half) dlt += g.dom_n[a];
+        }
+        if (dlt < -1 || dlt > 1) {
+            atomicOr(&st->flags, FLAG_IMAGE);
+            dlt = dlt < -1 ? -1 : 1;
+        }
+        code |= (uint32_t)(dlt + 1) << (2 * a);
+        if (dlt != lc[a] - own[a]) code |= 1u << 6;
+    }
+    return code;
+}
+
 // The nearest image of a displacement d on a periodic axis of length L,
 // for |d| < 1.5 L (the offsets of binned atoms are within half a cell of
 // their cell centres, so one shift suffices on axes of one or two cells).
@@ -259,141 +295,104 @@ __device__ __forceinline__ float min_image_f(float d, float L) {
     return d;
 }
 
-// The list of every atom of one bin (cell), one lane per atom, `width`
-// lanes per cell (a cell holds ~10-20 atoms, so two cells share a warp): the
-// 27 (or fewer, on small periodic axes) neighbour cells in the reference's
-// order.
-__device__ __forceinline__ void nbuild_bin(const NbArgs& A, const GridParams& g, int bin, int lane,
-                                           bool uniform_rns, int width) {
+// The list of atom i (one thread per atom, over the whole grid: used for
+// grids with a periodic axis of 2 cells or fewer, which have few cells of
+// many atoms each): its cell's 27 (or fewer, on small periodic axes)
+// neighbour cells in the reference's order, x outer, z inner, each cell's
+// atoms in slot order. The FP32 prefilter also holds on periodic axes of
+// one or two cells when the grid covers the whole box: every cell there is
+// an edge cell, so the exact test takes the minimum image, and the FP32
+// minimum image of the neighbour cell's displacement is the same distance
+// to ~1e-6 of r^2, inside the band that goes to FP64. A local grid short of
+// the box keeps the FP64 test for every candidate.
+__device__ __forceinline__ void nbuild_atom(const NbArgs& A, const GridParams& g, uint32_t i, bool uniform_rns) {
     // prefilter band: rns^2 (1 -/+ 1e-5), valid when every atom has the same rns
     const float lo2 = (float)(g.max_rns * g.max_rns * (1.0 - 1e-5));
     const float hi2 = (float)(g.max_rns * g.max_rns * (1.0 + 1e-5));
-    uint32_t s0 = A.bin_start[bin], s1 = A.bin_start[bin + 1];
-    if (s0 == s1) return;
     int cx, cy, cz;
-    unpack_cell(A.cellp[s0], cx, cy, cz);
+    unpack_cell(A.cellp[i], cx, cy, cz);
     int gc[3] = {cx + g.offset[0], cy + g.offset[1], cz + g.offset[2]};
     if (g.dim < 3) gc[2] = 0;
     if (g.dim < 2) gc[1] = 0;
     bool edge[3] = {false, false, false};
     for (int a = 0; a < g.dim; ++a) edge[a] = gc[a] == 0 || gc[a] == g.num[a] - 1;
-    // The FP32 prefilter also holds on periodic axes of one or two cells
-    // when the grid covers the whole box: every cell there is an edge cell,
-    // so the exact test takes the minimum image, and the FP32 minimum image
-    // of the neighbour cell's displacement is the same distance to ~1e-6 of
-    // r^2, inside the band that goes to FP64. A local grid short of the box
-    // keeps the FP64 test for every candidate.
     bool mi[3] = {false, false, false};
-    bool whole = true;
-    for (int a = 0; a < g.dim; ++a) {
-        mi[a] = g.periodic[a] && g.dom_n[a] <= 2;
-        if (g.periodic[a] && (g.offset[a] != 0 || g.num[a] != g.dom_n[a])) whole = false;
-    }
-    const bool prefilter = uniform_rns && whole;
-
-    for (uint32_t base = s0; base < s1; base += width) {
-        uint32_t i = base + lane;
-        bool active = i < s1;
-        double xi = 0, yi = 0, zi = 0, rni = 0;
-        float4 oi = make_float4(0, 0, 0, 0);
-        uint32_t origi = 0;
-        if (active) {
-            xi = A.rx[i]; yi = A.ry[i]; zi = A.rz[i]; rni = A.rns[i];
-            oi = A.o0[i];
-            origi = A.orig[i];
+    for (int a = 0; a < g.dim; ++a) mi[a] = g.periodic[a] && g.dom_n[a] <= 2;
+    const bool prefilter = uniform_rns && grid_whole(g);
+    const int own[3] = {cx, cy, cz};
+    const double xi = A.rx[i], yi = A.ry[i], zi = A.rz[i], rni = A.rns[i];
+    const float4 oi = A.o0[i];
+    const uint32_t origi = A.orig[i];
+    const bool pfi = prefilter && oi.w == 0.0f;
+    int cnt = 0;
+    for (int x = -1; x <= 1; ++x) {
+        if (g.periodic[0]) {
+            if (g.dom_n[0] == 1 && x != 0) continue;
+            if (g.dom_n[0] == 2 && x == 1) continue;
         }
-        int cnt = 0;
-        for (int x = -1; x <= 1; ++x) {
-            if (g.periodic[0]) {
-                if (g.dom_n[0] == 1 && x != 0) continue;
-                if (g.dom_n[0] == 2 && x == 1) continue;
+        for (int y = -1; y <= 1; ++y) {
+            if (g.periodic[1]) {
+                if (g.dom_n[1] == 1 && y != 0) continue;
+                if (g.dom_n[1] == 2 && y == 1) continue;
             }
-            for (int y = -1; y <= 1; ++y) {
-                if (g.periodic[1]) {
-                    if (g.dom_n[1] == 1 && y != 0) continue;
-                    if (g.dom_n[1] == 2 && y == 1) continue;
+            for (int z = -1; z <= 1; ++z) {
+                if (g.periodic[2]) {
+                    if (g.dom_n[2] == 1 && z != 0) continue;
+                    if (g.dom_n[2] == 2 && z == 1) continue;
                 }
-                for (int z = -1; z <= 1; ++z) {
-                    if (g.periodic[2]) {
-                        if (g.dom_n[2] == 1 && z != 0) continue;
-                        if (g.dom_n[2] == 2 && z == 1) continue;
-                    }
-                    int nb[3] = {gc[0] + x, gc[1] + y, gc[2] + z};
-                    for (int a = 0; a < 3; ++a)
-                        if (g.periodic[a]) nb[a] = (nb[a] + g.dom_n[a]) % g.dom_n[a];
-                    int lc[3] = {nb[0] - g.offset[0], nb[1] - g.offset[1], nb[2] - g.offset[2]};
-                    if (lc[0] < 0 || lc[0] >= g.num[0] || lc[1] < 0 || lc[1] >= g.num[1] ||
-                        lc[2] < 0 || lc[2] >= g.num[2])
-                        continue;
-                    int bk = bin_key(g, lc[0], lc[1], lc[2]);
-                    uint32_t j0 = A.bin_start[bk], j1 = A.bin_start[bk + 1];
-                    // image of the neighbour cell relative to this cell
-                    int dl[3] = {x, y, z};
-                    float sh[3] = {(float)x * g.csf[0], (float)y * g.csf[1], (float)z * g.csf[2]};
-                    for (uint32_t j = j0; j < j1; ++j) {
-                        float4 oj = A.o0[j];
-                        if (!active || j == i) continue;
-                        if (A.half && A.orig[j] < origi) continue;
-                        float dx = oi.x - oj.x - sh[0];
-                        float dy = oi.y - oj.y - sh[1];
-                        float dz = oi.z - oj.z - sh[2];
-                        const float ex = mi[0] ? min_image_f(dx, g.Lf[0]) : dx;
-                        const float ey = mi[1] ? min_image_f(dy, g.Lf[1]) : dy;
-                        const float ez = mi[2] ? min_image_f(dz, g.Lf[2]) : dz;
-                        float d2 = ex * ex + ey * ey + ez * ez;
-                        bool acc;
-                        if (prefilter && oi.w == 0.0f && oj.w == 0.0f && d2 < lo2) {
-                            acc = true;
-                        } else if (prefilter && oi.w == 0.0f && oj.w == 0.0f && d2 > hi2) {
-                            acc = false;
-                        } else {
-                            acc = are_neibs_exact(g, xi, yi, zi, rni, A.rx[j], A.ry[j], A.rz[j],
-                                                  A.rns[j], edge);
-                        }
-                        if (!acc) continue;
-                        // periodic image code: minimum image of j seen from i
-                        uint32_t code = 0;
-                        for (int a = 0; a < 3; ++a) {
-                            int dlt = dl[a];
-                            if (g.periodic[a] && a < g.dim && g.dom_n[a] <= 3) {
-                                float dd = -(a == 0 ? dx : a == 1 ? dy : dz);
-                                float half = 0.5f * g.Lf[a];
-                                if (dd > half) dlt -= g.dom_n[a];
-                                else if (dd < -half) dlt += g.dom_n[a];
-                            }
-                            if (dlt < -1 || dlt > 1) {
-                                atomicOr(&A.st->flags, FLAG_IMAGE);
-                                dlt = dlt < -1 ? -1 : 1;
-                            }
-                            code |= (uint32_t)(dlt + 1) << (2 * a);
-                            // the image crossed a periodic face
-                            int own[3] = {cx, cy, cz};
-                            if (dlt != lc[a] - own[a]) code |= 1u << 6;
-                        }
-                        if (cnt < A.K) A.nbr[nidx(cnt, i, A.np)] = j | (code << kJBits);
-                        ++cnt;
-                    }
+                const int dl[3] = {x, y, z};
+                int lc[3];
+                bool inside = true;
+                for (int a = 0; a < 3; ++a) {
+                    int nb = gc[a] + dl[a];  // |dl| <= 1: one period at most
+                    if (g.periodic[a]) nb = nb < 0 ? nb + g.dom_n[a] : nb >= g.dom_n[a] ? nb - g.dom_n[a] : nb;
+                    lc[a] = nb - g.offset[a];
+                    inside = inside && lc[a] >= 0 && lc[a] < g.num[a];
+                }
+                if (!inside) continue;
+                const int bk = bin_key(g, lc[0], lc[1], lc[2]);
+                const uint32_t j0 = A.bin_start[bk], j1 = A.bin_start[bk + 1];
+                // image of the neighbour cell relative to this cell
+                const float sh[3] = {(float)x * g.csf[0], (float)y * g.csf[1], (float)z * g.csf[2]};
+                for (uint32_t j = j0; j < j1; ++j) {
+                    if (j == i) continue;
+                    if (A.half && A.orig[j] < origi) continue;
+                    const float4 oj = A.o0[j];
+                    const float dx = oi.x - oj.x - sh[0];
+                    const float dy = oi.y - oj.y - sh[1];
+                    const float dz = oi.z - oj.z - sh[2];
+                    const float ex = mi[0] ? min_image_f(dx, g.Lf[0]) : dx;
+                    const float ey = mi[1] ? min_image_f(dy, g.Lf[1]) : dy;
+                    const float ez = mi[2] ? min_image_f(dz, g.Lf[2]) : dz;
+                    const float d2 = ex * ex + ey * ey + ez * ez;
+                    bool acc;
+                    if (pfi && oj.w == 0.0f && d2 < lo2) acc = true;
+                    else if (pfi && oj.w == 0.0f && d2 > hi2) acc = false;
+                    else acc = are_neibs_exact(g, xi, yi, zi, rni, A.rx[j], A.ry[j], A.rz[j], A.rns[j], edge);
+                    if (!acc) continue;
+                    // periodic image code: minimum image of j seen from i
+                    const uint32_t code = pair_image_code(g, own, lc, dl, dx, dy, dz, A.st);
+                    if (cnt < A.K) A.nbr[nidx(cnt, i, A.np)] = j | (code << kJBits);
+                    ++cnt;
                 }
             }
         }
-        if (active) {
-            // pad to a multiple of four with self entries
-            int padded = (cnt + 3) & ~3;
-            for (int k = cnt; k < padded && k < A.K; ++k) A.nbr[nidx(k, i, A.np)] = i | kSelfCode;
-            A.ncnt[i] = padded < A.K ? padded : A.K;
-            if (cnt > A.K) {
-                atomicOr(&A.st->flags, FLAG_OVERFLOW);
-                atomicOr(&A.st->build_flags, FLAG_OVERFLOW);
-            }
-            atomicMax(&A.st->max_count, (uint32_t)cnt);
-            A.r0x[i] = xi;
-            A.r0y[i] = yi;
-            A.r0z[i] = zi;
-            A.saved_rcut[i] = A.rcut[i];
-            A.saved_rns[i] = rni;
-            A.saved_uid[i] = A.uid[i];
-        }
     }
+    // pad to a multiple of four with self entries
+    const int padded = (cnt + 3) & ~3;
+    for (int k = cnt; k < padded && k < A.K; ++k) A.nbr[nidx(k, i, A.np)] = i | kSelfCode;
+    A.ncnt[i] = padded < A.K ? padded : A.K;
+    if (cnt > A.K) {
+        atomicOr(&A.st->flags, FLAG_OVERFLOW);
+        atomicOr(&A.st->build_flags, FLAG_OVERFLOW);
+    }
+    atomicMax(&A.st->max_count, (uint32_t)cnt);
+    A.r0x[i] = xi;
+    A.r0y[i] = yi;
+    A.r0z[i] = zi;
+    A.saved_rcut[i] = A.rcut[i];
+    A.saved_rns[i] = rni;
+    A.saved_uid[i] = A.uid[i];
 }
 
 // ---- list build, a warp per cell with lanes over candidates -------------------
@@ -403,9 +402,9 @@ __device__ __forceinline__ void nbuild_bin(const NbArgs& A, const GridParams& g,
 // ballot per atom, so lane i ends with atom i's row of the chunk's accept
 // matrix and appends those candidates in lane order.
 // Entry order per atom is therefore the order of the per-atom loop in
-// nbuild_bin, and the lists are the same, entry for entry. Used when no
+// nbuild_atom, and the lists are the same, entry for entry. Used when no
 // periodic axis has 2 cells or fewer (no minimum-image adjustment of the
-// image code, GridParams::small_box); otherwise nbuild_bin runs.
+// image code, GridParams::small_box); otherwise nbuild_atom runs.
 struct NbWarpSmem {
     uint32_t cj0[27];        // first slot of each non-empty neighbour cell
     uint32_t cpre[28];       // candidate prefix over those cells

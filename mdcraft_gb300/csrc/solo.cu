@@ -210,10 +210,9 @@ __device__ __noinline__ bool solo_rebuild(const SoloArgs& S, GridParams& g, doub
             extern __shared__ __align__(16) unsigned char solo_dyn[];
             NbWarpSmem* nbs = reinterpret_cast<NbWarpSmem*>(solo_dyn);
             for (int b = w; b < nb; b += NT / 32) nbuild_cell_warp(S.N, g, b, lane, uniform, nbs[w]);
-        } else if (n > 16 * g.ncells) {
-            for (int b = w; b < nb; b += NT / 32) nbuild_bin(S.N, g, b, lane, uniform, 32);
         } else {
-            for (int b = 2 * w + (lane >> 4); b < nb; b += NT / 16) nbuild_bin(S.N, g, b, lane & 15, uniform, 16);
+            // a few cells of many atoms: a thread per atom
+            for (int i = t; i < n; i += NT) nbuild_atom(S.N, g, (uint32_t)i, uniform);
         }
     }
     __syncthreads();

@@ -66,9 +66,14 @@ def tune_serving(specs, solvers, device=0, candidates=(256, 512, 1024), sample=1
     """Fastest block size for a stream like `specs` (request specs of
     workloads.serving_stream): returns (threads, {threads: atom-steps/s}).
     The sample is the first `sample` requests with `steps` steps each, all
-    submitted at once (the throughput regime of a backlog)."""
+    submitted at once. A candidate's rate is the throughput of a saturated
+    GPU, the regime of a backlog: its resident blocks (the most seen alive
+    while the sample runs) times the sample's atom-steps per block-second
+    (atom-steps over the sum of the requests' service times). The time to
+    finish the sample would instead be set by its few longest requests
+    running on after the rest."""
     sub = [dict(s, steps=steps, t_arrival=0.0) for s in specs[:sample]]
-    key = f"serving|{_gpu_name(device)}|{_signature(sub)}|{','.join(map(str, candidates))}"
+    key = f"serving-saturated|{_gpu_name(device)}|{_signature(sub)}|{','.join(map(str, candidates))}"
     table = _load() if use_cache else {}
     if key in table:
         got = table[key]
@@ -82,15 +87,28 @@ def tune_serving(specs, solvers, device=0, candidates=(256, 512, 1024), sample=1
         rid = srv.submit(solvers[s0["kind"]], d0, a0, s0["dt"], 5)
         srv.wait(rid, 120.0)
         srv.result(rid, atoms=False)
-        t0 = time.perf_counter()
-        ids = [srv.submit(solvers[s["kind"]], d, a, s["dt"], s["steps"]) for s, a, d in reqs]
-        for rid in ids:
-            srv.wait(rid, 600.0)
-        sec = time.perf_counter() - t0
-        for rid in ids:
-            srv.result(rid, atoms=False)
+        ids = {srv.submit(solvers[s["kind"]], d, a, s["dt"], s["steps"]): k for k, (s, a, d) in enumerate(reqs)}
+        busy = 0.0
+        blocks = 0
+        left = len(ids)
+        t_end = time.perf_counter() + 600.0
+        while left:
+            blocks = max(blocks, srv.stats()["live_blocks"])
+            got = srv.poll()
+            for rid in got:
+                _, info = srv.result(rid, atoms=False)
+                if info["status"] != 0:
+                    srv.close()
+                    raise RuntimeError(f"tuning request failed with status {info['status']}")
+                busy += info["service_s"]
+                left -= 1
+            if not got:
+                if time.perf_counter() > t_end:
+                    srv.close()
+                    raise TimeoutError("tuning sample did not finish in 600 s")
+                time.sleep(1e-3)
         srv.close()
-        rates[nt] = sum(s["n"] * s["steps"] for s in sub) / sec
+        rates[nt] = max(blocks, 1) * sum(s["n"] * s["steps"] for s in sub) / busy
     best = max(rates, key=rates.get)
     if use_cache:
         table = _load()
