@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--serve-slots", type=int, default=320)
     ap.add_argument("--serve-steps", type=int, default=1000)
     ap.add_argument("--serve-block-threads", type=int, default=0,
-                    help="threads of the fused per-system block (256, 512, 1024; 0: chosen by the autotuner "
+                    help="threads of the fused per-system block (256, 512, 640, 768, 896, 1024; 0: chosen by the autotuner "
                          "on a sample of the stream; -1: a graph loop per request)")
     ap.add_argument("--serve-order", default="balanced", choices=["fifo", "largest", "balanced"],
                     help="admission order of waiting requests in the serving stream")

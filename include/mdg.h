@@ -368,8 +368,8 @@ typedef struct mdg_server_config {
     size_t hbm_budget;  /* device bytes the live systems may hold; 0 = half the free memory */
     size_t max_atoms;   /* largest request accepted (sizes the pinned staging) */
     int block_threads;  /* fused one-block loop per system (mixed precision, one kind,
-                           <= 65536 atoms): its threads (256, 512, 1024), 0 = the default
-                           (1024), -1 = off (a graph loop per request instead) */
+                           <= 65536 atoms): its threads (256, 512, 640, 768, 896, 1024), 0 = the default
+                           (768), -1 = off (a graph loop per request instead) */
     int order;          /* admission order of waiting requests: MDG_ORDER_FIFO (0, the
                            default), MDG_ORDER_LARGEST (most atom-steps first, which
                            shortens the tail of a backlog at the cost of small requests'

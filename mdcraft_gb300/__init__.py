@@ -679,7 +679,7 @@ class Server:
 
     def __init__(self, device: int = 0, slots: int = 16, hbm_budget: int = 0, max_atoms: int = 1 << 16,
                  block_threads: int = 0, order: str = "fifo"):
-        """block_threads: threads of the fused per-request block (256, 512, 1024; 0 = 1024);
+        """block_threads: threads of the fused per-request block (256, 512, 640, 768, 896, 1024; 0 = 768);
         -1 runs every request as a graph loop on its slot's stream instead. order: "fifo"
         admits waiting requests in arrival order, "largest" the one with the most
         atom-steps first, "balanced" in arrival order except that the largest

@@ -545,7 +545,16 @@ int solo_persistent_launch(cudaStream_t stream, int threads, int blocks, const v
     if (blocks <= 0) return MDG_OK;
     if (blocks > kSoloMaxBlocks || gen < 0 || gen >= kSoloGens) return MDG_ERR_INVALID;
     const size_t dyn = solo_dyn_bytes(threads);
-    if (threads == 256) {
+    if (threads == 640) {
+        MDG_CUDA(solo_prepare_attr<640>());
+        k_solo_persistent<640><<<blocks, 640, dyn, stream>>>(d, q_dev, head, idle_limit, gen);
+    } else if (threads == 768) {
+        MDG_CUDA(solo_prepare_attr<768>());
+        k_solo_persistent<768><<<blocks, 768, dyn, stream>>>(d, q_dev, head, idle_limit, gen);
+    } else if (threads == 896) {
+        MDG_CUDA(solo_prepare_attr<896>());
+        k_solo_persistent<896><<<blocks, 896, dyn, stream>>>(d, q_dev, head, idle_limit, gen);
+    } else if (threads == 256) {
         MDG_CUDA(solo_prepare_attr<256>());
         k_solo_persistent<256><<<blocks, 256, dyn, stream>>>(d, q_dev, head, idle_limit, gen);
     } else if (threads == 1024) {
@@ -612,7 +621,16 @@ void solo_graph_destroy(SoloGraph& G) {
 int solo_blocks_per_sm(int threads, int* blocks) {
     cudaError_t e;
     const size_t dyn = solo_dyn_bytes(threads);
-    if (threads == 256) {
+    if (threads == 640) {
+        MDG_CUDA(solo_prepare_attr<640>());
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solo_persistent<640>, 640, dyn);
+    } else if (threads == 768) {
+        MDG_CUDA(solo_prepare_attr<768>());
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solo_persistent<768>, 768, dyn);
+    } else if (threads == 896) {
+        MDG_CUDA(solo_prepare_attr<896>());
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solo_persistent<896>, 896, dyn);
+    } else if (threads == 256) {
         MDG_CUDA(solo_prepare_attr<256>());
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_solo_persistent<256>, 256, dyn);
     } else if (threads == 1024) {

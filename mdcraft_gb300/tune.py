@@ -61,7 +61,7 @@ def _store(table):
     os.replace(tmp, CACHE)
 
 
-def tune_serving(specs, solvers, device=0, candidates=(256, 512, 1024), sample=192, steps=200, slots=320,
+def tune_serving(specs, solvers, device=0, candidates=(512, 640, 768, 896, 1024), sample=192, steps=200, slots=320,
                  use_cache=True):
     """Fastest block size for a stream like `specs` (request specs of
     workloads.serving_stream): returns (threads, {threads: atom-steps/s}).
