@@ -14,6 +14,17 @@
 
 namespace mdg {
 
+// A group of four list entries: streamed once per pass, so kept out of L1
+// (the gathers of neighbour records and table rows keep it).
+__device__ __forceinline__ uint4 ldg_list(const uint4* p) {
+    uint4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+
+
 struct FArgs {
     int n, np;
     const double *rx, *ry, *rz, *rns;
@@ -186,11 +197,11 @@ __device__ __forceinline__ bool lj_mixed_force(const FArgs& A, const PotSet* __r
     double R2c = P0.R2cut;
     Kahan3 acc;
     const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
-    uint4 e4n = ng > 0 ? __ldg(row) : make_uint4(0, 0, 0, 0);
+    uint4 e4n = ng > 0 ? ldg_list(row) : make_uint4(0, 0, 0, 0);
     for (int g = 0; g < ng; ++g) {
         // the next group's entries are requested before this group's work
         const uint4 e4 = e4n;
-        if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
+        if (g + 1 < ng) e4n = ldg_list(row + (size_t)(g + 1) * A.np);
         const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
         int4 pj[4];
 #pragma unroll
@@ -278,10 +289,10 @@ __device__ __forceinline__ bool pair_mixed_force(const FArgs& A, const PotSet* _
     const float uf[3] = {A.uf[0], A.uf[1], A.uf[2]};
     Kahan3 acc;
     const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
-    uint4 e4n = ng > 0 ? __ldg(row) : make_uint4(0, 0, 0, 0);
+    uint4 e4n = ng > 0 ? ldg_list(row) : make_uint4(0, 0, 0, 0);
     for (int g = 0; g < ng; ++g) {
         const uint4 e4 = e4n;
-        if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
+        if (g + 1 < ng) e4n = ldg_list(row + (size_t)(g + 1) * A.np);
         const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
         int4 pj[4];
 #pragma unroll
@@ -355,13 +366,13 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
         int Nr1 = P->Nr1;
         const float4* tab = P->rho_c;
         const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
-        uint4 e4n = ng > 0 ? __ldg(row) : make_uint4(0, 0, 0, 0);
+        uint4 e4n = ng > 0 ? ldg_list(row) : make_uint4(0, 0, 0, 0);
         uint32_t bits = 0;   // FP64 cut decisions of this word's band entries, for A.cutbits
         bool band = false;  // the word has a band entry
         for (int g = 0; g < ng; ++g) {
             // the next group's entries are requested before this group's work
             const uint4 e4 = e4n;
-            if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
+            if (g + 1 < ng) e4n = ldg_list(row + (size_t)(g + 1) * A.np);
             const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
             int4 pj[4];
 #pragma unroll
@@ -433,11 +444,11 @@ __device__ __forceinline__ bool eam_mixed_force(const FArgs& A, const PotSet* __
     const float4* rv = P->rv_c;
     Kahan3 acc;
     const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
-    uint4 e4n = ng > 0 ? __ldg(row) : make_uint4(0, 0, 0, 0);
+    uint4 e4n = ng > 0 ? ldg_list(row) : make_uint4(0, 0, 0, 0);
     for (int g = 0; g < ng; ++g) {
         // the next group's entries are requested before this group's work
         const uint4 e4 = e4n;
-        if (g + 1 < ng) e4n = __ldg(row + (size_t)(g + 1) * A.np);
+        if (g + 1 < ng) e4n = ldg_list(row + (size_t)(g + 1) * A.np);
         const uint32_t e[4] = {e4.x, e4.y, e4.z, e4.w};
         int4 pj[4];
 #pragma unroll

@@ -111,15 +111,16 @@ __device__ __forceinline__ bool drift64_one(const IArgs& A, int i, int drift, in
 // The offsets refresh and the rebuild test of drift_mixed_one, for the
 // atom's position r after its drift.
 __device__ __forceinline__ bool offsets_check_mixed(const IArgs& A, int i, const double r[3]) {
-    const int4 q = make_int4(off_encode(r[0] - A.Rx[i], A.inv_u[0]), off_encode(r[1] - A.Ry[i], A.inv_u[1]),
-                             off_encode(r[2] - A.Rz[i], A.inv_u[2]), 0);
+    const int4 q = make_int4(off_encode(r[0] - __ldcs(A.Rx + i), A.inv_u[0]),
+                             off_encode(r[1] - __ldcs(A.Ry + i), A.inv_u[1]),
+                             off_encode(r[2] - __ldcs(A.Rz + i), A.inv_u[2]), 0);
     A.pos32[i] = q;
-    const int4 p = A.q0[i];
+    const int4 p = __ldcs(A.q0 + i);
     const float dx = __int2float_rn((int)((uint32_t)q.x - (uint32_t)p.x)) * A.uf[0];
     const float dy = __int2float_rn((int)((uint32_t)q.y - (uint32_t)p.y)) * A.uf[1];
     const float dz = __int2float_rn((int)((uint32_t)q.z - (uint32_t)p.z)) * A.uf[2];
     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float2 tb = A.trig[i];
+    const float2 tb = __ldcs(A.trig + i);
     if (d2 > tb.x + tb.y) return true;
     if (d2 < tb.x - tb.y) return false;
     double skin = dsub(A.saved_rns[i], A.saved_rcut[i]);
@@ -145,6 +146,10 @@ __device__ __forceinline__ bool drift_mixed_one(const IArgs& A, int i) {
     return offsets_check_mixed(A, i, r);
 }
 
+// Per-atom fields read once per step (cell centres, rebuild-time offsets
+// and thresholds, mass, position, velocity) are loaded cache-streaming
+// (evict-first), so that they do not displace the neighbour records and
+// table rows the force pass gathers from L1.
 // The end of a mixed step's force pass when the next step starts in it:
 // the FP32 force stored, this step's second half-kick, then the next
 // step's first half-kick and drift, offsets refresh and rebuild test —
@@ -156,12 +161,12 @@ __device__ __forceinline__ bool kick_drift_mixed(const IArgs& A, float* gx, floa
     gx[i] = fx;
     gy[i] = fy;
     gz[i] = fz;
-    const float hm = (0.5f * (float)A.dt) * __frcp_rn((float)A.m[i]);
+    const float hm = (0.5f * (float)A.dt) * __frcp_rn((float)__ldcs(A.m + i));
     const float g[3] = {fx, fy, fz};
     double* v[3] = {A.vx, A.vy, A.vz};
-    double r[3] = {A.rx[i], A.ry[i], A.rz[i]};
+    double r[3] = {__ldcs(A.rx + i), __ldcs(A.ry + i), __ldcs(A.rz + i)};
     for (int k = 0; k < 3; ++k) {
-        double vk = v[k][i] + (double)(g[k] * hm);  // second half-kick of this step
+        double vk = __ldcs(v[k] + i) + (double)(g[k] * hm);  // second half-kick of this step
         vk = vk + (double)(g[k] * hm);               // first half-kick of the next
         v[k][i] = vk;
         r[k] = fma(vk, A.dt, r[k]);
