@@ -382,8 +382,9 @@ __global__ void __launch_bounds__(kBlock) k_nbuild_atoms(NbArgs A, const GridPar
     if (threadIdx.x == 0) g = *gp;
     __syncthreads();
     if (g.empty || !g.small_box) return;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < (uint32_t)A.n) nbuild_atom(A, g, i, A.st->nonuniform == 0);
+    const bool uniform = A.st->nonuniform == 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (uint32_t)A.n; i += gridDim.x * blockDim.x)
+        nbuild_atom(A, g, i, uniform);
 }
 
 // VerletList::optimize_search_radius (verlet-list.cxx:72-92):
@@ -741,7 +742,9 @@ int nlist_enqueue(mdg_system* sys) {
     else if (cpb == 8) k_nbuild_warp<8><<<nbw, 8 * 32, 0, st>>>(A, sys->dgrid);
     else k_nbuild_warp<4><<<nbw, 4 * 32, 0, st>>>(A, sys->dgrid);
     MDG_LAUNCHED(ctx);
-    k_nbuild_atoms<<<nblk(n), kBlock, 0, st>>>(A, sys->dgrid);
+    // a grid-stride launch of at most four blocks per SM: on the large
+    // grids, where it returns at once, its blocks are few
+    k_nbuild_atoms<<<std::min(nblk(n), 4 * std::max(ctx->num_sms, 1)), kBlock, 0, st>>>(A, sys->dgrid);
     MDG_LAUNCHED(ctx);
     return MDG_OK;
 }
