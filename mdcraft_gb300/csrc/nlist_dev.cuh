@@ -476,16 +476,25 @@ __device__ __forceinline__ void nbuild_cell_warp(const NbArgs& A, const GridPara
     }
     const uint32_t T = __shfl_sync(full, incl, 31);
     if (lane == 0) S.cpre[nc] = T;
+    // the cell itself (lane 13: offset (0, 0, 0)) among the used cells
+    const int home = __popc(vm & ((1u << 13) - 1u));
     __syncwarp();
+    const float kInf = __int_as_float(0x7f800000), kNaN = __int_as_float(0x7fffffff);
 
     for (uint32_t base = s0; base < s1; base += 32) {
         const uint32_t ni = s1 - base < 32u ? s1 - base : 32u;
         const bool act = (uint32_t)lane < ni;
         const uint32_t me = base + lane;
         if (act) {
-            S.oi[lane] = A.o0[me];
+            // an atom whose offset is not exact carries NaN in z and w: its
+            // pairs fail every FP32 test (w is the flag the FP32 tests read)
+            float4 o = A.o0[me];
+            if (o.w != 0.0f) o.z = o.w = kNaN;
+            S.oi[lane] = o;
             S.origi[lane] = A.orig[me];
         }
+        // this atom's own candidate index (it is a candidate of its own cell)
+        const uint32_t self_t = act ? S.cpre[home] + (me - S.cj0[home]) : 0xffffffffu;
         __syncwarp();
         int cnt = 0;  // list length of atom `me`
         int c = 0;    // neighbour cell of this lane's candidate
@@ -513,18 +522,44 @@ __device__ __forceinline__ void nbuild_cell_warp(const NbArgs& A, const GridPara
             // within 1e-5 of rns (or of atoms whose offsets are not exact)
             // are marked in a second row and settled in FP64 below
             unsigned mine = 0, mine_x = 0;
+            bool exact = A.half;
+            if (!A.half) {
+                // One ballot per atom: the candidate's coordinates are +inf
+                // without a candidate and NaN when the prefilter cannot
+                // decide its pairs, so neither is ever accepted here; the
+                // atom's own slot is cleared after the loop. A pair that the
+                // prefilter cannot settle (band, NaN) sends the whole chunk
+                // to the loop below, whose rows are therefore the same.
+                const float qx = !have ? kInf : pfj ? px : kNaN;
+                bool band = false;
 #pragma unroll 2
-            for (uint32_t ii = 0; ii < ni; ++ii) {
-                const float4 oi = S.oi[ii];
-                const float dx = oi.x - px, dy = oi.y - py, dz = oi.z - pz;
-                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                const bool pf = pfj && oi.w == 0.0f;
-                const bool ok = have && j != base + ii && !(A.half && origj < S.origi[ii]);
-                const unsigned m = __ballot_sync(full, ok && pf && d2 < lo2);
-                const unsigned mx = __ballot_sync(full, ok && !(pf && (d2 < lo2 || d2 > hi2)));
-                if ((uint32_t)lane == ii) {
-                    mine = m;
-                    mine_x = mx;
+                for (uint32_t ii = 0; ii < ni; ++ii) {
+                    const float4 oi = S.oi[ii];
+                    const float dx = oi.x - qx, dy = oi.y - py, dz = oi.z - pz;
+                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const bool sure = d2 < lo2;
+                    const unsigned m = __ballot_sync(full, sure);
+                    band |= !sure && !(d2 > hi2);
+                    if ((uint32_t)lane == ii) mine = m;
+                }
+                if (self_t - tb < 32u) mine &= ~(1u << (self_t - tb));
+                exact = __any_sync(full, band);
+            }
+            if (exact) {
+                mine = 0;
+#pragma unroll 2
+                for (uint32_t ii = 0; ii < ni; ++ii) {
+                    const float4 oi = S.oi[ii];
+                    const float dx = oi.x - px, dy = oi.y - py, dz = oi.z - pz;
+                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const bool pf = pfj && oi.w == 0.0f;
+                    const bool ok = have && j != base + ii && !(A.half && origj < S.origi[ii]);
+                    const unsigned m = __ballot_sync(full, ok && pf && d2 < lo2);
+                    const unsigned mx = __ballot_sync(full, ok && !(pf && (d2 < lo2 || d2 > hi2)));
+                    if ((uint32_t)lane == ii) {
+                        mine = m;
+                        mine_x = mx;
+                    }
                 }
             }
             while (mine_x) {
@@ -552,7 +587,6 @@ __device__ __forceinline__ void nbuild_cell_warp(const NbArgs& A, const GridPara
                 atomicOr(&A.st->flags, FLAG_OVERFLOW);
                 atomicOr(&A.st->build_flags, FLAG_OVERFLOW);
             }
-            atomicMax(&A.st->max_count, (uint32_t)cnt);
             A.r0x[me] = A.rx[me];
             A.r0y[me] = A.ry[me];
             A.r0z[me] = A.rz[me];
@@ -560,6 +594,9 @@ __device__ __forceinline__ void nbuild_cell_warp(const NbArgs& A, const GridPara
             A.saved_rns[me] = A.rns[me];
             A.saved_uid[me] = A.uid[me];
         }
+        // the longest list, one atomic per warp
+        const unsigned wmax = __reduce_max_sync(full, act ? (unsigned)cnt : 0u);
+        if (lane == 0) atomicMax(&A.st->max_count, wmax);
         __syncwarp();
     }
 }
