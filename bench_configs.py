@@ -273,12 +273,22 @@ def lj_liquid(device=0, steps=200, dims=(128, 128, 256), cpu_steps=1):
     rb0 = nl.rebuilds()
     sec = _timed_run(ctx, sysg, st, p["dt"], steps)
     rebuilds = nl.rebuilds() - rb0
+    # per-stage device times: the same loop step by step with CUDA events
+    # around each stage launch (40 steps)
+    ctx.set_timing(True)
+    st.run(sysg, p["dt"], 40)
+    ctx.synchronize()
+    stage = {}
+    for k in ("drift", "forces", "rebuild"):
+        ms, nlaunch = ctx.stage_time(k)
+        stage[k] = {"ms_per_launch": ms / max(nlaunch, 1), "launches": nlaunch}
+    ctx.set_timing(False)
     eerr = _energy_error(sysg, nl, atoms, s64, smx, p["dt"], 10)
     n = len(atoms)
     out = {"config": f"LJ liquid rho*=0.8442 T*=0.72, fcc melt start, {n} atoms, rc 2.5 sigma, skin 0.3 sigma, "
                      f"dt*=0.005, mixed", "atoms": n, "steps": steps,
            "mixed": {"value": n * steps / sec, "unit": "atom-steps/s", "ms_per_step": 1e3 * sec / steps,
-                     "rebuilds": rebuilds},
+                     "rebuilds": rebuilds, "stage_ms": stage},
            "force_error_vs_fp64": err, "energy_error_vs_fp64": eerr, "shapes": shapes}
     sysg.close()
     if cpu_steps:
