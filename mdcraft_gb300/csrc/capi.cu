@@ -951,10 +951,8 @@ int mdg_system_get_forces(mdg_system* sys, double* xyz) { return vec_io(sys, xyz
 int mdg_nlist_update(mdg_system* sys, double kbuf, int half) {
     if (!sys) return MDG_ERR_INVALID;
     MDG_CUDA(cudaSetDevice(sys->ctx->device));
-    int rc = nlist_build(sys, kbuf, half ? 1 : 0);
+    int rc = nlist_build(sys, kbuf, half ? 1 : 0);  // it also refreshes the rebuild thresholds
     if (rc && rc != MDG_ERR_RANGE) return rc;
-    int rc2 = launch_trig(sys);
-    if (rc2) return rc2;
     MDG_CUDA(cudaStreamSynchronize(sys->ctx->stream));
     return rc;
 }
@@ -2072,8 +2070,6 @@ int run_graph_finish(mdg_solver* s, mdg_system* sys, long* left) {
         sys->rebuilds--;
         int rc = nlist_build(sys, -1.0, sys->half);
         if (rc && rc != MDG_ERR_RANGE) return rc;
-        rc = launch_trig(sys);
-        if (rc) return rc;
     }
     return MDG_OK;
 }
@@ -2280,8 +2276,6 @@ static int run_host_step_body(mdg_solver* s, mdg_system* sys, const PotSet& ps, 
             MDG_CUDA(cudaStreamWaitEvent(st, ev_vel_in, 0));  // the rebuild permutes the velocities
             rc = nlist_build(sys, -1.0, sys->half);
             if (rc && rc != MDG_ERR_RANGE) return rc;
-            rc = launch_trig(sys);
-            if (rc) return rc;
             c = sys->cur;
         }
         rc = launch_offsets(sys);
@@ -2339,8 +2333,6 @@ static int run_host_step_body(mdg_solver* s, mdg_system* sys, const PotSet& ps, 
         MDG_CUDA(cudaStreamWaitEvent(st, ev_reads, 0));
         rc = nlist_build(sys, -1.0, sys->half);
         if (rc && rc != MDG_ERR_RANGE) return rc;
-        rc = launch_trig(sys);
-        if (rc) return rc;
         if (prec == MDG_PREC_MIXED) {
             rc = launch_offsets(sys);
             if (rc) return rc;
@@ -2425,8 +2417,6 @@ static int run_loop_next(mdg_solver* s, mdg_system* sys, const PotSet& ps, doubl
             rc = nlist_build(sys, -1.0, sys->half);
             timer_end(ctx, MDG_TIME_REBUILD, t0);
             if (rc && rc != MDG_ERR_RANGE) return rc;
-            rc = launch_trig(sys);
-            if (rc) return rc;
             t0 = timer_begin(ctx);
             rc = launch_drift_guarded(sys, dt, sys->dcounter, 2);
             timer_end(ctx, MDG_TIME_DRIFT, t0);
@@ -2511,8 +2501,6 @@ int mdg_run(mdg_solver* s, mdg_system* sys, double dt, long steps) {
             rc = nlist_build(sys, -1.0, sys->half);
             timer_end(sys->ctx, MDG_TIME_REBUILD, t0);
             if (rc && rc != MDG_ERR_RANGE) goto done;
-            rc = launch_trig(sys);
-            if (rc) goto done;
             if (prec == MDG_PREC_MIXED) {
                 rc = launch_offsets(sys);
                 if (rc) goto done;

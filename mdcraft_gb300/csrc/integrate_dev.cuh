@@ -189,7 +189,9 @@ __device__ __forceinline__ void kick_mixed_one(const IArgs& A, int i) {
 // error is at most sqrt(3) u per axis from the offset quantisation (u the
 // largest offset unit), i.e. 2 sqrt(3) |d| u + 3 u^2 in d^2, plus ~1e-6
 // relative from the FP32 arithmetic; the band, 1e-5 of the threshold +
-// 4 sqrt(threshold) u + 4 u^2, covers both.
+// 4 sqrt(threshold) u + 4 u^2, covers both. The threshold is FP64 (as
+// decide_one's) rounded to FP32; the band, a bound with 15% or more to
+// spare in each term, is evaluated in FP32 (FP64 square roots are slow).
 __device__ __forceinline__ void trig_one(int i, const double* __restrict__ saved_rns,
                                          const double* __restrict__ saved_rcut, const GridParams& g,
                                          float2* __restrict__ trig) {
@@ -198,9 +200,9 @@ __device__ __forceinline__ void trig_one(int i, const double* __restrict__ saved
         trig[i] = make_float2(-1.0f, 0.0f);
         return;
     }
-    double t = dmul(dmul(0.25, skin), skin);
-    double u = fmax(g.cs[0], fmax(g.cs[1], g.cs[2])) / kOffUnits;
-    trig[i] = make_float2((float)t, (float)(1e-5 * t + 4.0 * sqrt(t) * u + 4.0 * u * u));
+    const float t = (float)dmul(dmul(0.25, skin), skin);
+    const float u = fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2])) * (1.0f / (float)kOffUnits);
+    trig[i] = make_float2(t, fmaf(1e-5f, t, fmaf(4.0f * sqrtf(t), u, 4.0f * u * u)));
 }
 
 }  // namespace mdg

@@ -60,6 +60,7 @@ struct GridParams {
     float csf[3];
     float Lf[3];
     double inv_u[3];   // 2^29 / cs: FP64 offset -> fixed-point units (pos32)
+    double inv_cs[3];  // 1 / cs, for the cell of a position (floor_div)
 };
 
 // Fixed-point cell offsets of the mixed form. An offset from the atom's cell

@@ -72,6 +72,7 @@ __host__ __device__ inline void grid_from_bounds(const DomainDev& d, const doubl
         g.csf[i] = (float)g.cs[i];
         g.Lf[i] = (float)d.size[i];
         g.inv_u[i] = g.cs[i] > 0.0 ? kOffUnits / g.cs[i] : 0.0;
+        g.inv_cs[i] = g.cs[i] > 0.0 ? 1.0 / g.cs[i] : 0.0;
         // A periodic axis of 3 cells keeps the fast paths: its cells are at
         // least max rns wide (floor(L / rns) = 3), so every listed pair is
         // nearer than L / 2 and the image of its neighbour cell is the
@@ -91,13 +92,28 @@ __host__ __device__ inline void grid_from_bounds(const DomainDev& d, const doubl
     g.nbins = (int)nb;
 }
 
+// floor(x / cs) with the quotient correctly rounded in FP64, as the
+// reference's cell index takes it (grid.cxx). The product with the
+// reciprocal 1/cs (itself rounded) lies within 1.5 * 2^-52 (relative) of the
+// exact quotient, as does the rounded quotient, so the two have the same
+// floor unless an integer lies within that distance of the product. Below
+// 2^20 cells that distance is under 3.5e-10: a product within 1e-9 of an
+// integer, or beyond 2^20, takes the division instead.
+__device__ __forceinline__ int floor_div(double x, double cs, double inv_cs) {
+    const double q = dmul(x, inv_cs);
+    const double f = floor(q);
+    const double frac = dsub(q, f);  // exact: f <= q < f + 1
+    if (frac > 1e-9 && frac < 1.0 - 1e-9 && fabs(q) < 1048576.0) return (int)f;
+    return (int)floor(__ddiv_rn(x, cs));
+}
+
 __device__ __forceinline__ void local_cell(const GridParams& g, double x, double y, double z,
                                            int c[3], bool& clamped) {
     double r[3] = {x, y, z};
     clamped = false;
     for (int a = 0; a < 3; ++a) {
         int v = 0;
-        if (a < g.dim) v = (int)floor(__ddiv_rn(dsub(r[a], g.bmin[a]), g.cs[a])) - g.offset[a];
+        if (a < g.dim) v = floor_div(dsub(r[a], g.bmin[a]), g.cs[a], g.inv_cs[a]) - g.offset[a];
         if (v < 0) { v = 0; clamped = true; }
         if (v >= g.num[a]) { v = g.num[a] - 1; clamped = true; }
         c[a] = v;
