@@ -261,7 +261,9 @@ int mdg_solver_stages(mdg_solver* s, mdg_system* sys);
  * choice cached per GPU and workload); 0 restores the measured default.
  * No counterpart in the reference. Values:
  *   MDG_SHAPE_LIST_CELLS_PER_BLOCK   cells (warps) per block of the list build: 2, 4, 8
- *   MDG_SHAPE_FORCE_BLOCKS_PER_SM    register budget of the mixed force pass: 3, 4
+ *   MDG_SHAPE_FORCE_BLOCKS_PER_SM    register budget of the mixed force pass: 3, 4, or 8
+ *                                    (eight 128-thread blocks: the step loop's EAM force
+ *                                    pass; the other force passes take 4 then)
  *   MDG_SHAPE_DENSITY_BLOCKS_PER_SM  register budget of the mixed density pass: 3, 4, 5 */
 #define MDG_SHAPE_LIST_CELLS_PER_BLOCK 0
 #define MDG_SHAPE_FORCE_BLOCKS_PER_SM 1

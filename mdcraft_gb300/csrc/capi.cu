@@ -1546,7 +1546,7 @@ static int thermo_sync(mdg_solver* s) {
 
 int mdg_system_set_shape(mdg_system* sys, int what, int value) {
     if (!sys || what < 0 || what > 2) return MDG_ERR_INVALID;
-    static const int ok[3][4] = {{0, 2, 4, 8}, {0, 3, 4, -1}, {0, 3, 4, 5}};
+    static const int ok[3][4] = {{0, 2, 4, 8}, {0, 3, 4, 8}, {0, 3, 4, 5}};
     bool valid = false;
     for (int v : ok[what]) valid = valid || v == value;
     if (!valid) {

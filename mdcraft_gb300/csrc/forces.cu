@@ -623,8 +623,8 @@ static void launch_forces_mixed(const mdg_system* sys, const FArgs& A, const Pot
 // neighbours only through the density pass's copies (pos32b, Fp32) and takes
 // each pair's cut decision from the density pass (cutbits), where the
 // unfused pass would settle pairs near the cutoff on the FP64 positions.
-template <bool MULTI, int MB>
-__global__ void __launch_bounds__(kBlock, MB)
+template <bool MULTI, int MB, int NT = kBlock>
+__global__ void __launch_bounds__(NT, MB)
     k_force_step(FArgs A, IArgs D, const PotSet* __restrict__ ps, const unsigned long long* __restrict__ left) {
     const bool next = *left > 1ull && A.st->need_rebuild == 0u;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -660,11 +660,16 @@ int launch_forces_step(mdg_system* sys, const PotSet* dps, const PotSet& ps, dou
     cudaStream_t st = ctx->stream;
     const bool multi = ps.multi != 0;
     const int mb = force_blocks(sys, multi);
+    // 8: eight 128-thread blocks per SM (the 4-block budget in blocks half
+    // the size, so the launch's last, partly filled wave is shorter)
+    const int nb128 = nblk(sys->n, 128);
     if (multi) {
         if (mb == 3) k_force_step<true, 3><<<nb, kBlock, 0, st>>>(A, D, dps, left);
+        else if (mb == 8) k_force_step<true, 8, 128><<<nb128, 128, 0, st>>>(A, D, dps, left);
         else k_force_step<true, 4><<<nb, kBlock, 0, st>>>(A, D, dps, left);
     } else {
         if (mb == 3) k_force_step<false, 3><<<nb, kBlock, 0, st>>>(A, D, dps, left);
+        else if (mb == 8) k_force_step<false, 8, 128><<<nb128, 128, 0, st>>>(A, D, dps, left);
         else k_force_step<false, 4><<<nb, kBlock, 0, st>>>(A, D, dps, left);
     }
     MDG_LAUNCHED(ctx);

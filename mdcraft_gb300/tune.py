@@ -8,7 +8,8 @@ the fastest is kept.
 A system's step kernels (`tune_shapes`): the cells per block of the list
 build (2, 4 or 8 warps, a cell each) are timed on the system's own rebuilds
 (median of single rebuilds), then the register budgets of the mixed force
-and density passes (blocks of 256 threads per SM) by the CUDA events the
+and density passes (blocks of 256 threads per SM; for the force pass also
+eight blocks of 128 threads, whose last partial wave is shorter) by the CUDA events the
 step loop puts around each of its force and density launches, one
 dimension at a time. Whole-step times are not used: a list rebuild (about
 three steps' worth of work) lands in some windows and not others.
@@ -118,7 +119,7 @@ def tune_serving(specs, solvers, device=0, candidates=(512, 640, 768, 896, 1024)
     return best, rates
 
 
-SHAPE_CANDIDATES = {"list_cells_per_block": (2, 4, 8), "force_blocks_per_sm": (3, 4),
+SHAPE_CANDIDATES = {"list_cells_per_block": (2, 4, 8), "force_blocks_per_sm": (3, 4, 8),
                     "density_blocks_per_sm": (3, 4, 5)}
 
 
@@ -155,7 +156,7 @@ def tune_shapes(system, nlist, stepper, dt, signature, device=0, eam=True, steps
     and Verlet stepper). The system's state advances while it is measured.
     Returns ({shape: value}, {shape: {value: seconds}}) and leaves the
     chosen shapes set on the system."""
-    key = f"shapes|{_gpu_name(device)}|{signature}"
+    key = f"shapes-v2|{_gpu_name(device)}|{signature}"
     table = _load() if use_cache else {}
     if key in table:
         got = table[key]

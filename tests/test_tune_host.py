@@ -49,7 +49,7 @@ class _System:
 
 # seconds per unit of work for each candidate: the fastest is unambiguous
 _COST = {"list_cells_per_block": {2: 1.5e-3, 4: 5e-4, 8: 1e-3},
-         "force_blocks_per_sm": {3: 1e-3, 4: 2.5e-4},
+         "force_blocks_per_sm": {3: 1e-3, 4: 2.5e-4, 8: 6e-4},
          "density_blocks_per_sm": {3: 1e-3, 4: 1e-3, 5: 2.5e-4}}
 
 
@@ -95,7 +95,7 @@ def test_picks_fastest_and_caches(cache):
     s2 = _System()
     best2, sec2 = tune.tune_shapes(s2, None, None, 1e-3, signature="fake")
     assert best2 == best and s2.shape == best
-    assert sorted(sec2["force_blocks_per_sm"]) == [3, 4]  # integer keys, as when measured
+    assert sorted(sec2["force_blocks_per_sm"]) == [3, 4, 8]  # integer keys, as when measured
     assert sec["force_blocks_per_sm"][4] == pytest.approx(2.5e-4)  # per launch, rebuilds excluded
     assert len(s2.calls) == len(best)
 
