@@ -246,6 +246,27 @@ def _cases():
     g3["r"][:, 0] = rng.random(3000) * 1.5
     g3["rns"] = 0.5
     cases.append(("gas_3cells_periodic_x_rns_third", g3, (0.0, 1.5, 0.0, 6.0, 0.0, 6.0), (1, 0, 0), None))
+    # atoms on cell faces: integer sites of a box of 6 unit cells per axis
+    # (cs = 1 = rns exactly, so neighbours sit at exactly rns) and the same
+    # sites one ulp to either side (below 0 they wrap to just under 6)
+    k = np.arange(6.0)
+    site = np.stack(np.meshgrid(k, k, k, indexing="ij"), -1).reshape(-1, 3)
+    faces = np.concatenate([site, np.nextafter(site, np.inf), np.nextafter(site, -np.inf)])
+    g4 = W.new_atoms(len(faces))
+    g4["r"] = faces
+    g4["rns"] = 1.0
+    g4["rcut"] = 0.9
+    g4["m"] = 1.0
+    g4["uid"] = np.arange(1, len(faces) + 1)
+    cases.append(("faces_exact_6cells", g4, (0.0, 6.0, 0.0, 6.0, 0.0, 6.0), (1, 1, 1), None))
+    # one cell per periodic axis (L < 2 rns): every pair by its nearest image
+    g5 = W.new_atoms(60)
+    g5["r"] = rng.random((60, 3)) * 1.5
+    g5["rns"] = 1.0
+    g5["rcut"] = 0.8
+    g5["m"] = 1.0
+    g5["uid"] = np.arange(1, 61)
+    cases.append(("gas_1cell_periodic", g5, (0.0, 1.5, 0.0, 1.5, 0.0, 1.5), (1, 1, 1), None))
     return cases
 
 
