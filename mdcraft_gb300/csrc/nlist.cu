@@ -375,16 +375,20 @@ __global__ void __launch_bounds__(NW * 32, 32 / NW) k_nbuild_warp(NbArgs A, cons
 }
 
 // The list build of grids with a periodic axis of 2 cells or fewer (a few
-// cells of many atoms): a thread per atom. Launched after k_nbuild_warp;
-// each of the two returns at once on the other's grids.
+// cells of many atoms): a thread per atom. Launched after k_nbuild_warp. On
+// the other grids it returns at once, unless some atom was clamped into the
+// grid (FLAG_RANGE): those atoms' lists are built again from their
+// unclamped cells (nbuild_atom), over what the warp build wrote.
 __global__ void __launch_bounds__(kBlock) k_nbuild_atoms(NbArgs A, const GridParams* __restrict__ gp) {
     __shared__ GridParams g;
     if (threadIdx.x == 0) g = *gp;
     __syncthreads();
-    if (g.empty || !g.small_box) return;
+    if (g.empty) return;
+    const bool clamped_only = !g.small_box;
+    if (clamped_only && !(A.st->build_flags & FLAG_RANGE)) return;
     const bool uniform = A.st->nonuniform == 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (uint32_t)A.n; i += gridDim.x * blockDim.x)
-        nbuild_atom(A, g, i, uniform);
+        if (!clamped_only || A.o0[i].w == 2.0f) nbuild_atom(A, g, i, uniform);
 }
 
 // VerletList::optimize_search_radius (verlet-list.cxx:72-92):

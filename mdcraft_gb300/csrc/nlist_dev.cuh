@@ -224,7 +224,10 @@ __device__ __forceinline__ void cells_one(const GridParams& g, int i, const doub
     Rz[i] = R[2];
     pos32[i] = make_int4(q[0], q[1], q[2], 0);
     q0[i] = make_int4(q[0], q[1], q[2], 0);
-    o0[i] = make_float4(o[0], o[1], o[2], outlier ? 1.0f : 0.0f);
+    // w: 0 exact offsets; 1 not exact (the FP32 tests send its pairs to FP64);
+    // 2 clamped into the grid (also not exact: its list is walked from the
+    // unclamped cell, nbuild_atom)
+    o0[i] = make_float4(o[0], o[1], o[2], cl ? 2.0f : outlier ? 1.0f : 0.0f);
     slot_of[orig[i]] = (uint32_t)i;
 }
 
@@ -321,13 +324,31 @@ __device__ __forceinline__ float min_image_f(float d, float L) {
 // minimum image of the neighbour cell's displacement is the same distance
 // to ~1e-6 of r^2, inside the band that goes to FP64. A local grid short of
 // the box keeps the FP64 test for every candidate.
+// An atom clamped into the grid (a position on the upper face of a periodic
+// axis after the wrap, or outside the grid) is binned in its clamped cell,
+// but, as Grid::adjacent_cells (grid.cxx:138-207) takes the cell of the
+// position itself, its own walk and edge flags come from the unclamped cell;
+// the image codes stay relative to the cell it is binned in.
 __device__ __forceinline__ void nbuild_atom(const NbArgs& A, const GridParams& g, uint32_t i, bool uniform_rns) {
     // prefilter band: rns^2 (1 -/+ 1e-5), valid when every atom has the same rns
     const float lo2 = (float)(g.max_rns * g.max_rns * (1.0 - 1e-5));
     const float hi2 = (float)(g.max_rns * g.max_rns * (1.0 + 1e-5));
     int cx, cy, cz;
     unpack_cell(A.cellp[i], cx, cy, cz);
+    const int own[3] = {cx, cy, cz};
+    const double xi = A.rx[i], yi = A.ry[i], zi = A.rz[i], rni = A.rns[i];
+    const float4 oi = A.o0[i];
+    // the walk's cell (global index) and its offset from the binned cell
     int gc[3] = {cx + g.offset[0], cy + g.offset[1], cz + g.offset[2]};
+    int shift[3] = {0, 0, 0};
+    if (oi.w == 2.0f) {
+        const double r[3] = {xi, yi, zi};
+        for (int a = 0; a < g.dim; ++a) {
+            const int u = floor_div(dsub(r[a], g.bmin[a]), g.cs[a], g.inv_cs[a]);
+            shift[a] = u - gc[a];
+            gc[a] = u;
+        }
+    }
     if (g.dim < 3) gc[2] = 0;
     if (g.dim < 2) gc[1] = 0;
     bool edge[3] = {false, false, false};
@@ -335,9 +356,6 @@ __device__ __forceinline__ void nbuild_atom(const NbArgs& A, const GridParams& g
     bool mi[3] = {false, false, false};
     for (int a = 0; a < g.dim; ++a) mi[a] = g.periodic[a] && g.dom_n[a] <= 2;
     const bool prefilter = uniform_rns && grid_whole(g);
-    const int own[3] = {cx, cy, cz};
-    const double xi = A.rx[i], yi = A.ry[i], zi = A.rz[i], rni = A.rns[i];
-    const float4 oi = A.o0[i];
     const uint32_t origi = A.orig[i];
     const bool pfi = prefilter && oi.w == 0.0f;
     int cnt = 0;
@@ -356,11 +374,11 @@ __device__ __forceinline__ void nbuild_atom(const NbArgs& A, const GridParams& g
                     if (g.dom_n[2] == 1 && z != 0) continue;
                     if (g.dom_n[2] == 2 && z == 1) continue;
                 }
-                const int dl[3] = {x, y, z};
                 int lc[3];
                 bool inside = true;
                 for (int a = 0; a < 3; ++a) {
-                    int nb = gc[a] + dl[a];  // |dl| <= 1: one period at most
+                    // the walk's cell is within one cell of the grid, so one period at most
+                    int nb = gc[a] + (a == 0 ? x : a == 1 ? y : z);
                     if (g.periodic[a]) nb = nb < 0 ? nb + g.dom_n[a] : nb >= g.dom_n[a] ? nb - g.dom_n[a] : nb;
                     lc[a] = nb - g.offset[a];
                     inside = inside && lc[a] >= 0 && lc[a] < g.num[a];
@@ -368,8 +386,9 @@ __device__ __forceinline__ void nbuild_atom(const NbArgs& A, const GridParams& g
                 if (!inside) continue;
                 const int bk = bin_key(g, lc[0], lc[1], lc[2]);
                 const uint32_t j0 = A.bin_start[bk], j1 = A.bin_start[bk + 1];
-                // image of the neighbour cell relative to this cell
-                const float sh[3] = {(float)x * g.csf[0], (float)y * g.csf[1], (float)z * g.csf[2]};
+                // image of the neighbour cell relative to the binned cell
+                const int dl[3] = {x + shift[0], y + shift[1], z + shift[2]};
+                const float sh[3] = {(float)dl[0] * g.csf[0], (float)dl[1] * g.csf[1], (float)dl[2] * g.csf[2]};
                 for (uint32_t j = j0; j < j1; ++j) {
                     if (j == i) continue;
                     if (A.half && A.orig[j] < origi) continue;

@@ -214,6 +214,11 @@ __device__ __noinline__ bool solo_rebuild(const SoloArgs& S, GridParams& g, doub
             // a few cells of many atoms: a thread per atom
             for (int i = t; i < n; i += NT) nbuild_atom(S.N, g, (uint32_t)i, uniform);
         }
+        __syncthreads();
+        // atoms clamped into the grid: their own lists from their unclamped cells
+        if (!g.small_box && (S.st->build_flags & FLAG_RANGE))
+            for (int i = t; i < n; i += NT)
+                if (S.N.o0[i].w == 2.0f) nbuild_atom(S.N, g, (uint32_t)i, uniform);
     }
     __syncthreads();
     for (int i = t; i < n; i += NT) trig_one(i, S.saved_rns, S.saved_rcut, g, S.trig);
