@@ -443,6 +443,15 @@ __device__ __forceinline__ bool eam_mixed_force(const FArgs& A, const PotSet* __
     int Nr1 = P->Nr1;
     const float4* rv = P->rv_c;
     Kahan3 acc;
+    // Multi: F' of atom i for the kinds 1..3 of its partners, read once (the
+    // density pass's Fp32 rows; kind 0's is the record's w, the same bits)
+    float fpi1 = 0.f, fpi2 = 0.f, fpi3 = 0.f;
+    if (MULTI) {
+        const int nk = ps->nkinds;
+        if (nk > 1) fpi1 = A.Fp32[A.np + i];
+        if (nk > 2) fpi2 = A.Fp32[2 * (size_t)A.np + i];
+        if (nk > 3) fpi3 = A.Fp32[3 * (size_t)A.np + i];
+    }
     const uint4* row = reinterpret_cast<const uint4*>(A.nbr) + i;
     uint4 e4n = ng > 0 ? ldg_list(row) : make_uint4(0, 0, 0, 0);
     for (int g = 0; g < ng; ++g) {
@@ -467,8 +476,9 @@ __device__ __forceinline__ bool eam_mixed_force(const FArgs& A, const PotSet* __
                 eam = P->type == POT_EAM || P->type == POT_TAB;
                 lj = P->type == POT_LJCUT || P->type == POT_LJS;
                 r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; rv = P->rv_c; R2c = P->R2cut;
-                Fpj = A.Fp32[(size_t)ki * A.np + j];
-                Fpi = A.Fp32[(size_t)kj * A.np + i];
+                // j's F' for i's kind (kind 0's is in j's record)
+                if (ki != 0) Fpj = A.Fp32[(size_t)ki * A.np + j];
+                Fpi = kj == 0 ? Fpi : kj == 1 ? fpi1 : kj == 2 ? fpi2 : fpi3;
             }
             float dx, dy, dz;
             pair_vec32(e[q], pi, pj[q], uf, dx, dy, dz);
