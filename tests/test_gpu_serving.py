@@ -213,7 +213,7 @@ def test_first_list_overflow_takes_checked_path():
     s.close()
 
 
-@pytest.mark.parametrize("threads", [256, 512, 1024])
+@pytest.mark.parametrize("threads", [256, 512, 640, 768, 896, 1024])
 def test_fused_block_loop_matches_graph_loop(threads):
     """The fused one-block loop (every pass of every step, rebuilds included,
     in one block per system) gives the same bits as the graph loop, for LJ
