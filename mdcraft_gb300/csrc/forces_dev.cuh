@@ -421,7 +421,10 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
         if (b == 0) Fp0 = dF;
         if (MULTI) A.Fp32[(size_t)b * A.np + i] = dF;
     }
-    A.pos32b[i] = make_int4(pi.x, pi.y, pi.z, __float_as_int(Fp0));
+    // Multi: the two lowest mantissa bits of F' (relative 2^-22, below the
+    // FP32 sums' own rounding) carry the atom's kind for the force pass
+    const int w = MULTI ? ((__float_as_int(Fp0) & ~3) | ki) : __float_as_int(Fp0);
+    A.pos32b[i] = make_int4(pi.x, pi.y, pi.z, w);
 }
 
 // BITS: a pair in the 1e-5 band around the cutoff takes the density pass's
@@ -444,7 +447,8 @@ __device__ __forceinline__ bool eam_mixed_force(const FArgs& A, const PotSet* __
     const float4* rv = P->rv_c;
     Kahan3 acc;
     // Multi: F' of atom i for the kinds 1..3 of its partners, read once (the
-    // density pass's Fp32 rows; kind 0's is the record's w, the same bits)
+    // density pass's Fp32 rows; kind 0's is the record's w, with the atom's
+    // kind in its two lowest bits)
     float fpi1 = 0.f, fpi2 = 0.f, fpi3 = 0.f;
     if (MULTI) {
         const int nk = ps->nkinds;
@@ -465,11 +469,11 @@ __device__ __forceinline__ bool eam_mixed_force(const FArgs& A, const PotSet* __
         float fx = 0.f, fy = 0.f, fz = 0.f;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            float Fpi = __int_as_float(pi.w), Fpj = __int_as_float(pj[q].w);
+            float Fpi = __int_as_float(MULTI ? pi.w & ~3 : pi.w), Fpj = __int_as_float(MULTI ? pj[q].w & ~3 : pj[q].w);
             bool eam = true, lj = false;
             if (MULTI) {
                 uint32_t j = e[q] & kJMask;
-                int kj = A.kind[j] & 3;
+                const int kj = pj[q].w & 3;
                 P = &ps->p[ki][kj];
                 // a tabulated Pair has zero rho rows: the EAM arithmetic
                 // below reduces to its pair term exactly
