@@ -210,7 +210,7 @@ __device__ __forceinline__ bool lj_mixed_force(const FArgs& A, const PotSet* __r
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             if (MULTI) {
-                const PotParams& P = ps->p[ki][A.kind[e[q] & kJMask] & 3];
+                const PotParams& P = ps->p[ki][pj[q].w & 3];
                 r2c = P.r2cut_f; l1 = P.lj1_f; l2 = P.lj2_f; mh = P.mhf_f; R2c = P.R2cut;
             }
             float dx, dy, dz;
@@ -300,7 +300,7 @@ __device__ __forceinline__ bool pair_mixed_force(const FArgs& A, const PotSet* _
         float fx = 0.f, fy = 0.f, fz = 0.f;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const PotParams& P = ps->p[ki][MULTI ? (A.kind[e[q] & kJMask] & 3) : 0];
+            const PotParams& P = ps->p[ki][MULTI ? (pj[q].w & 3) : 0];
             float dx, dy, dz;
             pair_vec32(e[q], pi, pj[q], uf, dx, dy, dz);
             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
@@ -382,7 +382,7 @@ __device__ __forceinline__ void density_mixed_one(const FArgs& A, const PotSet* 
             for (int q = 0; q < 4; ++q) {
                 bool eam = true;
                 if (MULTI) {
-                    P = &ps->p[ki][A.kind[e[q] & kJMask] & 3];
+                    P = &ps->p[ki][pj[q].w & 3];  // the partner's kind rides in its offsets' w
                     r2c = P->r2cut_f; idr = P->inv_dr_f; Nr1 = P->Nr1; tab = P->rho_c; R2c = P->R2cut;
                     eam = P->type == 2;
                 }

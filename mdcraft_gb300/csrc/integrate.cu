@@ -87,10 +87,11 @@ __global__ void k_trig(int n, const double* __restrict__ saved_rns, const double
 __global__ void k_offsets(int n, const double* __restrict__ rx, const double* __restrict__ ry,
                           const double* __restrict__ rz, const double* __restrict__ Rx,
                           const double* __restrict__ Ry, const double* __restrict__ Rz, double ux, double uy,
-                          double uz, int4* __restrict__ pos32) {
+                          double uz, int4* __restrict__ pos32, const uint16_t* __restrict__ kind) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    pos32[i] = make_int4(off_encode(rx[i] - Rx[i], ux), off_encode(ry[i] - Ry[i], uy), off_encode(rz[i] - Rz[i], uz), 0);
+    pos32[i] = make_int4(off_encode(rx[i] - Rx[i], ux), off_encode(ry[i] - Ry[i], uy), off_encode(rz[i] - Rz[i], uz),
+                         kind[i] & 3);
 }
 
 // FP32 -> FP64 force copy after a mixed stage, so downloads and a later
@@ -219,6 +220,7 @@ IArgs integrator_args(mdg_system* sys, double dt) {
     A.gx = sys->f32[0][c]; A.gy = sys->f32[1][c]; A.gz = sys->f32[2][c];
     A.m = sys->f64[MASS][c];
     A.tag = sys->u16[TAG][c];
+    A.kind = sys->u16[KIND][c];
     A.rcut = sys->f64[RCUT][c];
     A.rns = sys->f64[RNS][c];
     A.uid = sys->u32[UID][c];
@@ -299,7 +301,7 @@ int launch_offsets(mdg_system* sys) {
     k_offsets<<<nblk(sys->n), kBlock, 0, sys->ctx->stream>>>((int)sys->n, sys->f64[RX][c], sys->f64[RY][c],
                                                              sys->f64[RZ][c], sys->Rc[0], sys->Rc[1], sys->Rc[2],
                                                              sys->grid.inv_u[0], sys->grid.inv_u[1],
-                                                             sys->grid.inv_u[2], sys->pos32);
+                                                             sys->grid.inv_u[2], sys->pos32, sys->u16[KIND][c]);
     MDG_LAUNCHED(sys->ctx);
     return MDG_OK;
 }

@@ -21,6 +21,7 @@ struct IArgs {
     const float *gx, *gy, *gz;
     const double* m;
     const uint16_t* tag;
+    const uint16_t* kind;  // w of the fixed-point offsets (pos32): the atom's kind
     double* rcut;
     const double* rns;
     const uint32_t* uid;
@@ -113,7 +114,7 @@ __device__ __forceinline__ bool drift64_one(const IArgs& A, int i, int drift, in
 __device__ __forceinline__ bool offsets_check_mixed(const IArgs& A, int i, const double r[3]) {
     const int4 q = make_int4(off_encode(r[0] - __ldcs(A.Rx + i), A.inv_u[0]),
                              off_encode(r[1] - __ldcs(A.Ry + i), A.inv_u[1]),
-                             off_encode(r[2] - __ldcs(A.Rz + i), A.inv_u[2]), 0);
+                             off_encode(r[2] - __ldcs(A.Rz + i), A.inv_u[2]), __ldcs(A.kind + i) & 3);
     A.pos32[i] = q;
     const int4 p = __ldcs(A.q0 + i);
     const float dx = __int2float_rn((int)((uint32_t)q.x - (uint32_t)p.x)) * A.uf[0];

@@ -218,11 +218,12 @@ __global__ void k_cells(int n, const double* __restrict__ rx, const double* __re
                         const double* __restrict__ rz, const GridParams* __restrict__ gp,
                         uint32_t* __restrict__ cellp, double* __restrict__ Rx, double* __restrict__ Ry,
                         double* __restrict__ Rz, int4* __restrict__ pos32, int4* __restrict__ q0, float4* __restrict__ o0,
-                        const uint32_t* __restrict__ orig, uint32_t* __restrict__ slot_of) {
+                        const uint32_t* __restrict__ orig, uint32_t* __restrict__ slot_of,
+                        const uint16_t* __restrict__ kind) {
     const GridParams g = *gp;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || g.empty) return;
-    cells_one(g, i, rx, ry, rz, cellp, Rx, Ry, Rz, pos32, q0, o0, orig, slot_of);
+    cells_one(g, i, rx, ry, rz, cellp, Rx, Ry, Rz, pos32, q0, o0, orig, slot_of, kind);
 }
 
 // ---------------------------------------------------------------------------
@@ -735,7 +736,7 @@ int nlist_enqueue(mdg_system* sys) {
     }
     k_cells<<<nblk(n), kBlock, 0, st>>>(n, sys->f64[RX][c], sys->f64[RY][c], sys->f64[RZ][c], sys->dgrid,
                                         sys->cellp, sys->Rc[0], sys->Rc[1], sys->Rc[2], sys->pos32, sys->q0, sys->o0,
-                                        sys->u32[ORIG][c], sys->slot_of);
+                                        sys->u32[ORIG][c], sys->slot_of, sys->u16[KIND][c]);
     MDG_LAUNCHED(ctx);
     NbArgs A = nb_args(sys);
     // a half warp per bin of the capacity (a whole warp where cells hold more

@@ -202,7 +202,7 @@ __device__ __forceinline__ void bin_sort_one(int b, const uint32_t* start, uint3
 __device__ __forceinline__ void cells_one(const GridParams& g, int i, const double* rx, const double* ry,
                                           const double* rz, uint32_t* cellp, double* Rx, double* Ry, double* Rz,
                                           int4* pos32, int4* q0, float4* o0, const uint32_t* orig,
-                                          uint32_t* slot_of) {
+                                          uint32_t* slot_of, const uint16_t* kind) {
     double r[3] = {rx[i], ry[i], rz[i]};
     int c[3];
     bool cl;
@@ -222,7 +222,7 @@ __device__ __forceinline__ void cells_one(const GridParams& g, int i, const doub
     Rx[i] = R[0];
     Ry[i] = R[1];
     Rz[i] = R[2];
-    pos32[i] = make_int4(q[0], q[1], q[2], 0);
+    pos32[i] = make_int4(q[0], q[1], q[2], kind[i] & 3);  // w: the atom's kind (Multi passes)
     q0[i] = make_int4(q[0], q[1], q[2], 0);
     // w: 0 exact offsets; 1 not exact (the FP32 tests send its pairs to FP64);
     // 2 clamped into the grid (also not exact: its list is walked from the

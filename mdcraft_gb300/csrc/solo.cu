@@ -199,7 +199,7 @@ __device__ __noinline__ bool solo_rebuild(const SoloArgs& S, GridParams& g, doub
     copy_back_block<NT>(S.G, n);
     __syncthreads();
     for (int i = t; i < n; i += NT)
-        cells_one(g, i, S.rx, S.ry, S.rz, S.cellp, S.Rx, S.Ry, S.Rz, S.pos32, S.q0, S.o0, S.orig, S.slot_of);
+        cells_one(g, i, S.rx, S.ry, S.rz, S.cellp, S.Rx, S.Ry, S.Rz, S.pos32, S.q0, S.o0, S.orig, S.slot_of, S.F.kind);
     __syncthreads();
     {
         const bool uniform = S.st->nonuniform == 0;
@@ -310,7 +310,7 @@ __device__ __noinline__ bool solo_setup(const SoloArgs& S, GridParams& g, double
     if (!solo_rebuild<NT>(S, g, red, scan_sh)) return false;
     for (int i = t; i < n; i += NT)
         S.pos32[i] = make_int4(off_encode(S.rx[i] - S.Rx[i], g.inv_u[0]), off_encode(S.ry[i] - S.Ry[i], g.inv_u[1]),
-                               off_encode(S.rz[i] - S.Rz[i], g.inv_u[2]), 0);
+                               off_encode(S.rz[i] - S.Rz[i], g.inv_u[2]), S.F.kind[i] & 3);
     for (int i = t; i < n; i += NT) solo_zero_one(S, i);
     __syncthreads();
     for (int i = t; i < n; i += NT) drift64_one(S.I, i, 0, 0);
