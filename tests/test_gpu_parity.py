@@ -302,6 +302,10 @@ FORCE_CASES = [
     ("lj_argon", lambda: W.lj_argon_fcc(jitter=0.01)),
     ("eam_cu", lambda: W.eam_cu_fcc(ncell=10)),
     ("nial_multi", lambda: W.eam_nial_b2(ncell=8)),
+    # 2 cells per periodic axis (the per-atom list build with its minimum
+    # image), box edges still above 2 rns
+    ("eam_cu_2cells", lambda: W.eam_cu_fcc(ncell=4)),
+    ("lj_argon_2cells", lambda: W.lj_argon_fcc(ncell=4, jitter=0.01)),
 ]
 
 
