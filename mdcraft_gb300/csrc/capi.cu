@@ -1680,6 +1680,19 @@ static int check_ready(mdg_solver* s, mdg_system* sys, PotSet* ps, bool need_lis
         set_error("no Verlet list: call mdg_nlist_update first");
         return MDG_ERR_STATE;
     }
+    // The mixed form takes each pair's minimum image. The Periodic boundary's
+    // ghost pass (boundary/periodic.cxx:36-102) gives that image only when
+    // every periodic box edge is at least 2 rns; in a smaller box the
+    // reference keeps a listed pair's raw difference inside rns.
+    if (s->precision == MDG_PREC_MIXED && s->periodic && sys->have_list && sys->n) {
+        const GridParams& g = sys->grid;
+        for (int a = 0; a < g.dim; ++a)
+            if (g.periodic[a] && g.size[a] < 2.0 * g.max_rns) {
+                set_error("the mixed form needs every periodic box edge to be at least 2 rns (its minimum images "
+                          "are the Periodic boundary's only then); use the FP64 form for this box");
+                return MDG_ERR_STATE;
+            }
+    }
     MDG_CUDA(cudaSetDevice(sys->ctx->device));
     if (s->multi) {
         for (int i = 0; i < s->nkinds; ++i)

@@ -733,6 +733,19 @@ int mdg_server_submit(mdg_server* srv, mdg_solver* solver, const mdg_domain* dom
         set_error("request larger than the server's max_atoms");
         return MDG_ERR_INVALID;
     }
+    if (solver->precision == MDG_PREC_MIXED && solver->periodic && n) {
+        // as the mixed stages require: every periodic box edge at least 2 rns
+        double mr = 0.0;
+        for (size_t k = 0; k < n; ++k) mr = std::max(mr, atoms[k].rns);
+        for (int a = 0; a < 3; ++a) {
+            const double L = domain->bmax[a] - domain->bmin[a];
+            if (domain->periodic[a] && L > 0.0 && L < 2.0 * mr) {
+                set_error("the mixed form needs every periodic box edge to be at least 2 rns; use an FP64 solver "
+                          "for this request");
+                return MDG_ERR_INVALID;
+            }
+        }
+    }
     size_t fp = footprint_of(n, neighbours_of(*domain, atoms, n));
     if (fp > srv->budget) {
         set_error("request footprint exceeds the server's device-memory budget");

@@ -338,6 +338,33 @@ def test_fp64_forces_energies_match_oracle(case):
         assert mg[key] == pytest.approx(mo[key], rel=FP64_REL, abs=1e-300)
 
 
+def test_box_below_two_rns_fp64_follows_ghost_pass_mixed_refused():
+    """A periodic box shorter than 2 rns (LJ argon, 3 fcc cells per axis:
+    1.58 nm against rns 0.88 nm). The FP64 form follows the reference's
+    Periodic ghost pass, so its forces match the oracle's; the mixed form,
+    whose minimum images equal that pass only for edges of at least 2 rns,
+    refuses the box."""
+    atoms, box, per, p = W.lj_argon_fcc(ncell=3, jitter=0.01)
+    assert box[1] - box[0] < 2.0 * float(atoms["rns"][0])
+    o, g = H.make_pair(atoms, box, (1, 1, 1), p, precision="fp64")
+    o["nl"].update(-1.0)
+    g["nl"].update(-1.0)
+    o["solver"].prepare(o["atoms"])
+    o["solver"].stages(o["atoms"], o["nl"])
+    g["solver"].prepare(g["sys"])
+    g["solver"].stages(g["sys"])
+    fo = o["atoms"]["f"]
+    fg = g["sys"].download()["f"]
+    scale = np.sqrt(np.mean(np.sum(fo ** 2, axis=1)))
+    assert scale > 0.0
+    assert np.max(np.abs(fg - fo)) <= FP64_REL * scale
+    _, gm = H.make_pair(atoms, box, (1, 1, 1), p, precision="mixed")
+    gm["nl"].update(-1.0)
+    with pytest.raises(RuntimeError, match="2 rns"):
+        gm["solver"].prepare(gm["sys"])
+        gm["solver"].stages(gm["sys"])
+
+
 @pytest.mark.parametrize("case", FORCE_CASES, ids=lambda c: c[0])
 def test_mixed_forces_within_tolerance(case):
     atoms, box, per, p = case[1]()

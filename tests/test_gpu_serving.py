@@ -324,3 +324,21 @@ def test_balanced_order_promotes_the_largest_on_the_tail():
     # on this stream the rule is neither arrival order nor largest-first
     assert order[2:] != sorted(order[2:])
     assert [works[k] for k in order[2:]] != sorted((works[k] for k in order[2:]), reverse=True)
+
+
+def test_mixed_request_in_a_box_below_two_rns_is_refused():
+    """A periodic box shorter than 2 rns: a mixed-precision request is
+    refused at submission (the mixed form's minimum images are the Periodic
+    boundary's only for edges of at least 2 rns); an FP64 one runs."""
+    _ensure_built()
+    atoms, box, _, p = W.lj_argon_fcc(ncell=3, jitter=0.01)
+    dom = SV.periodic_domain(box)
+    srv = mdg.Server(slots=1, max_atoms=4096)
+    with pytest.raises(RuntimeError, match="2 rns"):
+        srv.submit(SV.solvers("mixed")["lj"], dom, atoms, p["dt"], 10)
+    s64 = SV.solvers("fp64")
+    rid = srv.submit(s64["lj"], dom, atoms, p["dt"], 10)
+    srv.wait(rid, 120.0)
+    _, info = srv.result(rid, atoms=False)
+    assert info["status"] == 0
+    srv.close()
