@@ -1,9 +1,9 @@
 """Project autotuner: launch shapes chosen by measuring them on the workload.
 
-Serving: the threads of the fused per-request block (256, 512 or 1024; the
-block count follows from occupancy) are timed on a sample of the request
-stream itself, each candidate on the same sample through its own server, and
-the fastest is kept.
+Serving: the threads of the fused per-request block (512, 640, 768, 896 or
+1024; the block count follows from occupancy) are timed on a sample of the
+request stream itself, each candidate on the same sample through its own
+server, and the one with the highest saturated throughput is kept.
 
 A system's step kernels (`tune_shapes`): the cells per block of the list
 build (2, 4 or 8 warps, a cell each) are timed on the system's own rebuilds
