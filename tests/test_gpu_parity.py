@@ -273,6 +273,10 @@ def _cases():
 @pytest.mark.parametrize("case", _cases(), ids=lambda c: c[0])
 def test_neighbour_sets_bit_identical(case):
     name, atoms, box, per, _ = case
+    _sets_match_oracle(atoms, box, per)
+
+
+def _sets_match_oracle(atoms, box, per):
     do, dg = H.domains(box, per)
     ao = H.to_oracle_atoms(atoms)
     nlo = R.VerletList(ao, do, threads=R.hardware_threads())
@@ -298,6 +302,31 @@ def test_half_list_matches_oracle():
 
 
 # ---- forces / energies ------------------------------------------------------
+def _slab(made, keep_below, z_lo, z_hi):
+    """A slab of a periodic workload: periodic in x and y, open in z, the
+    atoms below keep_below·L kept, the domain's z extent [z_lo, z_hi]·L.
+    Atoms above z_hi·L lie outside the domain on the open axis (binned into
+    the top cell, their lists walked from the cell above it); atoms below
+    z_lo·L extend the grid below the domain (a negative grid offset)."""
+    atoms, box, _, p = made
+    L = box[1] - box[0]
+    a = atoms[atoms["r"][:, 2] < box[4] + keep_below * L].copy()
+    return a, (box[0], box[1], box[2], box[3], box[4] + z_lo * L, box[4] + z_hi * L), (1, 1, 0), p
+
+
+def _cluster(made, radius):
+    """A sphere of radius·L cut from a periodic workload, in an open box."""
+    atoms, box, _, p = made
+    L = box[1] - box[0]
+    c = np.array([box[0], box[2], box[4]]) + 0.5 * L
+    a = atoms[np.linalg.norm(atoms["r"] - c, axis=1) < radius * L].copy()
+    return a, box, (0, 0, 0), p
+
+
+def _axes(per):
+    return (1, 1, 1) if per is True else per
+
+
 FORCE_CASES = [
     ("lj_argon", lambda: W.lj_argon_fcc(jitter=0.01)),
     ("eam_cu", lambda: W.eam_cu_fcc(ncell=10)),
@@ -306,13 +335,28 @@ FORCE_CASES = [
     # image), box edges still above 2 rns
     ("eam_cu_2cells", lambda: W.eam_cu_fcc(ncell=4)),
     ("lj_argon_2cells", lambda: W.lj_argon_fcc(ncell=4, jitter=0.01)),
+    # free surfaces on an open axis, with atoms outside the domain on both
+    # sides of it (2,400 atoms, 200 above the domain's top)
+    ("eam_cu_slab", lambda: _slab(W.eam_cu_fcc(ncell=10), 0.6, 0.05, 0.55)),
+    ("lj_argon_slab", lambda: _slab(W.lj_argon_fcc(jitter=0.01), 0.6, 0.0, 0.55)),
+    # Multi: 3 periodic cells per axis in x and y, one open cell in z
+    ("nial_slab", lambda: _slab(W.eam_nial_b2(ncell=8), 0.6, 0.0, 0.55)),
+    # a 1,088-atom Cu nanoparticle in an open box
+    ("eam_cu_cluster", lambda: _cluster(W.eam_cu_fcc(ncell=10), 0.4)),
 ]
+
+
+@pytest.mark.parametrize("case", [c for c in FORCE_CASES if c[0].endswith(("_slab", "_cluster"))],
+                         ids=lambda c: c[0])
+def test_neighbour_sets_bit_identical_open_axis(case):
+    atoms, box, per, _ = case[1]()
+    _sets_match_oracle(atoms, box, per)
 
 
 @pytest.mark.parametrize("case", FORCE_CASES, ids=lambda c: c[0])
 def test_fp64_forces_energies_match_oracle(case):
     atoms, box, per, p = case[1]()
-    o, g = H.make_pair(atoms, box, (1, 1, 1), p, precision="fp64")
+    o, g = H.make_pair(atoms, box, _axes(per), p, precision="fp64")
     o["nl"].update(-1.0)
     g["nl"].update(-1.0)
     for so, ao, nl in [(o["solver"], o["atoms"], o["nl"])]:
@@ -368,7 +412,7 @@ def test_box_below_two_rns_fp64_follows_ghost_pass_mixed_refused():
 @pytest.mark.parametrize("case", FORCE_CASES, ids=lambda c: c[0])
 def test_mixed_forces_within_tolerance(case):
     atoms, box, per, p = case[1]()
-    o, g = H.make_pair(atoms, box, (1, 1, 1), p, precision="mixed")
+    o, g = H.make_pair(atoms, box, _axes(per), p, precision="mixed")
     o["nl"].update(-1.0)
     g["nl"].update(-1.0)
     o["solver"].prepare(o["atoms"])
