@@ -347,7 +347,10 @@ int mdg_measure_static(const double* d_m, const double* d_v, const double* d_Ep,
                        const double* d_V, size_t n, double* d_out, void* stream);
 /* Error/diagnostic flags accumulated on the device since the last call
  * (bit 0 atom out of grid, bit 1 neighbour overflow, bit 2 EAM table range,
- * bit 3 non-finite force); clears them. */
+ * bit 3 non-finite force, bit 4 a listed pair whose image lies more than one
+ * cell from the atom's cell: the mixed form's pair vector cannot express it.
+ * Bit 4 is a guard: a listed pair is within rns, which is at most one cell
+ * edge, so it is not raised by any input); clears them. */
 int mdg_system_flags(mdg_system* sys, uint32_t* flags);
 
 /* ---- serving: continuous batching of independent systems ------------------------

@@ -287,6 +287,8 @@ def _sets_match_oracle(atoms, box, per):
     assert H.same_sets(nlo.lists(), nlg.lists()) == 0
     # wrapped positions identical too (fit_in_period at the rebuild)
     assert np.array_equal(s.positions(), ao["r"])
+    # every listed pair's image within one cell (the mixed pair vectors)
+    assert not s.flags() & 16
 
 
 def test_half_list_matches_oracle():
