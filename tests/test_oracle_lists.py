@@ -1,0 +1,82 @@
+"""CPU check of the oracle's Verlet lists against a brute-force pair search
+(no GPU).
+
+The reference's list (VerletList::build_linked_cells and are_neibs,
+mdcraft/neibs/verlet-list.cxx:306-400, over Grid::adjacent_cells,
+mdcraft/neibs/grid.cxx:138-207) walks the 27 neighbour cells, or fewer on
+periodic axes of one or two cells, and takes the minimum image only for edge
+cells. When every atom lies inside the grid and every periodic edge is at
+least 2 max(rns), that walk must find exactly the pairs whose nearest-image
+distance satisfies d^2 <= max(rns_i, rns_j)^2, self included. A half list
+keeps the j >= i of them (verlet-list.cxx:345). The brute-force search
+below states that set directly over all pairs.
+"""
+import numpy as np
+import pytest
+
+from mdcraft_gb300 import workloads as W
+from oracle import mdref as R
+
+
+def _oracle_atoms(k):
+    a = np.zeros(len(k), dtype=R.ATOM_DTYPE)
+    a.view(np.uint8)[:] = np.ascontiguousarray(k).view(np.uint8)
+    return a
+
+
+def _brute(a, box, per):
+    r, rns = a["r"], a["rns"]
+    L = np.array([box[1] - box[0], box[3] - box[2], box[5] - box[4]])
+    out = []
+    for i in range(len(a)):
+        d = r - r[i]
+        for k in range(3):
+            if per[k]:
+                d[:, k] -= L[k] * np.round(d[:, k] / L[k])
+        d2 = (d * d).sum(axis=1)
+        out.append(set(np.nonzero(d2 <= np.maximum(rns, rns[i]) ** 2)[0].tolist()))
+    return out
+
+
+def _gas(n=1500, edge=5.0, seed=11):
+    rng = np.random.default_rng(seed)
+    g = R.new_atoms(n)
+    g["r"] = rng.random((n, 3)) * edge
+    g["rns"] = 0.3 + 0.2 * rng.random(n)
+    g["rcut"] = 0.25
+    g["m"] = 1.0
+    return g, (0.0, edge, 0.0, edge, 0.0, edge)
+
+
+def _lattice(made):
+    atoms, box, _, _ = made
+    return _oracle_atoms(atoms), box
+
+
+CASES = [
+    ("lj_argon_3cells", lambda: _lattice(W.lj_argon_fcc(ncell=6, jitter=0.02)), (1, 1, 1)),
+    ("eam_cu_3cells", lambda: _lattice(W.eam_cu_fcc(ncell=6)), (1, 1, 1)),
+    ("eam_cu_2cells", lambda: _lattice(W.eam_cu_fcc(ncell=4)), (1, 1, 1)),
+    ("nial_b2_3cells", lambda: _lattice(W.eam_nial_b2(ncell=8)), (1, 1, 1)),
+    ("gas_mixed_rns_open", _gas, (0, 0, 0)),
+    ("gas_mixed_rns_periodic", _gas, (1, 1, 1)),
+    ("gas_mixed_rns_slab", _gas, (1, 1, 0)),
+]
+
+
+@pytest.mark.parametrize("half", [False, True], ids=["full", "half"])
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c[0])
+def test_lists_equal_brute_force_pairs(case, half):
+    name, make, per = case
+    atoms, box = make()
+    d = R.Domain(*box)
+    for k in range(3):
+        if per[k]:
+            d.set_periodic(k, True)
+    nl = R.VerletList(atoms, d, threads=1, half=half)
+    nl.update(-1.0)
+    got = [set(map(int, x)) for x in nl.lists()]
+    want = _brute(atoms, box, per)
+    if half:
+        want = [{j for j in s if j >= i} for i, s in enumerate(want)]
+    assert got == want
