@@ -45,10 +45,19 @@ FIELDS = ["r", "v", "f", "V", "m", "rcut", "rns", "Ep", "Em", "nc", "bc", "kind"
 
 def test_atom_record_layouts_agree(tmp_path):
     """mdg_atom of the C-ABI, the C++ drop-in's mdcraft::data::Atom, the
-    binding's ATOM_DTYPE and the oracle's record place every field of
+    binding's ATOM_DTYPE, the Python drop-in's nested record
+    (mdcraft.data.Atoms) and the oracle's record place every field of
     mdcraft/data/atom.h:21-40 at the same byte offset, 208 bytes in all."""
     import shutil
     import subprocess
+    import sys
+
+    dropin = os.path.join(ROOT, "mdcraft_gb300", "dropin")
+    sys.path.insert(0, dropin)
+    try:
+        from mdcraft.data import ATOM as DROPIN_ATOM
+    finally:
+        sys.path.remove(dropin)
 
     import mdcraft_gb300 as mdg
     from oracle import mdref as R
@@ -77,4 +86,5 @@ def test_atom_record_layouts_agree(tmp_path):
         want = mdg.ATOM_DTYPE.fields[name][1]
         assert got[name] == (want, want), name
         assert R.ATOM_DTYPE.fields[name][1] == want, name
-    assert mdg.ATOM_DTYPE.itemsize == R.ATOM_DTYPE.itemsize == 208
+        assert DROPIN_ATOM.fields[name][1] == want, name
+    assert mdg.ATOM_DTYPE.itemsize == R.ATOM_DTYPE.itemsize == DROPIN_ATOM.itemsize == 208
