@@ -80,3 +80,32 @@ def test_lists_equal_brute_force_pairs(case, half):
     if half:
         want = [{j for j in s if j >= i} for i, s in enumerate(want)]
     assert got == want
+
+
+@pytest.mark.parametrize("half", [False, True], ids=["full", "half"])
+def test_lists_equal_brute_force_pairs_random_boxes(half):
+    """60 seeded random systems: 2 to 400 atoms, rns in [0.2, 0.5], box edges
+    in [1, 4] (at least 2 max(rns), so 2 to 8 cells per axis), and each
+    axis periodic or open at random."""
+    rng = np.random.default_rng(123)
+    for _ in range(60):
+        n = int(rng.integers(2, 400))
+        per = tuple(int(x) for x in rng.integers(0, 2, 3))
+        edges = rng.uniform(1.0, 4.0, 3)
+        box = (0.0, edges[0], 0.0, edges[1], 0.0, edges[2])
+        a = R.new_atoms(n)
+        a["r"] = rng.random((n, 3)) * edges
+        a["rns"] = rng.uniform(0.2, 0.5, n)
+        a["rns"][0] = 0.5
+        a["rcut"] = 0.1
+        a["m"] = 1.0
+        d = R.Domain(*box)
+        for k in range(3):
+            if per[k]:
+                d.set_periodic(k, True)
+        nl = R.VerletList(a, d, threads=1, half=half)
+        nl.update(-1.0)
+        want = _brute(a, box, per)
+        if half:
+            want = [{j for j in s if j >= i} for i, s in enumerate(want)]
+        assert [set(map(int, x)) for x in nl.lists()] == want, (n, per, edges)
