@@ -109,3 +109,51 @@ def test_lists_equal_brute_force_pairs_random_boxes(half):
         if half:
             want = [{j for j in s if j >= i} for i, s in enumerate(want)]
         assert [set(map(int, x)) for x in nl.lists()] == want, (n, per, edges)
+
+
+def test_decide_is_the_half_skin_rule():
+    """VerletList::decide (mdcraft/neibs/verlet-list.cxx:110-158): a rebuild
+    is due when some atom moved, by the nearest periodic image, more than
+    half its skin (rns - rcut) since the last update, or changed its uid,
+    rcut or rns. Random displacements near the threshold, some of them
+    wrapped back across a periodic face (which is no motion), on 200 trials."""
+    rng = np.random.default_rng(5)
+    L = np.array([3.0, 3.0, 3.0])
+    box = (0.0, 3.0, 0.0, 3.0, 0.0, 3.0)
+    for trial in range(200):
+        n = 50
+        a = R.new_atoms(n)
+        a["r"] = rng.random((n, 3)) * L
+        a["rns"] = rng.uniform(0.3, 0.5, n)
+        a["rcut"] = a["rns"] - rng.uniform(0.05, 0.2, n)
+        a["m"] = 1.0
+        a["uid"] = np.arange(1, n + 1)
+        d = R.Domain(*box)
+        per = (1, 1, trial % 2)
+        for k in range(3):
+            if per[k]:
+                d.set_periodic(k, True)
+        nl = R.VerletList(a, d, threads=1)
+        nl.update(-1.0)
+        r0 = a["r"].copy()
+        half = 0.5 * (a["rns"] - a["rcut"])
+        # each atom moves by a fraction of its half skin in a random direction
+        u = rng.normal(size=(n, 3))
+        u /= np.linalg.norm(u, axis=1)[:, None]
+        frac = rng.uniform(0.0, 0.999, n)
+        if trial % 4 == 1:
+            frac[rng.integers(n)] = rng.uniform(1.001, 1.5)
+        a["r"] = r0 + u * (frac * half)[:, None]
+        # wrap some coordinates back into the box on periodic axes: no motion
+        for k in range(3):
+            if per[k]:
+                a["r"][:, k] = np.where(rng.random(n) < 0.5, np.mod(a["r"][:, k], L[k]), a["r"][:, k])
+        dr = a["r"] - r0
+        for k in range(3):
+            if per[k]:
+                dr[:, k] -= L[k] * np.round(dr[:, k] / L[k])
+        want = bool(np.any((dr * dr).sum(axis=1) > half * half))
+        assert nl.decide() == want, trial
+        if trial % 10 == 0 and not want:
+            a["rns"][3] += 1e-12
+            assert nl.decide()
