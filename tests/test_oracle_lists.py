@@ -157,3 +157,39 @@ def test_decide_is_the_half_skin_rule():
         if trial % 10 == 0 and not want:
             a["rns"][3] += 1e-12
             assert nl.decide()
+
+
+def test_list_for_equals_brute_force_in_cubic_grids():
+    """VerletList::list_for (mdcraft/neibs/verlet-list.cxx:251-276) keeps the
+    atoms of the point's adjacent cells within max(cell_size, rns_j) of it,
+    cell_size being the largest cell edge (mdcraft/neibs/grid.h:116). In a
+    cube with equal cells every atom within that radius (nearest image on
+    periodic axes) lies in those cells, so the result is the brute-force
+    set: 40 random gases, periodic or open, 10 query points each."""
+    rng = np.random.default_rng(9)
+    for trial in range(40):
+        n = int(rng.integers(20, 500))
+        edge = rng.uniform(1.0, 4.0)
+        periodic = trial % 2 == 0
+        box = (0.0, edge, 0.0, edge, 0.0, edge)
+        a = R.new_atoms(n)
+        a["r"] = rng.random((n, 3)) * edge
+        a["rns"] = rng.uniform(0.2, 0.5, n)
+        a["rns"][0] = 0.5
+        a["rcut"] = 0.1
+        a["m"] = 1.0
+        d = R.Domain(*box)
+        if periodic:
+            for k in range(3):
+                d.set_periodic(k, True)
+        nl = R.VerletList(a, d, threads=1)
+        nl.update(-1.0)
+        radius = np.maximum(nl.grid().fields["cell_sizes"].max(), a["rns"])
+        lo, hi = a["r"].min(axis=0), a["r"].max(axis=0)
+        for _ in range(10):
+            x = lo + rng.random(3) * (hi - lo)
+            dd = a["r"] - x
+            if periodic:
+                dd -= edge * np.round(dd / edge)
+            want = set(np.nonzero((dd * dd).sum(axis=1) <= radius * radius)[0].tolist())
+            assert set(map(int, nl.list_for(x))) == want, (trial, x)
